@@ -1,0 +1,153 @@
+"""ctypes bindings of libfempar_gpu.so (declarations in include/fempar_gpu.h).
+
+The shared library is built in-tree by ``fempar_gb300.build``.  Loading fails
+loudly when it is missing: there is no CPU fallback for the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfempar_gpu.so")
+
+FG_OK = 0
+STATUS = {0: "FG_OK", -1: "FG_ERR_BADARG", -2: "FG_ERR_OOM", -3: "FG_ERR_CUDA", -4: "FG_ERR_NOT_CONVERGED",
+          -5: "FG_ERR_NUMERIC", -6: "FG_ERR_TIMEOUT", -7: "FG_ERR_UNSUPPORTED", -8: "FG_ERR_NO_DEVICE"}
+FG_ERR_NOT_CONVERGED = -4
+
+FG_POISSON, FG_ELASTICITY = 0, 1
+FG_FN_ZERO, FG_FN_CONST, FG_FN_SHARP_WAVE, FG_FN_LINEAR, FG_FN_QP_VALUES = 0, 1, 2, 3, 4
+FG_INPUTS_ON_DEVICE = 1
+FG_PREC_NONE, FG_PREC_JACOBI = 0, 1
+FG_FP64, FG_MIXED = 0, 1
+FG_RES_RES, FG_RES_RHS, FG_DELTA_RHS, FG_DELTA_DELTA, FG_RES_NRMGIVEN_RHS_NRMGIVEN, FG_RES_NRMGIVEN_RES_NRMGIVEN = range(6)
+
+# every symbol include/fempar_gpu.h declares
+EXPORTS = [
+    "fg_status_string", "fg_last_error", "fg_version",
+    "fg_ctx_create", "fg_ctx_destroy", "fg_ctx_memory",
+    "fg_mesh_create_structured", "fg_mesh_destroy",
+    "fg_space_create", "fg_space_destroy", "fg_space_get_info", "fg_space_get_dof_map",
+    "fg_space_get_dirichlet_coords",
+    "fg_assemble", "fg_system_reassemble", "fg_system_destroy",
+    "fg_system_export_csr", "fg_system_export_rhs", "fg_system_export_dirichlet_values",
+    "fg_system_spmv_device", "fg_solve", "fg_solve_device",
+    "fg_solver_params_default", "fg_integrand_default",
+]
+
+
+class Integrand(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("cell_coef", C.c_void_p),
+        ("coef_const", C.c_double),
+        ("nu", C.c_double),
+        ("source_fn", C.c_int),
+        ("fn_param", C.c_double * 8),
+        ("qp_source", C.c_void_p),
+        ("boundary_fn", C.c_int),
+        ("dirichlet_values", C.c_void_p),
+        ("flags", C.c_int),
+    ]
+
+
+class SolverParams(C.Structure):
+    _fields_ = [
+        ("precond", C.c_int),
+        ("precision", C.c_int),
+        ("criterion", C.c_int),
+        ("rtol", C.c_double),
+        ("atol", C.c_double),
+        ("max_iters", C.c_int),
+        ("inner_rtol", C.c_double),
+        ("inner_max_iters", C.c_int),
+        ("check_every", C.c_int),
+    ]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int),
+        ("outer_iterations", C.c_int),
+        ("converged", C.c_int),
+        ("error_estimate", C.c_double),
+        ("tolerance", C.c_double),
+        ("solve_ms", C.c_double),
+    ]
+
+
+class SpaceInfo(C.Structure):
+    _fields_ = [
+        ("num_dims", C.c_int), ("order", C.c_int), ("ncomp", C.c_int),
+        ("dofs_per_cell", C.c_int), ("qp_per_cell", C.c_int),
+        ("num_cells", C.c_int64), ("num_free", C.c_int64), ("num_dirichlet", C.c_int64),
+        ("nnz_full", C.c_int64), ("nnz_upper", C.c_int64),
+    ]
+
+
+class FGError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        msg = f"{where}: {STATUS.get(status, status)}"
+        try:
+            err = lib().fg_last_error().decode()
+            if err:
+                msg += f" ({err})"
+        except Exception:
+            pass
+        super().__init__(msg)
+
+
+_lib = None
+
+
+def lib():
+    """Load libfempar_gpu.so; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m fempar_gb300.build` "
+                          "(the GB300 path has no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_double
+    pp = C.POINTER(C.c_void_p)
+    sig = {
+        "fg_status_string": (C.c_char_p, [i32]),
+        "fg_last_error": (C.c_char_p, []),
+        "fg_version": (C.c_char_p, []),
+        "fg_ctx_create": (i32, [i32, C.c_uint64, pp]),
+        "fg_ctx_destroy": (i32, [vp]),
+        "fg_ctx_memory": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+        "fg_mesh_create_structured": (i32, [vp, i32, vp, vp, vp, pp]),
+        "fg_mesh_destroy": (i32, [vp]),
+        "fg_space_create": (i32, [vp, i32, i32, vp, i32, pp]),
+        "fg_space_destroy": (i32, [vp]),
+        "fg_space_get_info": (i32, [vp, C.POINTER(SpaceInfo)]),
+        "fg_space_get_dof_map": (i32, [vp, vp]),
+        "fg_space_get_dirichlet_coords": (i32, [vp, vp]),
+        "fg_assemble": (i32, [vp, C.POINTER(Integrand), pp]),
+        "fg_system_reassemble": (i32, [vp, C.POINTER(Integrand)]),
+        "fg_system_destroy": (i32, [vp]),
+        "fg_system_export_csr": (i32, [vp, i32, i32, vp, vp, vp]),
+        "fg_system_export_rhs": (i32, [vp, vp]),
+        "fg_system_export_dirichlet_values": (i32, [vp, vp]),
+        "fg_system_spmv_device": (i32, [vp, i32, vp, vp]),
+        "fg_solve": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
+        "fg_solve_device": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
+        "fg_solver_params_default": (None, [C.POINTER(SolverParams)]),
+        "fg_integrand_default": (None, [C.POINTER(Integrand)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status, where):
+    if status != FG_OK:
+        raise FGError(status, where)
+    return status

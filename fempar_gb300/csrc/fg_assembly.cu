@@ -1,0 +1,412 @@
+// fg_assembly.cu -- numeric phase: cell-batch integration and the deterministic,
+// atomic-free assembly of the global CSR matrix and right-hand side.
+//
+// Stage 1, k_integrate_poisson<P>: one warp per cell.  The warp computes the
+// trilinear Jacobian, its inverse and |det| at every Gauss point (reference:
+// sbm_cell_map.i90:245-369, invmtx in sbm_cell_integrator.i90:448-500), the physical
+// shape gradients grad(phi_a) = J^-T grad_ref(phi_a) (sbm_lagrangian_reference_fe.i90:
+// 1330-1342), the upper triangle of the element matrix (lanes own (a,b) pairs and
+// accumulate over the Gauss points; the lower triangle is its mirror, as the
+// reference's element matrix is exactly symmetric), the element vector, and the
+// strong-Dirichlet lifting elvec -= elmat(:,j) g_j in column order
+// (sbm_fe_cell_iterator.i90:1610-1637).  Element matrices go to an HBM buffer.
+// GB300's FP64 rate (about 1.25 TFLOP/s) makes this stage FP64-bound; the buffer's
+// extra HBM traffic costs a few milliseconds at cfg2 size.
+//
+// Stage 2, k_scatter_rows<P>: one warp per free row.  The row's node sits in at most
+// 8 cells; they are visited in increasing cell index, so every entry is summed in the
+// reference's order (COO appended cell by cell, stable sort, duplicates summed in
+// order -- base_sparse_matrix.f90:3469-3513,4121-4829), and the right-hand side entry
+// likewise (serial_scalar_array.f90:247-262).  Lanes own the row's (cell, column)
+// contributions of one cell at a time; the column position comes from a binary search
+// in the row's sorted columns staged in shared memory.  No atomics: the result is
+// identical run to run.  The FP32 copy of the values is written in the same pass.
+#include "fg_internal.h"
+
+namespace fg {
+
+struct AsmGeom {
+  int n[3];
+  int p;
+  int Ln[3];
+  int ncomp;
+};
+
+static AsmGeom make_geom(const fg_space* sp) {
+  AsmGeom g;
+  for (int d = 0; d < 3; ++d) { g.n[d] = sp->mesh->n[d]; g.Ln[d] = sp->Ln[d]; }
+  g.p = sp->order;
+  g.ncomp = sp->ncomp;
+  return g;
+}
+
+struct SourceSpec {
+  int fn;
+  double prm[8];
+  const double* qp;  // per-qp values
+};
+
+// tutorial_01 source f = -lap(atan(alpha(|x-c|-r))) (tutorial modules :395-458)
+__device__ double sharp_wave_source(const double* prm, const double* x) {
+  double alpha = prm[0], r = prm[1];
+  double alpha_2 = alpha * alpha, alpha_3 = alpha_2 * alpha;
+  double x_minus_xc_2 = (x[0] - prm[2]) * (x[0] - prm[2]);
+  double y_minus_yc_2 = (x[1] - prm[3]) * (x[1] - prm[3]);
+  double z_minus_zc_2 = (x[2] - prm[4]) * (x[2] - prm[4]);
+  double term1 = x_minus_xc_2 + y_minus_yc_2 + z_minus_zc_2;
+  double sqrt_term1 = sqrt(term1);
+  double term2 = sqrt_term1 - r;
+  double term2_2 = term2 * term2;
+  double a2t = alpha_2 * term2_2 + 1.0;
+  double denom1 = sqrt_term1 * a2t;
+  double denom2 = pow(term1, 1.5) * a2t;
+  double denom3 = term1 * a2t * a2t;
+  double dx2 = alpha / denom1 - (alpha * x_minus_xc_2) / denom2 - (2.0 * alpha_3 * x_minus_xc_2 * term2) / denom3;
+  double dy2 = alpha / denom1 - (alpha * y_minus_yc_2) / denom2 - (2.0 * alpha_3 * y_minus_yc_2 * term2) / denom3;
+  double dz2 = alpha / denom1 - (alpha * z_minus_zc_2) / denom2 - (2.0 * alpha_3 * z_minus_zc_2 * term2) / denom3;
+  return -dx2 - dy2 - dz2;
+}
+
+__device__ double boundary_value(int fn, const double* prm, const double* x) {
+  switch (fn) {
+    case FG_FN_CONST: return prm[0];
+    case FG_FN_LINEAR: return x[0] + x[1] + x[2];
+    case FG_FN_SHARP_WAVE: {
+      double dx = x[0] - prm[2], dy = x[1] - prm[3], dz = x[2] - prm[4];
+      return atan(prm[0] * (sqrt(dx * dx + dy * dy + dz * dz) - prm[1]));
+    }
+    default: return 0.0;
+  }
+}
+
+template <int P>
+struct PoissonShape {
+  static constexpr int NP1 = P + 1;
+  static constexpr int NN = NP1 * NP1 * NP1;
+  static constexpr int NQ = NN;
+  static constexpr int ND = NN;
+  static constexpr int NPAIR = ND * (ND + 1) / 2;
+  static constexpr int CH = P == 1 ? 2 : (P == 2 ? 12 : 16);  // pairs per lane per pass
+  static constexpr int WARPS = P == 1 ? 8 : (P == 2 ? 4 : 1);
+  // shared doubles per warp: xv, invj, fac, xq, fsrc, grads, elmat
+  static constexpr int SM_XV = 24, SM_INVJ = NQ * 9, SM_FAC = NQ, SM_XQ = NQ * 3, SM_F = NQ, SM_G = NQ * NN * 3,
+                       SM_EL = ND * ND;
+  static constexpr int SM_DOUBLES = SM_XV + SM_INVJ + SM_FAC + SM_XQ + SM_F + SM_G + SM_EL;
+  static constexpr int SM_INTS = ND;  // cell gids
+  // per-warp stride, rounded to 16 bytes so that the next warp's doubles stay aligned
+  // and the int tail of one warp never reaches into the next warp's region
+  static constexpr size_t SM_BYTES_WARP = ((size_t)SM_DOUBLES * 8 + SM_INTS * 4 + 15) / 16 * 16;
+};
+
+// upper-triangle pair index -> (a,b), row-packed
+__device__ __forceinline__ void pair_ab(int p, int nd, int& a, int& b) {
+  int row = 0, off = 0;
+  while (off + (nd - row) <= p) { off += nd - row; ++row; }
+  a = row;
+  b = row + (p - off);
+}
+
+template <int P>
+__global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
+    k_integrate_poisson(AsmGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
+                        const int32_t* __restrict__ latdof, const double* __restrict__ gvals,
+                        const double* __restrict__ coef, double coef_const, SourceSpec src,
+                        double* __restrict__ E, double* __restrict__ EV) {
+  using S = PoissonShape<P>;
+  constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND, NP1 = S::NP1;
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double* base = smem + (size_t)wib * (S::SM_BYTES_WARP / 8);
+  double* xv = base;
+  double* invj = xv + S::SM_XV;
+  double* fac = invj + S::SM_INVJ;
+  double* xq = fac + S::SM_FAC;
+  double* fsrc = xq + S::SM_XQ;
+  double* sg = fsrc + S::SM_F;
+  double* el = sg + S::SM_G;
+  int32_t* gid = (int32_t*)(el + S::SM_EL);
+
+  const int64_t c = (int64_t)blockIdx.x * S::WARPS + wib;
+  if (c >= ncells) return;
+  const int ci = (int)(c % g.n[0]);
+  const int cj = (int)((c / g.n[0]) % g.n[1]);
+  const int ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
+  const double kc = coef ? coef[c] : coef_const;
+
+  if (lane < 24) {
+    int k = lane / 3, l = lane % 3;
+    int64_t v = (int64_t)(ci + (k & 1)) + (int64_t)(g.n[0] + 1) * ((cj + ((k >> 1) & 1)) + (int64_t)(g.n[1] + 1) * (ck + ((k >> 2) & 1)));
+    xv[lane] = coords[v * 3 + l];
+  }
+  for (int s = lane; s < ND; s += 32) {
+    int ai = s % NP1, aj = (s / NP1) % NP1, ak = s / (NP1 * NP1);
+    int64_t L = (int64_t)(P * ci + ai) + (int64_t)g.Ln[0] * ((P * cj + aj) + (int64_t)g.Ln[1] * (P * ck + ak));
+    gid[s] = latdof[L];
+  }
+  __syncwarp();
+  // Jacobian, inverse, det and physical coordinates per Gauss point
+  for (int q = lane; q < NQ; q += 32) {
+    double J[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        double alpha = tb.gshg[(k * NQ + q) * 3 + j];
+        a0 = a0 + alpha * xv[k * 3 + 0];
+        a1 = a1 + alpha * xv[k * 3 + 1];
+        a2 = a2 + alpha * xv[k * 3 + 2];
+      }
+      J[0 + 3 * j] = a0; J[1 + 3 * j] = a1; J[2 + 3 * j] = a2;
+    }
+    // invmtx, 3x3 cofactors (column-major, A(i,j) = J[(i-1)+3(j-1)])
+    double t1 = J[4] * J[8] - J[5] * J[7];
+    double t2 = -J[1] * J[8] + J[2] * J[7];
+    double t3 = J[1] * J[5] - J[2] * J[4];
+    double det = J[0] * t1 + J[3] * t2 + J[6] * t3;
+    double denom = 1.0 / det;
+    double* b = invj + q * 9;
+    b[0] = t1 * denom;
+    b[1] = t2 * denom;
+    b[2] = t3 * denom;
+    b[4] = (J[0] * J[8] - J[2] * J[6]) * denom;
+    b[5] = (-J[0] * J[5] + J[3] * J[2]) * denom;
+    b[8] = (J[0] * J[4] - J[1] * J[3]) * denom;
+    b[3] = (-J[3] * J[8] + J[5] * J[6]) * denom;
+    b[6] = (J[3] * J[7] - J[4] * J[6]) * denom;
+    b[7] = (-J[0] * J[7] + J[1] * J[6]) * denom;
+    fac[q] = det;
+    double x0 = 0.0, x1 = 0.0, x2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      double a = tb.gshp[k * NQ + q];
+      x0 = x0 + a * xv[k * 3 + 0];
+      x1 = x1 + a * xv[k * 3 + 1];
+      x2 = x2 + a * xv[k * 3 + 2];
+    }
+    xq[q * 3 + 0] = x0; xq[q * 3 + 1] = x1; xq[q * 3 + 2] = x2;
+  }
+  __syncwarp();
+  const bool neg = fac[0] < 0.0;  // reference: |det| everywhere if the first one is negative
+  __syncwarp();
+  for (int q = lane; q < NQ; q += 32) {
+    double d = neg ? fabs(fac[q]) : fac[q];
+    fac[q] = d * tb.qw[q];
+    double f;
+    if (src.fn == FG_FN_SHARP_WAVE) f = sharp_wave_source(src.prm, xq + q * 3);
+    else if (src.fn == FG_FN_QP_VALUES) f = src.qp[c * NQ + q];
+    else if (src.fn == FG_FN_CONST) f = src.prm[0];
+    else f = 0.0;
+    fsrc[q] = f;
+  }
+  // physical gradients sg[(q*NN + a)*3 + i] = sum_j invJ(j,i) grad_ref_j
+  for (int idx = lane; idx < NQ * NN; idx += 32) {
+    int q = idx / NN, a = idx % NN;
+    const double* rg = tb.shg + ((size_t)a * NQ + q) * 3;
+    const double* b = invj + q * 9;
+    double r0 = rg[0], r1 = rg[1], r2 = rg[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) sg[idx * 3 + i] = b[0 + 3 * i] * r0 + b[1 + 3 * i] * r1 + b[2 + 3 * i] * r2;
+  }
+  __syncwarp();
+  // element matrix, upper triangle by pairs
+  for (int pbase = 0; pbase < S::NPAIR; pbase += 32 * S::CH) {
+    double acc[S::CH];
+    int pa[S::CH], pb[S::CH];
+#pragma unroll
+    for (int t = 0; t < S::CH; ++t) {
+      acc[t] = 0.0;
+      int p = pbase + lane + 32 * t;
+      if (p < S::NPAIR) pair_ab(p, ND, pa[t], pb[t]);
+      else { pa[t] = 0; pb[t] = 0; }
+    }
+    for (int q = 0; q < NQ; ++q) {
+      const double fk = fac[q] * kc;
+      const double* gq = sg + q * NN * 3;
+#pragma unroll
+      for (int t = 0; t < S::CH; ++t) {
+        const double* ga = gq + pa[t] * 3;
+        const double* gb = gq + pb[t] * 3;
+        double dot = gb[0] * ga[0] + gb[1] * ga[1] + gb[2] * ga[2];
+        acc[t] = acc[t] + fk * dot;
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < S::CH; ++t) {
+      int p = pbase + lane + 32 * t;
+      if (p < S::NPAIR) {
+        el[pa[t] * ND + pb[t]] = acc[t];
+        el[pb[t] * ND + pa[t]] = acc[t];
+      }
+    }
+  }
+  __syncwarp();
+  // element vector + Dirichlet lifting
+  bool any_dir = false;
+  for (int s = lane; s < ND; s += 32) any_dir |= gid[s] < 0;
+  any_dir = __any_sync(0xffffffffu, any_dir);
+  for (int a = lane; a < ND; a += 32) {
+    double ev = 0.0;
+    for (int q = 0; q < NQ; ++q) ev = ev + fac[q] * fsrc[q] * tb.shp[(size_t)a * NQ + q];
+    if (any_dir)
+      for (int b = 0; b < ND; ++b) {
+        int32_t gb = gid[b];
+        if (gb < 0) ev = ev - el[a * ND + b] * gvals[-gb - 1];
+      }
+    EV[c * ND + a] = ev;
+  }
+  double* Ec = E + (size_t)c * ND * ND;
+  for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = el[idx];
+}
+
+// warp per free row; CAP = power-of-two box capacity
+template <int P, int CAP>
+__global__ void __launch_bounds__(256)
+    k_scatter_rows(AsmGeom g, int64_t nfree, const int32_t* __restrict__ free2lat, const int32_t* __restrict__ latdof,
+                   const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                   const double* __restrict__ E, const double* __restrict__ EV, double* __restrict__ val,
+                   float* __restrict__ val32, double* __restrict__ rhs) {
+  constexpr int NP1 = P + 1, NN = NP1 * NP1 * NP1;
+  __shared__ int32_t s_col[8][CAP];
+  __shared__ double s_acc[8][CAP];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t r = (int64_t)blockIdx.x * 8 + wib;
+  if (r >= nfree) return;
+  const int ncomp = g.ncomp, ND = NN * ncomp;
+  const int32_t slot = free2lat[r];
+  const int64_t L = slot / ncomp;
+  const int comp = slot % ncomp;
+  const int I = (int)(L % g.Ln[0]);
+  const int J = (int)((L / g.Ln[0]) % g.Ln[1]);
+  const int K = (int)(L / ((int64_t)g.Ln[0] * g.Ln[1]));
+  const int64_t s = rowptr[r];
+  const int len = (int)(rowptr[r + 1] - s);
+  int32_t* cols = s_col[wib];
+  double* acc = s_acc[wib];
+  for (int t = lane; t < CAP; t += 32) {
+    cols[t] = t < len ? col[s + t] : 0x7fffffff;
+    acc[t] = 0.0;
+  }
+  __syncwarp();
+  int clo[3], chi[3];
+  const int IJK[3] = {I, J, K};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int cc = IJK[d] / P;
+    clo[d] = (IJK[d] % P == 0) ? cc - 1 : cc;
+    chi[d] = cc;
+    if (clo[d] < 0) clo[d] = 0;
+    if (chi[d] > g.n[d] - 1) chi[d] = g.n[d] - 1;
+  }
+  double rsum = 0.0;
+  for (int ck = clo[2]; ck <= chi[2]; ++ck)
+    for (int cj = clo[1]; cj <= chi[1]; ++cj)
+      for (int ci = clo[0]; ci <= chi[0]; ++ci) {
+        const int64_t c = (int64_t)ci + (int64_t)g.n[0] * (cj + (int64_t)g.n[1] * ck);
+        const int anode = (I - P * ci) + NP1 * ((J - P * cj) + NP1 * (K - P * ck));
+        const int a = anode + comp * NN;
+        const double* Erow = E + ((size_t)c * ND + a) * ND;
+        for (int b = lane; b < ND; b += 32) {
+          const int bnode = b % NN, bcomp = b / NN;
+          const int bi = bnode % NP1, bj = (bnode / NP1) % NP1, bk = bnode / (NP1 * NP1);
+          const int64_t M = (int64_t)(P * ci + bi) + (int64_t)g.Ln[0] * ((P * cj + bj) + (int64_t)g.Ln[1] * (P * ck + bk));
+          const int32_t id = latdof[M * ncomp + bcomp];
+          if (id > 0) {
+            const int32_t key = id - 1;
+            int lo = 0, hi = len;
+            while (lo < hi) {
+              int m = (lo + hi) >> 1;
+              if (cols[m] < key) lo = m + 1;
+              else hi = m;
+            }
+            acc[lo] = acc[lo] + Erow[b];
+          }
+        }
+        if (lane == 0) rsum = rsum + EV[c * ND + a];
+        __syncwarp();
+      }
+  for (int t = lane; t < len; t += 32) {
+    double v = acc[t];
+    val[s + t] = v;
+    val32[s + t] = (float)v;
+  }
+  if (lane == 0) rhs[r] = rsum;
+}
+
+__global__ void k_dirichlet_values(int64_t ndir, const double* xyz, int fn, SourceSpec prm, double* gv) {
+  int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (d >= ndir) return;
+  gv[d] = boundary_value(fn, prm.prm, xyz + d * 3);
+}
+
+static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+fg_status system_interpolate_dirichlet(fg_system* sys, int boundary_fn, const double* prm) {
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  if (sp->ndir == 0) return FG_OK;
+  double* xyz = nullptr;
+  FG_TRY(dev_alloc(ctx, (void**)&xyz, sizeof(double) * 3 * sp->ndir));
+  fg_status st = space_dirichlet_coords(sp, xyz);
+  if (st == FG_OK) {
+    SourceSpec s;
+    s.fn = boundary_fn;
+    for (int i = 0; i < 8; ++i) s.prm[i] = prm[i];
+    s.qp = nullptr;
+    k_dirichlet_values<<<nblk(sp->ndir, 256), 256, 0, ctx->stream>>>(sp->ndir, xyz, boundary_fn, s, sys->d_gvals);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { set_error("dirichlet values: %s", cudaGetErrorString(e)); st = FG_ERR_CUDA; }
+  }
+  cudaStreamSynchronize(ctx->stream);
+  dev_free(ctx, xyz);
+  return st;
+}
+
+template <int P>
+static fg_status launch_poisson(fg_system* sys) {
+  using S = PoissonShape<P>;
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  AsmGeom g = make_geom(sp);
+  const int64_t ncells = sp->mesh->ncells;
+  SourceSpec src;
+  src.fn = sys->integ.source_fn;
+  for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
+  src.qp = sys->d_qpsrc;
+  const size_t smem = S::SM_BYTES_WARP * S::WARPS;
+  static bool attr_set = false;
+  if (!attr_set) {
+    FG_CUDA_TRY(cudaFuncSetAttribute(k_integrate_poisson<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  const unsigned grid = nblk(ncells, S::WARPS);
+  k_integrate_poisson<P><<<grid, S::WARPS * 32, smem, ctx->stream>>>(
+      g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof, sys->d_gvals, sys->d_coef, sys->integ.coef_const, src,
+      sys->d_elmat, sys->d_elvec);
+  FG_CUDA_TRY(cudaGetLastError());
+  const int64_t n = sp->nfree;
+  if (n > 0) {
+    constexpr int CAP = P == 1 ? 32 : (P == 2 ? 128 : 512);
+    k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,
+                                                                 sp->d_col, sys->d_elmat, sys->d_elvec, sys->d_val,
+                                                                 sys->d_val32, sys->d_rhs);
+    FG_CUDA_TRY(cudaGetLastError());
+  }
+  return FG_OK;
+}
+
+fg_status system_assemble(fg_system* sys) {
+  fg_space* sp = sys->space;
+  if (sys->integ.kind != FG_POISSON || sp->ncomp != 1) {
+    set_error("integrand kind %d with %d components is not built", sys->integ.kind, sp->ncomp);
+    return FG_ERR_UNSUPPORTED;
+  }
+  switch (sp->order) {
+    case 1: return launch_poisson<1>(sys);
+    case 2: return launch_poisson<2>(sys);
+    case 3: return launch_poisson<3>(sys);
+    default: set_error("order %d not built", sp->order); return FG_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace fg

@@ -1,0 +1,152 @@
+// fg_internal.h -- internal types of libfempar_gpu.so (not part of the C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/fempar_gpu.h"
+
+#define FG_MAX_ORDER 3
+#define FG_MAX_NN 64          // nodes per cell, Q3 hex
+#define FG_MAX_NQ 64          // quadrature points per cell, Q3 hex
+
+namespace fg {
+
+void set_error(const char* fmt, ...);
+
+#define FG_CUDA_TRY(expr)                                                                   \
+  do {                                                                                      \
+    cudaError_t e_ = (expr);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      ::fg::set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e_));   \
+      return e_ == cudaErrorMemoryAllocation ? FG_ERR_OOM : FG_ERR_CUDA;                     \
+    }                                                                                       \
+  } while (0)
+
+#define FG_TRY(expr)                   \
+  do {                                 \
+    fg_status s_ = (expr);             \
+    if (s_ != FG_OK) return s_;        \
+  } while (0)
+
+// Host-side reference-element tables for a Lagrangian hex FE of order p with ncomp
+// components, and the Q1 geometry map, evaluated at the (p+1)^3 Gauss points.
+struct RefTables {
+  int dim = 3, order = 1, ncomp = 1;
+  int nn = 0;        // nodes per cell (p+1)^3
+  int nd = 0;        // dofs per cell nn*ncomp
+  int nq = 0;        // quadrature points (p+1)^3
+  int codes[27];     // polytope n-face codes sorted by (dim, code); volume last
+  int code2idx[64];  // inverse of codes (-1 if absent)
+  std::vector<double> qw;     // nq
+  std::vector<double> shp;    // nn*nq     shape values
+  std::vector<double> shg;    // nn*nq*3   reference gradients
+  std::vector<double> gshp;   // 8*nq      Q1 geometry shapes
+  std::vector<double> gshg;   // 8*nq*3    Q1 geometry gradients
+  std::vector<double> gnod;   // 8*nn      Q1 geometry shapes at the FE nodes
+  void build(int order, int ncomp);
+};
+
+// Device copy of the tables in one buffer.
+struct DevTables {
+  double* base = nullptr;
+  const double* qw;
+  const double* shp;
+  const double* shg;
+  const double* gshp;
+  const double* gshg;
+  const double* gnod;
+  size_t bytes = 0;
+};
+
+}  // namespace fg
+
+struct fg_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 0;
+  uint64_t in_use = 0;
+  int64_t launches = 0;           // kernels launched through this context
+  std::map<void*, size_t> allocs;
+};
+
+struct fg_mesh {
+  fg_ctx* ctx = nullptr;
+  int dim = 3;
+  int n[3] = {0, 0, 0};
+  double limits[6];
+  int64_t ncells = 0, nverts = 0;
+  double* d_coords = nullptr;  // 3*nverts, interleaved xyz, x-fastest lattice
+};
+
+struct fg_space {
+  fg_mesh* mesh = nullptr;
+  fg::RefTables tab;
+  fg::DevTables dtab;
+  int order = 1, ncomp = 1;
+  int Ln[3];                      // lattice nodes per direction: p*n+1
+  int64_t nlat = 0;               // lattice nodes
+  uint32_t dirmask = 0;           // bit s set: boundary set id s is strong Dirichlet
+  int64_t nfree = 0, ndir = 0;
+  int32_t* d_latdof = nullptr;    // nlat*ncomp: +id free (1-based), -id Dirichlet, 0 never
+  int32_t* d_free2lat = nullptr;  // nfree: lattice slot L*ncomp+comp of each free dof
+  int32_t* d_dir2lat = nullptr;   // ndir: lattice slot of each Dirichlet dof
+  // full CSR pattern of the free-dof matrix, 0-based sorted columns
+  int64_t nnz = 0;
+  int64_t* d_rowptr = nullptr;    // nfree+1
+  int32_t* d_col = nullptr;       // nnz
+  int64_t nnz_upper = 0;
+  int box_cap = 0;                // power-of-two capacity of a row's neighbour box
+};
+
+struct fg_system {
+  fg_space* space = nullptr;
+  double* d_val = nullptr;        // nnz FP64
+  float* d_val32 = nullptr;       // nnz FP32 copy (mixed precision)
+  double* d_rhs = nullptr;        // nfree
+  double* d_gvals = nullptr;      // ndir Dirichlet values
+  double* d_elmat = nullptr;      // ncells*nd*nd element matrices (scratch of the numeric phase)
+  double* d_elvec = nullptr;      // ncells*nd
+  double* d_coef = nullptr;       // ncells
+  double* d_qpsrc = nullptr;      // optional per-qp source
+  double* d_idiag = nullptr;      // nfree inverse diagonal (FP64)
+  float* d_idiag32 = nullptr;     // nfree inverse diagonal (FP32)
+  // solver work vectors (allocated on first solve)
+  double* d_work = nullptr;       // FP64 work area
+  float* d_work32 = nullptr;      // FP32 work area
+  double* d_red = nullptr;        // reduction partials + scalars
+  unsigned int* d_ticket = nullptr;
+  int red_blocks = 0;
+  fg_integrand integ;             // last integrand (host copy of scalars)
+};
+
+namespace fg {
+
+fg_status dev_alloc(fg_ctx* ctx, void** p, size_t bytes);
+void dev_free(fg_ctx* ctx, void* p);
+fg_status upload_tables(fg_ctx* ctx, const RefTables& t, DevTables& d);
+
+// fg_space.cu
+fg_status space_number_dofs(fg_space* sp);
+fg_status space_build_pattern(fg_space* sp);
+fg_status space_export_dof_map(fg_space* sp, int32_t* out_host);
+fg_status space_dirichlet_coords(fg_space* sp, double* d_xyz);
+fg_status space_export_upper(fg_space* sp, const double* d_val, int one_based, int64_t* irp, int32_t* ja,
+                             double* val);
+
+// fg_assembly.cu
+fg_status system_interpolate_dirichlet(fg_system* sys, int boundary_fn, const double* prm);
+fg_status system_assemble(fg_system* sys);
+
+// fg_solver.cu
+fg_status system_prepare_diag(fg_system* sys);
+fg_status system_spmv(fg_system* sys, int precision, const void* x, void* y, cudaStream_t st);
+fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double* d_b, const double* d_x0,
+                       double* d_x, fg_solve_info* info);
+
+}  // namespace fg

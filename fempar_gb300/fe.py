@@ -1,0 +1,317 @@
+"""Host-side mirror of FEMPAR's interfaces for the GB300 path.
+
+The objects wrap the C-ABI handles of libfempar_gpu.so and keep the reference's
+names and call order, so a driver reads like the reference's tutorial drivers
+(Tutorials/tutorial_01_poisson_sharp_circular_wave/tutorial_01_poisson_sharp_circular_wave.f90):
+
+    ctx   = Context()
+    tri   = SerialTriangulation(ctx, [32, 32, 32])              # triangulation%create
+    space = SerialFESpace(tri, order=1, dirichlet_ids=range(1,27))  # fe_space%create
+    op    = FEAffineOperator(space, PoissonIntegration(...))    # fe_affine_operator%create
+    op.compute()                                                 # fe_affine_operator%compute
+    solver = IterativeLinearSolver(); solver.set_type_from_string("CG")
+    solver.set_parameters_from_pl({"ILS_RTOL": 1e-8}); solver.set_operators(op, "jacobi")
+    x = solver.solve(op.get_translation())                       # iterative_linear_solver%solve
+
+Errors raise FGError (the C-ABI never aborts).  Arrays are numpy (host) or, for the
+``*_device`` methods, torch CUDA tensors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+class Context:
+    """One device, one CUDA stream, an HBM budget (serial_context_t + environment_t)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        h = C.c_void_p()
+        L.check(L.lib().fg_ctx_create(device, hbm_budget_bytes, C.byref(h)), "fg_ctx_create")
+        self.h = h
+        self.device = device
+
+    def memory(self):
+        used, budget = C.c_uint64(), C.c_uint64()
+        L.check(L.lib().fg_ctx_memory(self.h, C.byref(used), C.byref(budget)), "fg_ctx_memory")
+        return used.value, budget.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().fg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SerialTriangulation:
+    """Structured hexahedral mesh (uniform_hex_mesh_t + serial_triangulation_t)."""
+
+    def __init__(self, ctx: Context, n, limits=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), vertex_xyz=None):
+        self.ctx = ctx
+        self.n = [int(v) for v in n]
+        nn = (C.c_int32 * 3)(*self.n)
+        lim = (C.c_double * 6)(*[float(v) for v in limits])
+        vx = None
+        if vertex_xyz is not None:
+            vx = np.ascontiguousarray(vertex_xyz, dtype=np.float64)
+            expected = 3 * (self.n[0] + 1) * (self.n[1] + 1) * (self.n[2] + 1)
+            if vx.size != expected:
+                raise ValueError(f"vertex_xyz must hold {expected} values")
+        h = C.c_void_p()
+        L.check(L.lib().fg_mesh_create_structured(ctx.h, 3, nn, lim, _ptr(vx), C.byref(h)),
+                "fg_mesh_create_structured")
+        self.h = h
+        self.num_cells = self.n[0] * self.n[1] * self.n[2]
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().fg_mesh_destroy(self.h)
+            self.h = None
+
+
+class SerialFESpace:
+    """Lagrangian FE space with strong Dirichlet dofs (serial_fe_space_t)."""
+
+    def __init__(self, triangulation: SerialTriangulation, order: int = 1, ncomp: int = 1, dirichlet_ids=()):
+        self.triangulation = triangulation
+        ids = np.ascontiguousarray(list(dirichlet_ids), dtype=np.int32)
+        h = C.c_void_p()
+        L.check(L.lib().fg_space_create(triangulation.h, order, ncomp, _ptr(ids) if ids.size else None,
+                                        int(ids.size), C.byref(h)), "fg_space_create")
+        self.h = h
+        info = L.SpaceInfo()
+        L.check(L.lib().fg_space_get_info(h, C.byref(info)), "fg_space_get_info")
+        self.info = info
+        self.order = order
+        self.ncomp = ncomp
+        self.num_free_dofs = info.num_free
+        self.num_dirichlet_dofs = info.num_dirichlet
+        self.dofs_per_cell = info.dofs_per_cell
+        self.qp_per_cell = info.qp_per_cell
+        self.num_cells = info.num_cells
+
+    def get_dof_map(self):
+        """lst_dofs_gids, shape (ncells, dofs_per_cell), reference convention."""
+        out = np.zeros(self.num_cells * self.dofs_per_cell, dtype=np.int32)
+        L.check(L.lib().fg_space_get_dof_map(self.h, _ptr(out)), "fg_space_get_dof_map")
+        return out.reshape(self.num_cells, self.dofs_per_cell)
+
+    def get_dirichlet_coords(self):
+        out = np.zeros(3 * self.num_dirichlet_dofs)
+        L.check(L.lib().fg_space_get_dirichlet_coords(self.h, _ptr(out)), "fg_space_get_dirichlet_coords")
+        return out.reshape(-1, 3)
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().fg_space_destroy(self.h)
+            self.h = None
+
+
+class DiscreteIntegration:
+    """Description of discrete_integration_t%integrate_galerkin for the device kernels."""
+
+    def __init__(self, kind=L.FG_POISSON, cell_coef=None, coef_const=1.0, nu=0.3, source_fn=L.FG_FN_ZERO,
+                 fn_param=(), qp_source=None, boundary_fn=L.FG_FN_ZERO, dirichlet_values=None):
+        self.kind = kind
+        self.cell_coef = cell_coef
+        self.coef_const = coef_const
+        self.nu = nu
+        self.source_fn = source_fn
+        self.fn_param = list(fn_param)
+        self.qp_source = qp_source
+        self.boundary_fn = boundary_fn
+        self.dirichlet_values = dirichlet_values
+
+    def to_c(self):
+        g = L.Integrand()
+        L.lib().fg_integrand_default(C.byref(g))
+        keep = []
+        on_dev = None
+
+        def arr(a):
+            nonlocal on_dev
+            if a is None:
+                return None
+            if hasattr(a, "data_ptr"):
+                on_dev = True if on_dev in (None, True) else self._mixed()
+                keep.append(a)
+                return a.data_ptr()
+            on_dev = False if on_dev in (None, False) else self._mixed()
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return a.ctypes.data
+
+        g.kind = self.kind
+        g.cell_coef = arr(self.cell_coef)
+        g.coef_const = self.coef_const
+        g.nu = self.nu
+        g.source_fn = self.source_fn
+        for i, v in enumerate(self.fn_param):
+            g.fn_param[i] = float(v)
+        g.qp_source = arr(self.qp_source)
+        g.boundary_fn = self.boundary_fn
+        g.dirichlet_values = arr(self.dirichlet_values)
+        g.flags = L.FG_INPUTS_ON_DEVICE if on_dev else 0
+        return g, keep
+
+    @staticmethod
+    def _mixed():
+        raise ValueError("integrand arrays must be all host (numpy) or all device (torch) arrays")
+
+
+def PoissonIntegration(**kw):
+    return DiscreteIntegration(kind=L.FG_POISSON, **kw)
+
+
+def ElasticityIntegration(**kw):
+    return DiscreteIntegration(kind=L.FG_ELASTICITY, **kw)
+
+
+class FEAffineOperator:
+    """fe_affine_operator_t: integrate + assemble into CSR (+FP32 copy) and rhs on the device."""
+
+    def __init__(self, space: SerialFESpace, integration: DiscreteIntegration):
+        self.space = space
+        self.integration = integration
+        self.h = None
+
+    def compute(self):
+        g, keep = self.integration.to_c()
+        if self.h is None:
+            h = C.c_void_p()
+            L.check(L.lib().fg_assemble(self.space.h, C.byref(g), C.byref(h)), "fg_assemble")
+            self.h = h
+        else:
+            L.check(L.lib().fg_system_reassemble(self.h, C.byref(g)), "fg_system_reassemble")
+        del keep
+        return self
+
+    def get_matrix(self, symmetric_storage=True, one_based=True):
+        """(irp, ja, val) of the assembled matrix; the reference layout by default."""
+        n = self.space.num_free_dofs
+        nnz = self.space.info.nnz_upper if symmetric_storage else self.space.info.nnz_full
+        irp = np.zeros(n + 1, dtype=np.int64)
+        ja = np.zeros(nnz, dtype=np.int32)
+        val = np.zeros(nnz, dtype=np.float64)
+        L.check(L.lib().fg_system_export_csr(self.h, int(symmetric_storage), int(one_based), _ptr(irp), _ptr(ja),
+                                             _ptr(val)), "fg_system_export_csr")
+        return irp, ja, val
+
+    def get_translation(self):
+        out = np.zeros(self.space.num_free_dofs)
+        L.check(L.lib().fg_system_export_rhs(self.h, _ptr(out)), "fg_system_export_rhs")
+        return out
+
+    def get_dirichlet_values(self):
+        out = np.zeros(self.space.num_dirichlet_dofs)
+        L.check(L.lib().fg_system_export_dirichlet_values(self.h, _ptr(out)), "fg_system_export_dirichlet_values")
+        return out
+
+    def apply_device(self, x, y, precision=L.FG_FP64):
+        """y = A x with torch CUDA tensors (float64, or float32 for precision=FG_MIXED)."""
+        L.check(L.lib().fg_system_spmv_device(self.h, precision, _ptr(x), _ptr(y)), "fg_system_spmv_device")
+        return y
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().fg_system_destroy(self.h)
+            self.h = None
+
+
+_CRITERIA = {"RES_RES": L.FG_RES_RES, "RES_RHS": L.FG_RES_RHS, "DELTA_RHS": L.FG_DELTA_RHS,
+             "DELTA_DELTA": L.FG_DELTA_DELTA, "RES_NRMGIVEN_RHS_NRMGIVEN": L.FG_RES_NRMGIVEN_RHS_NRMGIVEN,
+             "RES_NRMGIVEN_RES_NRMGIVEN": L.FG_RES_NRMGIVEN_RES_NRMGIVEN}
+
+
+class IterativeLinearSolver:
+    """iterative_linear_solver_t with the CG type (FP64 reference CG or mixed precision)."""
+
+    def __init__(self):
+        p = L.SolverParams()
+        L.lib().fg_solver_params_default(C.byref(p))
+        self.params = p
+        self.A = None
+        self.last_info = None
+
+    def set_type_from_string(self, name: str):
+        if name.upper() not in ("CG", "GPU_CG", "GPU_MPCG"):
+            raise ValueError(f"solver type {name} is not built on the device (CG only)")
+        if name.upper() == "GPU_MPCG":
+            self.params.precision = L.FG_MIXED
+        return self
+
+    def set_parameters_from_pl(self, pl: dict):
+        """Keys of iterative_solver_parameters.f90:76-81 (+ the device-only ones)."""
+        for k, v in pl.items():
+            K = k.upper()
+            if K == "ILS_RTOL":
+                self.params.rtol = float(v)
+            elif K == "ILS_ATOL":
+                self.params.atol = float(v)
+            elif K == "ILS_MAX_NUM_ITERATIONS":
+                self.params.max_iters = int(v)
+            elif K == "ILS_STOPPING_CRITERIUM":
+                self.params.criterion = _CRITERIA[str(v).upper()]
+            elif K == "PRECISION":
+                self.params.precision = L.FG_MIXED if str(v).lower() in ("mixed", "fp32") else L.FG_FP64
+            elif K == "INNER_RTOL":
+                self.params.inner_rtol = float(v)
+            elif K == "INNER_MAX_NUM_ITERATIONS":
+                self.params.inner_max_iters = int(v)
+            elif K == "CHECK_EVERY":
+                self.params.check_every = int(v)
+            else:
+                raise KeyError(k)
+        return self
+
+    def set_operators(self, A: FEAffineOperator, M="identity"):
+        self.A = A
+        self.params.precond = L.FG_PREC_JACOBI if str(M).lower() == "jacobi" else L.FG_PREC_NONE
+        return self
+
+    def solve(self, b=None, x0=None, raise_on_nonconvergence=False):
+        n = self.A.space.num_free_dofs
+        x = np.zeros(n)
+        info = L.SolveInfo()
+        bb = None if b is None else np.ascontiguousarray(b, dtype=np.float64)
+        xx0 = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+        st = L.lib().fg_solve(self.A.h, C.byref(self.params), _ptr(bb), _ptr(xx0), _ptr(x), C.byref(info))
+        if st != L.FG_OK and (st != L.FG_ERR_NOT_CONVERGED or raise_on_nonconvergence):
+            raise L.FGError(st, "fg_solve")
+        self.last_info = info
+        return x
+
+    def solve_device(self, b=None, x0=None, x=None):
+        """Device-resident solve with torch CUDA tensors (float64)."""
+        import torch
+        n = self.A.space.num_free_dofs
+        if x is None:
+            x = torch.empty(n, dtype=torch.float64, device=f"cuda:{self.A.space.triangulation.ctx.device}")
+        info = L.SolveInfo()
+        st = L.lib().fg_solve_device(self.A.h, C.byref(self.params), _ptr(b), _ptr(x0), _ptr(x), C.byref(info))
+        if st not in (L.FG_OK, L.FG_ERR_NOT_CONVERGED):
+            raise L.FGError(st, "fg_solve_device")
+        self.last_info = info
+        return x
+
+    def info(self):
+        i = self.last_info
+        return None if i is None else {"iterations": i.iterations, "outer_iterations": i.outer_iterations,
+                                       "converged": bool(i.converged), "error_estimate": i.error_estimate,
+                                       "tolerance": i.tolerance, "solve_ms": i.solve_ms}

@@ -1,0 +1,201 @@
+/*
+ * fempar_gpu.h -- C-ABI of libfempar_gpu.so, the GB300 (sm_103a) implementation of
+ * FEMPAR's data-parallel hot path: cell-wise Galerkin integration, global sparse
+ * assembly into CSR, and the preconditioned CG solve.
+ *
+ * Conventions
+ *   - Every function returns fg_status (FG_OK = 0; errors < 0).  Nothing aborts.
+ *   - Handles are opaque and owned by the caller (fg_*_destroy).  A handle lives on
+ *     the context's device and CUDA stream; calls on one context are serialised.
+ *   - Host arrays passed in are copied; exports write into caller-allocated host
+ *     buffers.  Functions named *_device take device pointers instead.
+ *   - Global dof ids follow the reference: free dofs 1..nfree, strong-Dirichlet dofs
+ *     -1..-ndirichlet (numbered first, in cell/vef visit order).
+ *   - The parity export of the matrix is the reference's storage: 1-based CSR, upper
+ *     triangle (j >= i) when symmetric_storage = 1.  Row pointers are int64 (the
+ *     reference uses int32; a 96^3 Q2 elasticity matrix does not fit int32).
+ *
+ * Each entry point cites the reference interface it replaces (paths relative to the
+ * fempar source tree).
+ */
+#ifndef FEMPAR_GPU_H
+#define FEMPAR_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t fg_status;
+enum {
+  FG_OK = 0,
+  FG_ERR_BADARG = -1,
+  FG_ERR_OOM = -2,            /* device allocation failed or HBM budget exceeded */
+  FG_ERR_CUDA = -3,           /* CUDA runtime error (fg_last_error has the text)   */
+  FG_ERR_NOT_CONVERGED = -4,  /* solver hit max_iters; x holds the last iterate    */
+  FG_ERR_NUMERIC = -5,        /* NaN/Inf met (input or breakdown)                  */
+  FG_ERR_TIMEOUT = -6,        /* a bounded device wait ran out                     */
+  FG_ERR_UNSUPPORTED = -7,    /* order / dimension / kind not built                */
+  FG_ERR_NO_DEVICE = -8
+};
+
+typedef struct fg_ctx fg_ctx;
+typedef struct fg_mesh fg_mesh;
+typedef struct fg_space fg_space;
+typedef struct fg_system fg_system;
+
+/* Integrand kinds (discrete_integration_t extensions of the drivers). */
+enum { FG_POISSON = 0, FG_ELASTICITY = 1 };
+
+/* Analytic source / boundary functions. */
+enum {
+  FG_FN_ZERO = 0,
+  FG_FN_CONST = 1,        /* fn_param[0..ncomp-1]                                   */
+  FG_FN_SHARP_WAVE = 2,   /* u = atan(a(|x-c|-r)), f = -lap u; fn_param = a, r, cx, cy, cz */
+  FG_FN_LINEAR = 3,       /* u = x+y+z, f = 0                                       */
+  FG_FN_QP_VALUES = 4     /* source given at quadrature points: ncells*nq*ncomp     */
+};
+
+/* Input-location flag of fg_integrand.flags. */
+enum { FG_INPUTS_ON_DEVICE = 1 };
+
+typedef struct {
+  int kind;                        /* FG_POISSON / FG_ELASTICITY                     */
+  const double* cell_coef;         /* per-cell diffusion k (Poisson) or Young's E; NULL = coef_const */
+  double coef_const;
+  double nu;                       /* Poisson ratio (elasticity)                     */
+  int source_fn;                   /* FG_FN_*                                        */
+  double fn_param[8];
+  const double* qp_source;         /* FG_FN_QP_VALUES                                */
+  int boundary_fn;                 /* Dirichlet data when dirichlet_values == NULL   */
+  const double* dirichlet_values;  /* optional: ndirichlet values (fixed dof values) */
+  int flags;                       /* FG_INPUTS_ON_DEVICE                            */
+} fg_integrand;
+
+/* Solver selection (iterative_linear_solver_t parameters). */
+enum { FG_PREC_NONE = 0, FG_PREC_JACOBI = 1 };
+enum { FG_FP64 = 0, FG_MIXED = 1 };
+/* Stopping criteria, cg.f90 names. */
+enum { FG_RES_RES = 0, FG_RES_RHS = 1, FG_DELTA_RHS = 2, FG_DELTA_DELTA = 3,
+       FG_RES_NRMGIVEN_RHS_NRMGIVEN = 4, FG_RES_NRMGIVEN_RES_NRMGIVEN = 5 };
+
+typedef struct {
+  int precond;          /* FG_PREC_*                                                  */
+  int precision;        /* FG_FP64: reference CG in FP64; FG_MIXED: FP32 inner PCG + FP64 refinement */
+  int criterion;        /* FG_RES_RES (default in the reference)                      */
+  double rtol;          /* default 1e-6 (iterative_solver_parameters.f90:168-178)    */
+  double atol;          /* default 0                                                  */
+  int max_iters;        /* default 1000                                               */
+  double inner_rtol;    /* FG_MIXED: relative reduction per inner FP32 solve (0 = auto) */
+  int inner_max_iters;  /* FG_MIXED: cap per inner solve (0 = auto)                    */
+  int check_every;      /* iterations between host-side convergence polls (0 = auto)  */
+} fg_solver_params;
+
+typedef struct {
+  int iterations;       /* CG iterations (FG_MIXED: total inner iterations)           */
+  int outer_iterations; /* FG_MIXED: refinement steps (FP64 residuals)               */
+  int converged;
+  double error_estimate;/* last value of the stopping-criterion quantity              */
+  double tolerance;     /* rtol*|.|+atol the criterion compared against                */
+  double solve_ms;      /* device time of the solve                                    */
+  int64_t kernel_launches; /* kernels of this library launched by the solve (graph nodes included) */
+} fg_solve_info;
+
+typedef struct {
+  int num_dims, order, ncomp;
+  int dofs_per_cell, qp_per_cell;
+  int64_t num_cells, num_free, num_dirichlet;
+  int64_t nnz_full, nnz_upper;
+} fg_space_info;
+
+const char* fg_status_string(fg_status s);
+/* Text of the last error raised on this host thread. */
+const char* fg_last_error(void);
+/* Library version string. */
+const char* fg_version(void);
+
+/* Execution context: one device, one stream, an HBM budget (0 = all free memory).
+ * Replaces serial_context_t/environment_t setup (Sources/Lib/Tools/execution_context.f90:63-145). */
+fg_status fg_ctx_create(int device, uint64_t hbm_budget_bytes, fg_ctx** out);
+fg_status fg_ctx_destroy(fg_ctx* ctx);
+/* Bytes currently allocated by the context's objects. */
+fg_status fg_ctx_memory(fg_ctx* ctx, uint64_t* in_use, uint64_t* budget);
+/* The context's CUDA stream (cudaStream_t) for callers that order their own work or
+ * record events around the library's kernels. */
+fg_status fg_ctx_get_stream(fg_ctx* ctx, void** stream);
+/* Kernels launched by this context so far (assembly, symbolic phase and solves). */
+fg_status fg_ctx_kernel_launches(fg_ctx* ctx, int64_t* count);
+
+/* Structured hexahedral mesh of [lim0,lim1]x[lim2,lim3]x[lim4,lim5] with n[0]*n[1]*n[2] cells,
+ * cells lexicographic (x fastest).  vertex_xyz (nullable) gives 3*(n0+1)(n1+1)(n2+1) coordinates in
+ * x-fastest lattice order (interleaved xyz) for a perturbed geometry; the map stays trilinear.
+ * Replaces uniform_hex_mesh_t%generate_part_local_mesh + serial_triangulation_t%create
+ * (Sources/Lib/Geometry/Tools/uniform_hex_mesh_generator.f90:145-647,
+ *  Sources/Lib/Geometry/Triangulation/sbm_serial_triangulation.i90:29-201). */
+fg_status fg_mesh_create_structured(fg_ctx* ctx, int num_dims, const int32_t n[3], const double limits[6],
+                                    const double* vertex_xyz, fg_mesh** out);
+fg_status fg_mesh_destroy(fg_mesh* mesh);
+
+/* Lagrangian FE space of order 1..3 with ncomp components (1 = scalar, 3 = vector),
+ * global dof numbering and strong Dirichlet dofs on the boundary set ids listed
+ * (polytope ids 1..26 of the structured generator).
+ * Replaces serial_fe_space_t%create + set_up_strong_dirichlet_bcs + generate_global_dof_numbering
+ * (Sources/Lib/Integration/FESpace/sbm_serial_fe_space.i90:28-298,525-716,2423-2884). */
+fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* dirichlet_ids, int n_ids,
+                          fg_space** out);
+fg_status fg_space_destroy(fg_space* space);
+fg_status fg_space_get_info(fg_space* space, fg_space_info* info);
+/* lst_dofs_gids: ncells*dofs_per_cell int32 in the reference's cell-local dof order
+ * (fe_space.f90:636-637). */
+fg_status fg_space_get_dof_map(fg_space* space, int32_t* lst_dofs_gids);
+/* Physical coordinates (3 per dof) of the Dirichlet nodes, in Dirichlet-id order, for callers
+ * that interpolate their own boundary function (interpolate_dirichlet_values,
+ * sbm_serial_fe_space.i90:997-1176). */
+fg_status fg_space_get_dirichlet_coords(fg_space* space, double* xyz);
+
+/* Numeric assembly: integrate every cell, impose strong Dirichlet lifting and assemble the
+ * global CSR matrix (+ FP32 copy) and right-hand side on the device, deterministically.
+ * Replaces fe_affine_operator_t%compute -> discrete_integration_t%integrate_galerkin ->
+ * fe_cell_iterator_t%assembly -> sparse_assembler_t -> sparse_matrix_t%convert
+ * (Sources/Lib/Integration/FEOperator/sbm_fe_affine_operator.i90:15-34,
+ *  Sources/Lib/Integration/FEOperator/sparse_assembler.f90:58-205,
+ *  Sources/Lib/LinearAlgebra/SparseMatrix/base_sparse_matrix.f90:3469-3513,4121-4829). */
+fg_status fg_assemble(fg_space* space, const fg_integrand* integrand, fg_system** out);
+/* Re-run the numeric phase on an existing system (same space, new coefficients/data). */
+fg_status fg_system_reassemble(fg_system* sys, const fg_integrand* integrand);
+fg_status fg_system_destroy(fg_system* sys);
+
+/* Parity export of the matrix: symmetric_storage = 1 gives the reference's upper-triangle
+ * layout, 0 the full matrix; one_based = 1 gives the reference's 1-based indices.
+ * irp has nfree+1 entries, ja/val nnz (fg_space_info.nnz_upper or nnz_full).
+ * Replaces sparse_matrix_t's CSR state (csr_sparse_matrix.f90:44-115). */
+fg_status fg_system_export_csr(fg_system* sys, int symmetric_storage, int one_based,
+                               int64_t* irp, int32_t* ja, double* val);
+/* Right-hand side (fe_affine_operator_t%get_translation, fe_operator.f90:113-183). */
+fg_status fg_system_export_rhs(fg_system* sys, double* rhs);
+/* Dirichlet values used in the lifting (fe_function_t%get_fixed_dof_values). */
+fg_status fg_system_export_dirichlet_values(fg_system* sys, double* g);
+
+/* y = A x on the device (precision FG_FP64 or FG_MIXED for the FP32 copy), device pointers.
+ * Replaces sparse_matrix_t%apply (sparse_matrix.f90:1264-1276, csr_sparse_matrix.f90:626-672). */
+fg_status fg_system_spmv_device(fg_system* sys, int precision, const void* x, void* y);
+
+/* PCG solve of A x = b.  b == NULL uses the assembled right-hand side; x0 == NULL is the zero
+ * initial guess (base_iterative_linear_solver.f90:281-282).  Host pointers.
+ * Replaces iterative_linear_solver_t%solve -> cg_t (Sources/Lib/LinearAlgebra/IterativeLinearSolver/
+ * iterative_linear_solver.f90:124-131, cg.f90:101-407) with jacobi_preconditioner_t
+ * (Sources/Lib/LinearAlgebra/Preconditioner/jacobi_preconditioner.f90:356-412). */
+fg_status fg_solve(fg_system* sys, const fg_solver_params* params, const double* b, const double* x0,
+                   double* x, fg_solve_info* info);
+/* Same, device pointers (b may be NULL; x0 NULL = zero guess; x written on the device). */
+fg_status fg_solve_device(fg_system* sys, const fg_solver_params* params, const double* b_dev,
+                          const double* x0_dev, double* x_dev, fg_solve_info* info);
+
+/* Default parameters (reference defaults: CG, res_res, rtol 1e-6, 1000 iterations). */
+void fg_solver_params_default(fg_solver_params* p);
+void fg_integrand_default(fg_integrand* g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,973 @@
+// fempar_oracle.cpp -- CPU restatement of FEMPAR's serial FE assembly + CG path.
+//
+// TEST INFRASTRUCTURE ONLY (the checker for the GPU path; see fempar_oracle.h for
+// the list of reference files and lines each part follows).  The code is written
+// to reproduce the reference's results, in its operation order where rounding can
+// be affected, on structured hexahedral (3D) and quadrilateral (2D) meshes.
+//
+// Parity of the dof numbering / sparsity / matrix entries is pinned by this
+// restatement of the reference algorithm (the reference's own tests do not pin
+// them); quadrature, integration, Dirichlet interpolation and the solve are
+// pinned against the reference's own tables (tests/golden).
+#include "fempar_oracle.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+int popcount(int x) { int c = 0; while (x) { c += x & 1; x >>= 1; } return c; }
+
+// ---------------------------------------------------------------------------
+// Polytope n-faces of the hypercube.  A code holds the anchor vertex in the low
+// `dim` bits and the free ("extruded") directions in the next `dim` bits; the
+// list is sorted by (n-face dimension, code).
+// sbm_polytope.i90:175-269 (polytope_create / sort_n_faces / fill_polytope_chain)
+// ---------------------------------------------------------------------------
+std::vector<int> polytope_codes(int dim) {
+  std::vector<int> codes;
+  for (int t = 0; t < (1 << dim); ++t)
+    for (int a = 0; a < (1 << dim); ++a)
+      if ((a & t) == 0) codes.push_back(a | (t << dim));
+  std::sort(codes.begin(), codes.end(), [dim](int x, int y) {
+    int dx = popcount(x >> dim), dy = popcount(y >> dim);
+    if (dx != dy) return dx < dy;
+    return x < y;
+  });
+  return codes;
+}
+
+// ---------------------------------------------------------------------------
+// Reference Lagrangian hex FE: nodes (lexicographic, x fastest), own dofs per
+// n-face (interior nodes, node-iterator order: lowest free direction fastest),
+// vector components appended component-major.
+// sbm_polytope.i90:396-433,640-860; sbm_lagrangian_reference_fe.i90:1072-1153,1240-1285,1549-1758
+// ---------------------------------------------------------------------------
+struct RefFE {
+  int dim = 3, order = 1, ncomp = 1;
+  int nnodes = 0, nshape = 0, nfaces = 0;
+  std::vector<int> codes;
+  std::vector<std::vector<int>> own;  // per n-face (0-based, volume last): local shape ids (0-based)
+  std::vector<int> node_ijk;          // nnodes*3
+
+  void build(int d, int p, int nc) {
+    dim = d; order = p; ncomp = nc;
+    int np1 = p + 1;
+    nnodes = 1;
+    for (int i = 0; i < d; ++i) nnodes *= np1;
+    nshape = nnodes * nc;
+    node_ijk.assign(nnodes * 3, 0);
+    for (int n = 0; n < nnodes; ++n) {
+      int r = n;
+      for (int i = 0; i < d; ++i) { node_ijk[n * 3 + i] = r % np1; r /= np1; }
+    }
+    codes = polytope_codes(d);
+    nfaces = (int)codes.size();
+    own.assign(nfaces, {});
+    for (int f = 0; f < nfaces; ++f) {
+      int code = codes[f];
+      int anchor = code & ((1 << d) - 1), type = code >> d;
+      std::vector<int> freed;
+      for (int i = 0; i < d; ++i) if ((type >> i) & 1) freed.push_back(i);
+      std::vector<int> nodes;
+      // odometer over free directions, first free direction fastest, range [1,p-1]
+      std::vector<int> disp(freed.size(), 1);
+      bool empty = false;
+      for (size_t k = 0; k < freed.size(); ++k) if (p - 1 < 1) empty = true;
+      if (!empty) {
+        while (true) {
+          int ijk[3] = {0, 0, 0};
+          for (int i = 0; i < d; ++i) if (!((type >> i) & 1)) ijk[i] = ((anchor >> i) & 1) ? p : 0;
+          for (size_t k = 0; k < freed.size(); ++k) ijk[freed[k]] = disp[k];
+          int lex = 0, mul = 1;
+          for (int i = 0; i < d; ++i) { lex += ijk[i] * mul; mul *= np1; }
+          nodes.push_back(lex);
+          size_t k = 0;
+          for (; k < freed.size(); ++k) {
+            if (++disp[k] <= p - 1) break;
+            disp[k] = 1;
+          }
+          if (k == freed.size()) break;
+        }
+      }
+      for (int c = 0; c < nc; ++c)
+        for (int n : nodes) own[f].push_back(n + c * nnodes);
+    }
+  }
+  int comp_of(int s) const { return s / nnodes; }
+  int node_of(int s) const { return s % nnodes; }
+};
+
+// ---------------------------------------------------------------------------
+// Gauss-Legendre nodes/weights on [-1,1], ascending.  The reference uses the
+// Glaser-Liu-Rokhlin method (sbm_quadrature.i90:825-1334); this restatement uses
+// Newton iteration on P_n, which converges to the same nodes to machine precision
+// (checked against test_quadratures.f90's table in tests/).
+// ---------------------------------------------------------------------------
+void gauss_legendre(int n, double* x, double* w) {
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < n; ++i) {
+    double z = std::cos(pi * (i + 0.75) / (n + 0.5));
+    double dp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      if (n == 0) p1 = 1.0;
+      for (int k = 2; k <= n; ++k) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1; p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-17) break;
+    }
+    {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1; p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+    }
+    x[n - 1 - i] = z;
+    w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+  if (n == 1) { x[0] = 0.0; w[0] = 2.0; }
+  // exact symmetry
+  for (int i = 0; i < n / 2; ++i) {
+    double a = 0.5 * (x[n - 1 - i] - x[i]);
+    x[i] = -a; x[n - 1 - i] = a;
+    double b = 0.5 * (w[i] + w[n - 1 - i]);
+    w[i] = b; w[n - 1 - i] = b;
+  }
+  if (n % 2 == 1) x[n / 2] = 0.0;
+}
+
+// 1D Lagrange polynomial on equispaced nodes (2/p)i-1, value/1st/2nd derivative
+// evaluated with the reference's product recurrence (sbm_polynomial.i90:61-109).
+struct Lagrange1D {
+  int order;
+  std::vector<std::vector<double>> coef;  // per polynomial: order roots + scale
+  void build(int p) {
+    order = p;
+    std::vector<double> nc(p + 1);
+    for (int i = 0; i <= p; ++i) nc[i] = i;
+    if (p > 0) for (int i = 0; i <= p; ++i) nc[i] = (2.0 / p) * nc[i] - 1.0;
+    coef.assign(p + 1, std::vector<double>(p + 1, 0.0));
+    for (int i = 0; i <= p; ++i) {
+      int c = 0;
+      for (int j = 0; j <= p; ++j) if (j != i) coef[i][c++] = nc[j];
+      double s = 1.0;
+      for (int j = 0; j <= p; ++j) if (j != i) s = s * (nc[i] - nc[j]);
+      coef[i][p] = 1.0 / s;
+    }
+  }
+  void values(int i, double x, double* px) const {
+    px[0] = 1.0; px[1] = 0.0; px[2] = 0.0;
+    for (int k = 0; k < order; ++k) {
+      for (int j = 2; j >= 1; --j) px[j] = px[j] * (x - coef[i][k]) + px[j - 1];
+      px[0] = px[0] * (x - coef[i][k]);
+    }
+    px[2] = 2.0 * px[2];
+    for (int j = 0; j < 3; ++j) px[j] = px[j] * coef[i][order];
+  }
+};
+
+// Shape values and reference gradients of the tensor-product space at a set of
+// points (sbm_tensor_product_polynomial.i90:28-120, sbm_hex_lagrangian_reference_fe.i90:173-231).
+void tensor_shapes(int dim, int order, const std::vector<double>& pts /*npts*3*/, int npts,
+                   std::vector<double>& val /*nn*npts*/, std::vector<double>& grad /*nn*npts*3*/) {
+  Lagrange1D L; L.build(order);
+  int np1 = order + 1, nn = 1;
+  for (int i = 0; i < dim; ++i) nn *= np1;
+  val.assign((size_t)nn * npts, 0.0);
+  grad.assign((size_t)nn * npts * 3, 0.0);
+  std::vector<double> w((size_t)3 * np1 * npts * 3);  // [d][j][q][deriv]
+  for (int d = 0; d < dim; ++d)
+    for (int j = 0; j < np1; ++j)
+      for (int q = 0; q < npts; ++q) L.values(j, pts[q * 3 + d], &w[(((size_t)d * np1 + j) * npts + q) * 3]);
+  auto W = [&](int d, int j, int q, int k) { return w[(((size_t)d * np1 + j) * npts + q) * 3 + k]; };
+  for (int q = 0; q < npts; ++q)
+    for (int s = 0; s < nn; ++s) {
+      int ijk[3] = {0, 0, 0}, r = s;
+      for (int d = 0; d < dim - 1; ++d) { ijk[d] = r % np1; r /= np1; }
+      ijk[dim - 1] = r;
+      double v = 1.0;
+      for (int d = 0; d < dim; ++d) v = v * W(d, ijk[d], q, 0);
+      val[(size_t)s * npts + q] = v;
+      for (int d = 0; d < dim; ++d) {
+        double g = W(d, ijk[d], q, 1);
+        for (int e = 0; e < dim; ++e) if (e != d) g = g * W(e, ijk[e], q, 0);
+        grad[((size_t)s * npts + q) * 3 + d] = g;
+      }
+    }
+}
+
+// 3x3 (or 2x2) inverse and determinant, sbm_cell_integrator.i90:448-500 (invmtx).
+// a and b are column-major 3x3 (a[r + 3c] == a(r+1,c+1)).
+void invmtx(int n, const double* a, double* b, double& deter) {
+#define A(i, j) a[((i)-1) + 3 * ((j)-1)]
+#define B(i, j) b[((i)-1) + 3 * ((j)-1)]
+  if (n == 2) {
+    deter = A(1, 1) * A(2, 2) - A(2, 1) * A(1, 2);
+    if (deter != 0.0) {
+      double denom = 1.0 / deter;
+      B(1, 1) = A(2, 2) * denom;
+      B(2, 2) = A(1, 1) * denom;
+      B(2, 1) = -A(2, 1) * denom;
+      B(1, 2) = -A(1, 2) * denom;
+    }
+    return;
+  }
+  double t1 = A(2, 2) * A(3, 3) - A(3, 2) * A(2, 3);
+  double t2 = -A(2, 1) * A(3, 3) + A(3, 1) * A(2, 3);
+  double t3 = A(2, 1) * A(3, 2) - A(3, 1) * A(2, 2);
+  deter = A(1, 1) * t1 + A(1, 2) * t2 + A(1, 3) * t3;
+  if (deter == 0.0) return;
+  double denom = 1.0 / deter;
+  B(1, 1) = t1 * denom;
+  B(2, 1) = t2 * denom;
+  B(3, 1) = t3 * denom;
+  B(2, 2) = (A(1, 1) * A(3, 3) - A(3, 1) * A(1, 3)) * denom;
+  B(3, 2) = (-A(1, 1) * A(3, 2) + A(1, 2) * A(3, 1)) * denom;
+  B(3, 3) = (A(1, 1) * A(2, 2) - A(2, 1) * A(1, 2)) * denom;
+  B(1, 2) = (-A(1, 2) * A(3, 3) + A(3, 2) * A(1, 3)) * denom;
+  B(1, 3) = (A(1, 2) * A(2, 3) - A(2, 2) * A(1, 3)) * denom;
+  B(2, 3) = (-A(1, 1) * A(2, 3) + A(2, 1) * A(1, 3)) * denom;
+#undef A
+#undef B
+}
+
+// Analytic functions of the drivers.
+// tutorial_01_poisson_sharp_circular_wave_modules.f90:395-533 (sharp circular wave)
+// test_poisson/modules/poisson_analytical_functions.f90:71-124 (linear)
+double fn_value(int fn, const double* prm, int dim, const double* x) {
+  switch (fn) {
+    case ORC_FN_ZERO: return 0.0;
+    case ORC_FN_CONST: return prm[0];
+    case ORC_FN_LINEAR: return dim == 2 ? x[0] + x[1] : x[0] + x[1] + x[2];
+    case ORC_FN_SHARP_WAVE: {
+      double a = prm[0], r = prm[1];
+      double dx = x[0] - prm[2], dy = x[1] - prm[3];
+      if (dim == 2) return std::atan(a * (std::sqrt(dx * dx + dy * dy) - r));
+      double dz = x[2] - prm[4];
+      return std::atan(a * (std::sqrt(dx * dx + dy * dy + dz * dz) - r));
+    }
+  }
+  return 0.0;
+}
+
+double sharp_wave_source(const double* prm, int dim, const double* x) {
+  double alpha = prm[0], r = prm[1];
+  double alpha_2 = alpha * alpha, alpha_3 = alpha_2 * alpha;
+  double xc = prm[2], yc = prm[3], zc = prm[4];
+  double x_minus_xc_2 = (x[0] - xc) * (x[0] - xc);
+  double y_minus_yc_2 = (x[1] - yc) * (x[1] - yc);
+  double term1, z_minus_zc_2 = 0.0;
+  if (dim == 2) term1 = x_minus_xc_2 + y_minus_yc_2;
+  else { z_minus_zc_2 = (x[2] - zc) * (x[2] - zc); term1 = x_minus_xc_2 + y_minus_yc_2 + z_minus_zc_2; }
+  double sqrt_term1 = std::sqrt(term1);
+  double term2 = sqrt_term1 - r;
+  double term2_2 = term2 * term2;
+  double denom1 = sqrt_term1 * (alpha_2 * term2_2 + 1.0);
+  double denom2 = std::pow(term1, 1.5) * (alpha_2 * term2_2 + 1.0);
+  double denom3 = term1 * (alpha_2 * term2_2 + 1.0) * (alpha_2 * term2_2 + 1.0);
+  double dx2 = alpha / denom1 - (alpha * x_minus_xc_2) / denom2 - (2.0 * alpha_3 * x_minus_xc_2 * term2) / denom3;
+  double dy2 = alpha / denom1 - (alpha * y_minus_yc_2) / denom2 - (2.0 * alpha_3 * y_minus_yc_2 * term2) / denom3;
+  if (dim == 2) return -dx2 - dy2;
+  double dz2 = alpha / denom1 - (alpha * z_minus_zc_2) / denom2 - (2.0 * alpha_3 * z_minus_zc_2 * term2) / denom3;
+  return -dx2 - dy2 - dz2;
+}
+
+void fn_gradient(int fn, const double* prm, int dim, const double* x, double* g) {
+  g[0] = g[1] = g[2] = 0.0;
+  if (fn == ORC_FN_LINEAR) { g[0] = g[1] = 1.0; if (dim == 3) g[2] = 1.0; return; }
+  if (fn == ORC_FN_SHARP_WAVE) {
+    double alpha = prm[0], r = prm[1], alpha_2 = alpha * alpha;
+    double xc = prm[2], yc = prm[3], zc = prm[4];
+    double term1 = (x[0] - xc) * (x[0] - xc) + (x[1] - yc) * (x[1] - yc);
+    if (dim == 3) term1 += (x[2] - zc) * (x[2] - zc);
+    double sqrt_term1 = std::sqrt(term1);
+    double term2 = sqrt_term1 - r, term2_2 = term2 * term2;
+    g[0] = (alpha * (x[0] - xc)) / (sqrt_term1 * (alpha_2 * term2_2 + 1.0));
+    g[1] = (alpha * (x[1] - yc)) / (sqrt_term1 * (alpha_2 * term2_2 + 1.0));
+    if (dim == 3) g[2] = (alpha * (x[2] - zc)) / (sqrt_term1 * (alpha_2 * term2_2 + 1.0));
+  }
+}
+
+}  // namespace
+
+// ===========================================================================
+struct orc_problem {
+  orc_params p;
+  int dim, order, ncomp;
+  int n[3];
+  int64_t ncells, nverts_lattice;
+  RefFE fe, geo;
+  int nd, nq, ngeo;
+  std::vector<double> qx, qw;               // nq*3 reference qp coords, nq weights
+  std::vector<double> shp, shg;             // fe: nnodes*nq values, nnodes*nq*3 reference gradients
+  std::vector<double> gshp, gshg;           // geometry (Q1) at qps
+  std::vector<double> gnod;                 // geometry Q1 shapes at fe nodes: 2^d * nnodes
+  std::vector<double> coords;               // 3 * nverts_lattice
+  std::vector<double> coef;                 // per cell
+  std::vector<int32_t> gids;                // ncells*nd, reference convention
+  int64_t nfree = 0, ndir = 0;
+  std::vector<double> gvals;                // Dirichlet values, ndir
+  // COO (upper, free only) and CSR
+  int64_t coo_n = 0;
+  std::vector<int64_t> irp;                 // nfree+1, 1-based
+  std::vector<int32_t> ja;                  // 1-based
+  std::vector<double> val;
+  std::vector<double> rhs;
+  double t_setup = 0, t_integrate = 0, t_compress = 0;
+  std::vector<double> qp_source;            // copy of per-qp source if given
+
+  int64_t vert_index(const int* v) const {
+    return v[0] + (int64_t)(n[0] + 1) * (v[1] + (int64_t)(n[1] + 1) * (dim == 3 ? v[2] : 0));
+  }
+  void cell_ijk(int64_t c, int* ijk) const {
+    ijk[0] = (int)(c % n[0]);
+    int64_t r = c / n[0];
+    ijk[1] = (int)(r % n[1]);
+    ijk[2] = dim == 3 ? (int)(r / n[1]) : 0;
+  }
+  void cell_vertices(int64_t c, double* xv /*ngeo*3*/) const {
+    int ijk[3];
+    cell_ijk(c, ijk);
+    for (int k = 0; k < ngeo; ++k) {
+      int v[3] = {ijk[0] + (k & 1), ijk[1] + ((k >> 1) & 1), dim == 3 ? ijk[2] + ((k >> 2) & 1) : 0};
+      int64_t vi = vert_index(v);
+      for (int l = 0; l < 3; ++l) xv[k * 3 + l] = coords[vi * 3 + l];
+    }
+  }
+};
+
+namespace {
+
+// Boundary set id of a global vef (uniform_hex_mesh_generator.f90:600-630).
+int vef_set_id(const orc_problem& P, int type, const int* v, const std::vector<int>& codes) {
+  int d = P.dim, anchor = 0, t = 0;
+  for (int i = 0; i < d; ++i) {
+    if (!((type >> i) & 1)) {
+      if (v[i] == 0) {
+      } else if (v[i] == P.n[i]) anchor |= 1 << i;
+      else t |= 1 << i;
+    } else t |= 1 << i;
+  }
+  int code = anchor | (t << d);
+  for (size_t f = 0; f < codes.size(); ++f) if (codes[f] == code) return (int)f + 1;
+  return 0;
+}
+
+void build_mesh_and_dofs(orc_problem& P) {
+  const orc_params& p = P.p;
+  P.dim = p.num_dims; P.order = p.order;
+  P.ncomp = p.kind == ORC_ELASTICITY ? P.dim : 1;
+  P.n[0] = p.n[0]; P.n[1] = p.n[1]; P.n[2] = P.dim == 3 ? p.n[2] : 1;
+  P.ncells = (int64_t)P.n[0] * P.n[1] * (P.dim == 3 ? P.n[2] : 1);
+  P.nverts_lattice = (int64_t)(P.n[0] + 1) * (P.n[1] + 1) * (P.dim == 3 ? P.n[2] + 1 : 1);
+  P.fe.build(P.dim, P.order, P.ncomp);
+  P.geo.build(P.dim, 1, 1);
+  P.nd = P.fe.nshape;
+  P.ngeo = P.geo.nnodes;
+  int np1 = P.order + 1;
+  P.nq = 1;
+  for (int i = 0; i < P.dim; ++i) P.nq *= np1;
+  // quadrature: degree 2p -> p+1 points per direction (sbm_lagrangian_reference_fe.i90:1414-1423,
+  // sbm_hex_lagrangian_reference_fe.i90:320-327); x fastest (sbm_quadrature.i90:767-823)
+  std::vector<double> x1(np1), w1(np1);
+  gauss_legendre(np1, x1.data(), w1.data());
+  P.qx.assign(P.nq * 3, 0.0);
+  P.qw.assign(P.nq, 0.0);
+  for (int q = 0; q < P.nq; ++q) {
+    int i = q % np1, j = (q / np1) % np1, k = q / (np1 * np1);
+    if (P.dim == 2) { P.qw[q] = w1[i] * w1[j]; P.qx[q * 3] = x1[i]; P.qx[q * 3 + 1] = x1[j]; }
+    else { P.qw[q] = w1[i] * w1[j] * w1[k]; P.qx[q * 3] = x1[i]; P.qx[q * 3 + 1] = x1[j]; P.qx[q * 3 + 2] = x1[k]; }
+  }
+  tensor_shapes(P.dim, P.order, P.qx, P.nq, P.shp, P.shg);
+  tensor_shapes(P.dim, 1, P.qx, P.nq, P.gshp, P.gshg);
+  // geometry shapes at the FE nodes (nodal interpolation of Dirichlet data)
+  {
+    std::vector<double> npts(P.fe.nnodes * 3, 0.0), g;
+    for (int nn = 0; nn < P.fe.nnodes; ++nn)
+      for (int d = 0; d < P.dim; ++d)
+        npts[nn * 3 + d] = P.order > 0 ? (2.0 / P.order) * P.fe.node_ijk[nn * 3 + d] - 1.0 : 0.0;
+    tensor_shapes(P.dim, 1, npts, P.fe.nnodes, P.gnod, g);
+  }
+  // vertex coordinates: ijk/n mapped to the domain limits (uniform_hex_mesh_generator.f90:608-612,632-636)
+  P.coords.assign(P.nverts_lattice * 3, 0.0);
+  for (int64_t vi = 0; vi < P.nverts_lattice; ++vi) {
+    int64_t r = vi;
+    int v[3];
+    v[0] = (int)(r % (P.n[0] + 1)); r /= (P.n[0] + 1);
+    v[1] = (int)(r % (P.n[1] + 1)); r /= (P.n[1] + 1);
+    v[2] = (int)r;
+    for (int d = 0; d < P.dim; ++d) {
+      double c = (double)v[d] / (double)P.n[d];
+      P.coords[vi * 3 + d] = (p.limits[2 * d + 1] - p.limits[2 * d]) * c + p.limits[2 * d];
+    }
+  }
+  if (p.vertex_xyz)
+    std::memcpy(P.coords.data(), p.vertex_xyz, sizeof(double) * 3 * P.nverts_lattice);
+  P.coef.assign(P.ncells, 1.0);
+  if (p.cell_coef) std::memcpy(P.coef.data(), p.cell_coef, sizeof(double) * P.ncells);
+
+  // ---- dof numbering ----
+  const RefFE& fe = P.fe;
+  const int nvefs = fe.nfaces - 1;  // cell interior is the last n-face
+  P.gids.assign((size_t)P.ncells * P.nd, 0);
+  std::vector<char> is_dir_id(28, 0);
+  for (int i = 0; i < p.n_dirichlet_ids; ++i)
+    if (p.dirichlet_ids[i] >= 1 && p.dirichlet_ids[i] <= 27) is_dir_id[p.dirichlet_ids[i]] = 1;
+  const int ntypes = 1 << P.dim;
+  const int64_t nkeys = (int64_t)ntypes * P.nverts_lattice;
+  auto vef_of = [&](int64_t c, int f, int* v, int& type) {
+    int code = fe.codes[f];
+    int anchor = code & (ntypes - 1);
+    type = code >> P.dim;
+    int ijk[3];
+    P.cell_ijk(c, ijk);
+    for (int d = 0; d < 3; ++d) v[d] = d < P.dim ? ijk[d] + ((anchor >> d) & 1) : 0;
+    return (int64_t)type + ntypes * P.vert_index(v);
+  };
+  auto fetch = [&](int64_t c, int f, int64_t src_c, int src_f) {
+    // identity permutation: on a structured mesh all cells share one orientation,
+    // so the k-th own dof of the n-face maps to the k-th own dof of the owner's n-face
+    // (sbm_fe_cell_iterator.i90:736-856)
+    const std::vector<int>& t = fe.own[f];
+    const std::vector<int>& s = fe.own[src_f];
+    for (size_t k = 0; k < t.size(); ++k)
+      P.gids[(size_t)c * P.nd + t[k]] = P.gids[(size_t)src_c * P.nd + s[k]];
+  };
+  // (1) strong Dirichlet dofs, negative, first visit order (sbm_serial_fe_space.i90:525-716)
+  {
+    std::vector<int64_t> vis_cell(nkeys, -1);
+    std::vector<int> vis_f(nkeys, -1);
+    int64_t ndir = 0;
+    for (int64_t c = 0; c < P.ncells; ++c) {
+      for (int f = 0; f < nvefs; ++f) {
+        int v[3], type;
+        int64_t key = vef_of(c, f, v, type);
+        int sid = vef_set_id(P, type, v, fe.codes);
+        if (sid == 0) continue;
+        bool code = is_dir_id[sid] != 0;  // one condition per set id, all components
+        int64_t prev = ndir;
+        if (vis_cell[key] == -1) {
+          for (int s : fe.own[f]) {
+            int32_t& g = P.gids[(size_t)c * P.nd + s];
+            if (g >= 0 && code) g = (int32_t)(-(++ndir));
+          }
+        }
+        if (vis_cell[key] != -1) fetch(c, f, vis_cell[key], vis_f[key]);
+        if (vis_cell[key] == -1 && prev < ndir) { vis_cell[key] = c; vis_f[key] = f; }
+      }
+    }
+    P.ndir = ndir;
+  }
+  // (2) free dofs: cell interior first, then vefs in n-face order (sbm_serial_fe_space.i90:2623-2884)
+  {
+    std::vector<int64_t> own_cell(nkeys, -1);
+    std::vector<int> own_f(nkeys, -1);
+    int64_t cur = 0;
+    for (int64_t c = 0; c < P.ncells; ++c) {
+      for (int s : fe.own[nvefs]) P.gids[(size_t)c * P.nd + s] = (int32_t)(++cur);
+      for (int f = 0; f < nvefs; ++f) {
+        int v[3], type;
+        int64_t key = vef_of(c, f, v, type);
+        if (own_cell[key] == -1) {
+          int64_t prev = cur;
+          for (int s : fe.own[f]) {
+            int32_t& g = P.gids[(size_t)c * P.nd + s];
+            if (g >= 0) g = (int32_t)(++cur);
+          }
+          if (cur > prev) { own_cell[key] = c; own_f[key] = f; }
+        } else {
+          fetch(c, f, own_cell[key], own_f[key]);
+        }
+      }
+    }
+    P.nfree = cur;
+  }
+  // (3) nodal interpolation of the Dirichlet data (sbm_serial_fe_space.i90:997-1176)
+  P.gvals.assign(P.ndir, 0.0);
+  if (P.ndir > 0 && p.kind == ORC_POISSON) {
+    std::vector<double> xv(P.ngeo * 3);
+    for (int64_t c = 0; c < P.ncells; ++c) {
+      bool any = false;
+      for (int s = 0; s < P.nd; ++s) if (P.gids[(size_t)c * P.nd + s] < 0) { any = true; break; }
+      if (!any) continue;
+      P.cell_vertices(c, xv.data());
+      for (int s = 0; s < P.nd; ++s) {
+        int32_t g = P.gids[(size_t)c * P.nd + s];
+        if (g >= 0) continue;
+        int node = fe.node_of(s);
+        double x[3] = {0, 0, 0};
+        for (int k = 0; k < P.ngeo; ++k) {
+          double a = P.gnod[(size_t)k * fe.nnodes + node];
+          for (int l = 0; l < 3; ++l) x[l] = x[l] + a * xv[k * 3 + l];
+        }
+        P.gvals[-g - 1] = fn_value(p.boundary_fn, p.fn_param, P.dim, x);
+      }
+    }
+  }
+}
+
+// Geometry at the quadrature points of one cell: inverse Jacobian (column-major
+// 3x3 per qp), |det J| and physical qp coordinates.
+// sbm_base_map.i90:91-106, field.f90:763-787, sbm_cell_map.i90:245-369
+void cell_geometry(const orc_problem& P, int64_t c, std::vector<double>& invj, std::vector<double>& det,
+                   std::vector<double>& xq) {
+  std::vector<double> xv(P.ngeo * 3);
+  P.cell_vertices(c, xv.data());
+  invj.assign(P.nq * 9, 0.0);
+  det.assign(P.nq, 0.0);
+  xq.assign(P.nq * 3, 0.0);
+  for (int q = 0; q < P.nq; ++q) {
+    double J[9];
+    for (int j = 0; j < 3; ++j) {
+      for (int l = 0; l < 3; ++l) J[l + 3 * j] = 0.0;
+      for (int k = 0; k < P.ngeo; ++k) {
+        double alpha = P.gshg[((size_t)k * P.nq + q) * 3 + j];
+        for (int l = 0; l < 3; ++l) J[l + 3 * j] = J[l + 3 * j] + alpha * xv[k * 3 + l];
+      }
+    }
+    double* b = &invj[q * 9];
+    for (int i = 0; i < 3; ++i) b[i + 3 * i] = 1.0;
+    invmtx(P.dim, J, b, det[q]);
+  }
+  if (P.nq > 0 && det[0] < 0.0)
+    for (int q = 0; q < P.nq; ++q) det[q] = std::fabs(det[q]);
+  for (int q = 0; q < P.nq; ++q)
+    for (int k = 0; k < P.ngeo; ++k) {
+      double a = P.gshp[(size_t)k * P.nq + q];
+      for (int l = 0; l < 3; ++l) xq[q * 3 + l] = xq[q * 3 + l] + a * xv[k * 3 + l];
+    }
+}
+
+// Element matrix (column-major nd x nd) and vector of one cell, with the strong
+// Dirichlet lifting applied to the vector.
+void integrate_cell(const orc_problem& P, int64_t c, const std::vector<double>* invj0,
+                    const std::vector<double>* det0, double* elmat, double* elvec) {
+  const orc_params& p = P.p;
+  const int nd = P.nd, nq = P.nq, nn = P.fe.nnodes;
+  std::vector<double> invj, det, xq;
+  cell_geometry(P, c, invj, det, xq);
+  if (invj0) { invj = *invj0; det = *det0; }  // reference structured-mesh translation shortcut
+  // physical gradients of the scalar shape functions (sbm_lagrangian_reference_fe.i90:1330-1342)
+  std::vector<double> g((size_t)nn * nq * 3, 0.0);
+  for (int q = 0; q < nq; ++q)
+    for (int s = 0; s < nn; ++s)
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc = acc + invj[q * 9 + j + 3 * i] * P.shg[((size_t)s * nq + q) * 3 + j];
+        g[((size_t)s * nq + q) * 3 + i] = acc;
+      }
+  std::fill(elmat, elmat + (size_t)nd * nd, 0.0);
+  std::fill(elvec, elvec + nd, 0.0);
+  const double kc = P.coef[c];
+  if (p.kind == ORC_POISSON) {
+    for (int q = 0; q < nq; ++q) {
+      // tutorial modules :114-128; a per-cell diffusion coefficient k scales the
+      // bilinear form only: elmat += (factor*k) * grad(phi_j).grad(phi_i)
+      double factor = det[q] * P.qw[q];
+      double fk = factor * kc;
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j) {
+          const double* gi = &g[((size_t)i * nq + q) * 3];
+          const double* gj = &g[((size_t)j * nq + q) * 3];
+          double dot = gj[0] * gi[0] + gj[1] * gi[1] + gj[2] * gi[2];
+          elmat[i + (size_t)nd * j] = elmat[i + (size_t)nd * j] + fk * dot;
+        }
+      double f;
+      if (p.source_fn == ORC_FN_SHARP_WAVE) f = sharp_wave_source(p.fn_param, P.dim, &xq[q * 3]);
+      else if (p.source_fn == ORC_FN_QP_VALUES) f = P.qp_source[(size_t)c * nq + q];
+      else if (p.source_fn == ORC_FN_CONST) f = p.fn_param[0];
+      else f = 0.0;
+      for (int i = 0; i < nd; ++i) elvec[i] = elvec[i] + factor * f * P.shp[(size_t)i * nq + q];
+    }
+  } else {
+    // sbm_irreducible_discrete_integration.i90:100-121
+    double E = kc, nu = p.nu;
+    double lambda = (nu * E) / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    double mu = E / (2.0 * (1.0 + nu));
+    const int dim = P.dim;
+    for (int q = 0; q < nq; ++q) {
+      double dV = det[q] * P.qw[q];
+      double src[3] = {0, 0, 0};
+      if (p.source_fn == ORC_FN_CONST) for (int d = 0; d < dim; ++d) src[d] = p.fn_param[d];
+      else if (p.source_fn == ORC_FN_QP_VALUES) for (int d = 0; d < dim; ++d) src[d] = P.qp_source[((size_t)c * nq + q) * dim + d];
+      for (int i = 0; i < nd; ++i) {
+        int ci = P.fe.comp_of(i), ni = P.fe.node_of(i);
+        const double* gi = &g[((size_t)ni * nq + q) * 3];
+        double Gi[3][3] = {{0}};
+        for (int a = 0; a < 3; ++a) Gi[a][ci] = gi[a];
+        for (int j = 0; j < nd; ++j) {
+          int cj = P.fe.comp_of(j), nj = P.fe.node_of(j);
+          const double* gj = &g[((size_t)nj * nq + q) * 3];
+          double Gj[3][3] = {{0}};
+          for (int a = 0; a < 3; ++a) Gj[a][cj] = gj[a];
+          double eps[3][3], tr = 0.0;
+          for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) eps[a][b] = 0.5 * (Gj[a][b] + Gj[b][a]);
+          for (int a = 0; a < 3; ++a) tr = tr + eps[a][a];
+          double dc = 0.0;
+          for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+              double sig = lambda * tr * (a == b ? 1.0 : 0.0) + 2.0 * mu * eps[a][b];
+              dc = dc + Gi[a][b] * sig;
+            }
+          elmat[i + (size_t)nd * j] = elmat[i + (size_t)nd * j] + dV * dc;
+        }
+        elvec[i] = elvec[i] + dV * (src[ci] * P.shp[(size_t)ni * nq + q]);
+      }
+    }
+  }
+  // strong Dirichlet lifting (sbm_fe_cell_iterator.i90:1610-1637)
+  for (int j = 0; j < nd; ++j) {
+    int32_t gj = P.gids[(size_t)c * nd + j];
+    if (gj < 0) {
+      double gv = P.gvals[-gj - 1];
+      for (int i = 0; i < nd; ++i) elvec[i] = elvec[i] - elmat[i + (size_t)nd * j] * gv;
+    }
+  }
+}
+
+void assemble(orc_problem& P) {
+  const int nd = P.nd;
+  std::vector<double> invj0, det0, xq0;
+  if (P.p.translated_jacobian) cell_geometry(P, 0, invj0, det0, xq0);
+  // COO append in cell order (base_sparse_matrix.f90:3469-3513); rhs add (serial_scalar_array.f90:247-262)
+  std::vector<int32_t> cia, cja;
+  std::vector<double> cval;
+  P.rhs.assign(P.nfree, 0.0);
+  const int64_t chunk = 4096;
+  std::vector<double> em((size_t)chunk * nd * nd), ev((size_t)chunk * nd);
+  int nth = P.p.nthreads > 0 ? P.p.nthreads : 1;
+  (void)nth;
+  for (int64_t c0 = 0; c0 < P.ncells; c0 += chunk) {
+    int64_t c1 = std::min(P.ncells, c0 + chunk);
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nth) if (nth > 1)
+    for (int64_t c = c0; c < c1; ++c)
+      integrate_cell(P, c, P.p.translated_jacobian && c > 0 ? &invj0 : nullptr,
+                     P.p.translated_jacobian && c > 0 ? &det0 : nullptr,
+                     &em[(size_t)(c - c0) * nd * nd], &ev[(size_t)(c - c0) * nd]);
+    for (int64_t c = c0; c < c1; ++c) {
+      const int32_t* gid = &P.gids[(size_t)c * nd];
+      const double* elmat = &em[(size_t)(c - c0) * nd * nd];
+      for (int j = 0; j < nd; ++j) {
+        int32_t jas = gid[j];
+        if (jas < 1) continue;
+        for (int i = 0; i < nd; ++i) {
+          int32_t ias = gid[i];
+          if (ias < 1 || ias > jas) continue;
+          cia.push_back(ias); cja.push_back(jas); cval.push_back(elmat[i + (size_t)nd * j]);
+        }
+      }
+      const double* elvec = &ev[(size_t)(c - c0) * nd];
+      for (int i = 0; i < nd; ++i) if (gid[i] > 0) P.rhs[gid[i] - 1] = P.rhs[gid[i] - 1] + elvec[i];
+    }
+  }
+  P.coo_n = (int64_t)cia.size();
+  double t0 = now_s();
+  // sort_and_compress (base_sparse_matrix.f90:4121-4829): stable bucket by row, stable
+  // sort of the columns of each row, duplicates summed in sorted (= append) order.
+  const int64_t nr = P.nfree;
+  std::vector<int64_t> cnt(nr + 1, 0);
+  for (int64_t e = 0; e < P.coo_n; ++e) cnt[cia[e]]++;
+  std::vector<int64_t> start(nr + 1, 0);
+  for (int64_t r = 1; r <= nr; ++r) start[r] = start[r - 1] + cnt[r];
+  std::vector<int64_t> perm(P.coo_n);
+  {
+    std::vector<int64_t> pos(start.begin(), start.end());
+    for (int64_t e = 0; e < P.coo_n; ++e) perm[pos[cia[e] - 1]++] = e;
+  }
+  std::vector<int64_t> rowlen(nr, 0);
+  P.ja.clear(); P.val.clear();
+  P.ja.reserve(P.coo_n / 2 + 16); P.val.reserve(P.coo_n / 2 + 16);
+  std::vector<std::vector<int32_t>> rja(nth > 1 ? nr : 0);
+  std::vector<std::vector<double>> rva(nth > 1 ? nr : 0);
+  auto row_compress = [&](int64_t r, std::vector<int32_t>& oj, std::vector<double>& ov) {
+    int64_t s = start[r], e = start[r + 1];
+    std::stable_sort(perm.begin() + s, perm.begin() + e, [&](int64_t a, int64_t b) { return cja[a] < cja[b]; });
+    for (int64_t k = s; k < e; ++k) {
+      int64_t idx = perm[k];
+      if (!oj.empty() && k > s && oj.back() == cja[idx]) ov.back() = ov.back() + cval[idx];
+      else { oj.push_back(cja[idx]); ov.push_back(cval[idx]); }
+    }
+  };
+  if (nth > 1) {
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nth)
+    for (int64_t r = 0; r < nr; ++r) row_compress(r, rja[r], rva[r]);
+    P.irp.assign(nr + 1, 1);
+    for (int64_t r = 0; r < nr; ++r) {
+      P.irp[r + 1] = P.irp[r] + (int64_t)rja[r].size();
+      P.ja.insert(P.ja.end(), rja[r].begin(), rja[r].end());
+      P.val.insert(P.val.end(), rva[r].begin(), rva[r].end());
+    }
+  } else {
+    P.irp.assign(nr + 1, 1);
+    for (int64_t r = 0; r < nr; ++r) {
+      size_t before = P.ja.size();
+      int64_t s = start[r], e = start[r + 1];
+      std::stable_sort(perm.begin() + s, perm.begin() + e, [&](int64_t a, int64_t b) { return cja[a] < cja[b]; });
+      for (int64_t k = s; k < e; ++k) {
+        int64_t idx = perm[k];
+        if (P.ja.size() > before && P.ja.back() == cja[idx]) P.val.back() = P.val.back() + cval[idx];
+        else { P.ja.push_back(cja[idx]); P.val.push_back(cval[idx]); }
+      }
+      P.irp[r + 1] = P.irp[r] + (int64_t)(P.ja.size() - before);
+    }
+  }
+  P.t_compress = now_s() - t0;
+}
+
+// ---- linear algebra of the CG path -------------------------------------------
+// matvec_symmetric_storage (csr_sparse_matrix.f90:597-623), alpha=1, beta=0
+void spmv_sym(const orc_problem& P, const double* x, double* y) {
+  const int64_t n = P.nfree;
+  for (int64_t i = 0; i < n; ++i) y[i] = 0.0;
+  for (int64_t ir = 0; ir < n; ++ir) {
+    int64_t s = P.irp[ir] - 1, e = P.irp[ir + 1] - 1;
+    if (s >= e) continue;
+    y[ir] = y[ir] + x[P.ja[s] - 1] * P.val[s];
+    for (int64_t iz = s + 1; iz < e; ++iz) {
+      int64_t ic = P.ja[iz] - 1;
+      y[ir] = y[ir] + 1.0 * x[ic] * P.val[iz];
+      y[ic] = y[ic] + 1.0 * x[ir] * P.val[iz];
+    }
+  }
+}
+
+struct FullCSR { std::vector<int64_t> rp; std::vector<int32_t> ci; std::vector<double> v; };
+void expand_full(const orc_problem& P, FullCSR& F) {
+  const int64_t n = P.nfree;
+  std::vector<int64_t> len(n, 0);
+  for (int64_t r = 0; r < n; ++r)
+    for (int64_t k = P.irp[r] - 1; k < P.irp[r + 1] - 1; ++k) {
+      len[r]++;
+      if (P.ja[k] - 1 != r) len[P.ja[k] - 1]++;
+    }
+  F.rp.assign(n + 1, 0);
+  for (int64_t r = 0; r < n; ++r) F.rp[r + 1] = F.rp[r] + len[r];
+  F.ci.resize(F.rp[n]); F.v.resize(F.rp[n]);
+  std::vector<int64_t> pos(F.rp.begin(), F.rp.end() - 1);
+  for (int64_t r = 0; r < n; ++r)
+    for (int64_t k = P.irp[r] - 1; k < P.irp[r + 1] - 1; ++k) {
+      int64_t c = P.ja[k] - 1;
+      F.ci[pos[r]] = (int32_t)c; F.v[pos[r]++] = P.val[k];
+      if (c != r) { F.ci[pos[c]] = (int32_t)r; F.v[pos[c]++] = P.val[k]; }
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+orc_problem* orc_create(const orc_params* p) {
+  if (!p || (p->num_dims != 2 && p->num_dims != 3) || p->order < 1 || p->order > 8) return nullptr;
+  orc_problem* P = new orc_problem();
+  P->p = *p;
+  double t0 = now_s();
+  build_mesh_and_dofs(*P);
+  if (p->source_fn == ORC_FN_QP_VALUES && p->qp_source)
+    P->qp_source.assign(p->qp_source, p->qp_source + (size_t)P->ncells * P->nq * (p->kind == ORC_ELASTICITY ? P->dim : 1));
+  double t1 = now_s();
+  assemble(*P);
+  double t2 = now_s();
+  P->t_setup = t1 - t0;
+  P->t_integrate = (t2 - t1) - P->t_compress;
+  P->p.vertex_xyz = nullptr; P->p.cell_coef = nullptr; P->p.qp_source = nullptr;
+  return P;
+}
+
+void orc_destroy(orc_problem* h) { delete h; }
+int64_t orc_num_cells(const orc_problem* h) { return h->ncells; }
+int orc_dofs_per_cell(const orc_problem* h) { return h->nd; }
+int orc_qp_per_cell(const orc_problem* h) { return h->nq; }
+int64_t orc_num_free(const orc_problem* h) { return h->nfree; }
+int64_t orc_num_dirichlet(const orc_problem* h) { return h->ndir; }
+int64_t orc_nnz_upper(const orc_problem* h) { return (int64_t)h->ja.size(); }
+int64_t orc_coo_entries(const orc_problem* h) { return h->coo_n; }
+
+void orc_get_dof_map(const orc_problem* h, int32_t* out) { std::memcpy(out, h->gids.data(), sizeof(int32_t) * h->gids.size()); }
+void orc_get_csr_upper(const orc_problem* h, int64_t* irp, int32_t* ja, double* val) {
+  if (irp) std::memcpy(irp, h->irp.data(), sizeof(int64_t) * h->irp.size());
+  if (ja) std::memcpy(ja, h->ja.data(), sizeof(int32_t) * h->ja.size());
+  if (val) std::memcpy(val, h->val.data(), sizeof(double) * h->val.size());
+}
+void orc_get_rhs(const orc_problem* h, double* rhs) { std::memcpy(rhs, h->rhs.data(), sizeof(double) * h->rhs.size()); }
+void orc_get_dirichlet_values(const orc_problem* h, double* g) { std::memcpy(g, h->gvals.data(), sizeof(double) * h->gvals.size()); }
+void orc_get_elmat(const orc_problem* h, int64_t cell, double* elmat, double* elvec) {
+  std::vector<double> invj0, det0, xq0;
+  if (h->p.translated_jacobian && cell > 0) cell_geometry(*h, 0, invj0, det0, xq0);
+  integrate_cell(*h, cell, h->p.translated_jacobian && cell > 0 ? &invj0 : nullptr,
+                 h->p.translated_jacobian && cell > 0 ? &det0 : nullptr, elmat, elvec);
+}
+void orc_get_timings(const orc_problem* h, double* t3) { t3[0] = h->t_setup; t3[1] = h->t_integrate; t3[2] = h->t_compress; }
+
+void orc_spmv(const orc_problem* h, const double* x, double* y) { spmv_sym(*h, x, y); }
+
+// cg_solve_body (cg.f90:101-238) with init_convergence_data / update_convergence_data...
+// (cg.f90:279-407).  Vector kernels are the reference's BLAS calls restated as loops.
+int orc_cg(const orc_problem* h, int precond, double rtol, double atol, int maxit, int criterion,
+           const double* b, const double* x0, double* x, int* iters, double* history, int nthreads) {
+  const int64_t n = h->nfree;
+  std::vector<double> r(n), z(n), p(n), Ap(n), idiag(n, 1.0);
+  const int nth = nthreads > 0 ? nthreads : 1;
+  FullCSR F;
+  if (nth > 1) expand_full(*h, F);
+  auto A = [&](const double* in, double* out) {
+    if (nth > 1) {
+#pragma omp parallel for schedule(static) num_threads(nth)
+      for (int64_t i = 0; i < n; ++i) {
+        double acc = 0.0;
+        for (int64_t k = F.rp[i]; k < F.rp[i + 1]; ++k) acc += F.v[k] * in[F.ci[k]];
+        out[i] = acc;
+      }
+    } else spmv_sym(*h, in, out);
+  };
+  auto dot = [&](const double* a, const double* c) {
+    double s = 0.0;
+    if (nth > 1) {
+#pragma omp parallel for reduction(+ : s) schedule(static) num_threads(nth)
+      for (int64_t i = 0; i < n; ++i) s += a[i] * c[i];
+    } else for (int64_t i = 0; i < n; ++i) s = s + a[i] * c[i];
+    return s;
+  };
+  auto nrm2 = [&](const double* a) { return std::sqrt(dot(a, a)); };
+  // axpby: y = alpha*x + beta*y
+  auto axpby = [&](double alpha, const double* xx, double beta, double* yy) {
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+    for (int64_t i = 0; i < n; ++i) yy[i] = alpha * xx[i] + beta * yy[i];
+  };
+  if (precond == 1) {
+    // extract_diagonal (csr_sparse_matrix.f90:4231-4256) + entrywise_invert
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t s = h->irp[i] - 1, e = h->irp[i + 1] - 1;
+      const int32_t* lo = h->ja.data() + s;
+      const int32_t* hi = h->ja.data() + e;
+      const int32_t* it = std::lower_bound(lo, hi, (int32_t)(i + 1));
+      double d = (it != hi && *it == (int32_t)(i + 1)) ? h->val[s + (it - lo)] : 0.0;
+      idiag[i] = 1.0 / d;
+    }
+  }
+  auto M = [&](const double* in, double* out) {
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+    for (int64_t i = 0; i < n; ++i) out[i] = precond == 1 ? idiag[i] * in[i] : in[i];
+  };
+  for (int64_t i = 0; i < n; ++i) x[i] = x0 ? x0[i] : 0.0;
+  double b_nrm_M = 0.0;
+  if (criterion == ORC_RES_NRMGIVEN_RHS_NRMGIVEN) { M(b, r.data()); b_nrm_M = std::sqrt(dot(b, r.data())); }
+  A(x, r.data());
+  axpby(1.0, b, -1.0, r.data());
+  M(r.data(), z.data());
+  double r_z = dot(r.data(), z.data());
+  double r_nrm_M = std::sqrt(r_z);
+  for (int64_t i = 0; i < n; ++i) p[i] = z[i];
+  double rhs_test = 0.0;
+  switch (criterion) {
+    case ORC_RES_RHS: case ORC_DELTA_RHS: rhs_test = rtol * nrm2(b) + atol; break;
+    case ORC_RES_RES: rhs_test = rtol * nrm2(r.data()) + atol; break;
+    case ORC_RES_NRMGIVEN_RHS_NRMGIVEN: rhs_test = rtol * b_nrm_M + atol; break;
+    case ORC_RES_NRMGIVEN_RES_NRMGIVEN: rhs_test = rtol * r_nrm_M + atol; break;
+    default: break;
+  }
+  int it = 0;
+  bool conv = false;
+  double err = 0.0;
+  while (true) {
+    ++it;
+    A(p.data(), Ap.data());
+    double Ap_p = dot(Ap.data(), p.data());
+    double alpha = Ap_p != 0.0 ? r_z / Ap_p : 0.0;
+    axpby(alpha, p.data(), 1.0, x);
+    axpby(-alpha, Ap.data(), 1.0, r.data());
+    if (it == 1 && (criterion == ORC_DELTA_RHS || criterion == ORC_DELTA_DELTA)) {
+      err = alpha * nrm2(p.data());
+      if (criterion == ORC_DELTA_DELTA) rhs_test = rtol * err + atol;
+    }
+    switch (criterion) {
+      case ORC_RES_RES: case ORC_RES_RHS: err = nrm2(r.data()); break;
+      case ORC_DELTA_RHS: case ORC_DELTA_DELTA: if (it != 1) err = alpha * nrm2(p.data()); break;
+      default: err = r_nrm_M; break;
+    }
+    if (history) history[it - 1] = err;
+    conv = err <= rhs_test;
+    if (conv || it >= maxit) break;
+    M(r.data(), z.data());
+    double beta = 1.0 / r_z;
+    r_z = dot(r.data(), z.data());
+    beta = beta * r_z;
+    r_nrm_M = std::sqrt(r_z);
+    axpby(1.0, z.data(), beta, p.data());
+  }
+  if (iters) *iters = it;
+  return conv ? 0 : 1;
+}
+
+double orc_energy_error(const orc_problem* h, const double* x) {
+  const orc_params& p = h->p;
+  const int nd = h->nd, nq = h->nq;
+  double total = 0.0;
+  std::vector<double> invj, det, xq;
+  for (int64_t c = 0; c < h->ncells; ++c) {
+    cell_geometry(*h, c, invj, det, xq);
+    double sq = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      double gh[3] = {0, 0, 0};
+      for (int s = 0; s < nd; ++s) {
+        int32_t g = h->gids[(size_t)c * nd + s];
+        double u = g > 0 ? x[g - 1] : h->gvals[-g - 1];
+        double gp[3];
+        for (int i = 0; i < 3; ++i) {
+          double acc = 0.0;
+          for (int j = 0; j < 3; ++j) acc = acc + invj[q * 9 + j + 3 * i] * h->shg[((size_t)s * nq + q) * 3 + j];
+          gp[i] = acc;
+        }
+        for (int i = 0; i < 3; ++i) gh[i] = gh[i] + u * gp[i];
+      }
+      double ge[3];
+      fn_gradient(p.boundary_fn, p.fn_param, h->dim, &xq[q * 3], ge);
+      double factor = det[q] * h->qw[q];
+      double e0 = ge[0] - gh[0], e1 = ge[1] - gh[1], e2 = ge[2] - gh[2];
+      sq = sq + factor * (e0 * e0 + e1 * e1 + e2 * e2);
+    }
+    total += sq;
+  }
+  return std::sqrt(total);
+}
+
+void orc_gauss_legendre(int n, double* x, double* w) { gauss_legendre(n, x, w); }
+
+int orc_own_dofs(int num_dims, int order, int ncomp, int iface, int32_t* out) {
+  RefFE fe;
+  fe.build(num_dims, order, ncomp);
+  if (iface < 1 || iface > fe.nfaces) return -1;
+  const std::vector<int>& l = fe.own[iface - 1];
+  for (size_t k = 0; k < l.size(); ++k) out[k] = l[k];
+  return (int)l.size();
+}
+
+int orc_polytope_codes(int num_dims, int32_t* codes) {
+  std::vector<int> c = polytope_codes(num_dims);
+  for (size_t i = 0; i < c.size(); ++i) codes[i] = c[i];
+  return (int)c.size();
+}
+
+}  // extern "C"
