@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark: DOF/s to a 1e-8 relative residual on one GB300, mixed precision vs plain FP64.
+
+Workload (the single-GPU configuration the metric is quoted on): Poisson -div(k grad u) = 1
+on the unit cube, 128^3 hexahedra, Q2 Lagrangian elements, 3x3x3 Gauss points, interior
+vertices perturbed by a seeded U(-0.15h, 0.15h) per component (trilinear geometry),
+k = exp(N(0,1)) per cell, homogeneous Dirichlet on the whole boundary, Jacobi-PCG from
+x0 = 0 to ||r|| <= 1e-8 ||r0||.  16,581,375 free dofs.
+
+A step = numeric assembly (integration + CSR + FP32 copy + Jacobi diagonal) + PCG solve;
+the symbolic phase (dof numbering, sparsity) is built once before timing ("warm" DOF/s).
+value = free dofs / device time of a step (inputs resident in HBM), mixed precision
+(FP32 matrix/SpMV/Jacobi inner PCG, FP64 residual, dots and refinement).  The plain FP64
+drop-in is timed beside it.  e2e = the same through the public API with host buffers:
+per-cell coefficients copied in from pinned host memory and the solution copied out.
+
+--impl reference times the reference's CPU path (the C++ restatement in oracle/, the
+reference itself is Fortran and cannot be built here) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 20261203
+METRIC = "DOF/s to 1e-8 rel. residual, mixed vs plain FP64 on GB300; p50/p99 solve latency"
+# Jacobi-PCG iterations of this exact workload in FP64 (measured by the GPU arm of this
+# benchmark; the same algorithm on the CPU takes the same number of iterations).
+CFG2_FP64_ITERS = 1500
+
+
+def workload(n, seed=SEED):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    h = 1.0 / n
+    nv = n + 1
+    k, j, i = np.meshgrid(np.arange(nv), np.arange(nv), np.arange(nv), indexing="ij")
+    xyz = np.stack([i * h, j * h, k * h], axis=-1).reshape(-1, 3)
+    ii, jj, kk = i.ravel(), j.ravel(), k.ravel()
+    interior = (ii > 0) & (ii < n) & (jj > 0) & (jj < n) & (kk > 0) & (kk < n)
+    d = rng.uniform(-0.15 * h, 0.15 * h, size=xyz.shape)
+    xyz[interior] += d[interior]
+    coef = np.exp(rng.normal(0.0, 1.0, size=n ** 3))
+    return np.ascontiguousarray(xyz.ravel()), coef
+
+
+def spmv_bytes(n, nnz, fp32):
+    return (8 * nnz + 4 * (n + 1) + 8 * n) if fp32 else (12 * nnz + 4 * (n + 1) + 16 * n)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def cpu_baseline(iters_full, n_full, m=16, cg_iters=40, nthreads=1):
+    """Oracle on a bounded sample, scaled to the full workload by cells, nnz and iterations."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    xyz, coef = workload(m, seed=SEED + 1)
+    t0 = time.perf_counter()
+    P = O.Problem([m, m, m], order=2, vertex_xyz=xyz, cell_coef=coef, source_fn=O.FN_CONST, fn_param=[1.0],
+                  nthreads=nthreads)
+    t_asm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    P.cg(precond=1, rtol=1e-30, maxit=cg_iters, nthreads=nthreads)
+    t_cg = time.perf_counter() - t0
+    ncells_full = n_full ** 3
+    nfree_full = (2 * n_full - 1) ** 3
+    # nnz of the upper layout scales with the number of lattice nodes
+    nnz_up_full = P.nnz_upper * (nfree_full / P.nfree)
+    t_full = t_asm / P.ncells * ncells_full + t_cg / (cg_iters * P.nnz_upper) * nnz_up_full * iters_full
+    return {"value": nfree_full / t_full, "unit": "DOF/s", "cores": nthreads, "kind": "port",
+            "sample": f"oracle on a {m}^3 Q2 sample of the same distribution ({P.nfree} dofs): full assembly "
+                      f"({t_asm:.2f} s) + {cg_iters} Jacobi-PCG iterations ({t_cg:.2f} s), scaled per cell and per "
+                      f"upper-CSR nonzero to {n_full}^3 with {iters_full} iterations"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    nth = os.cpu_count() or 1
+    vals = []
+    for s in range(args.warmup + args.steps):
+        cb = cpu_baseline(CFG2_FP64_ITERS, args.n, m=args.ref_m, cg_iters=20, nthreads=nth)
+        if s >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    nfree = (2 * args.n - 1) ** 3
+    line = {"metric": METRIC, "value": v, "unit": "DOF/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": nfree / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (PCG64 seed {SEED})",
+            "config": {"workload": f"poisson_q{2}_{args.n}^3_perturbed_lognormal_jacobi_pcg_1e-8", "n": args.n,
+                       "order": 2, "num_free_dofs": nfree, "precision": "fp64",
+                       "note": "reference is Fortran (no compiler on the image): its path restated in C++ (oracle/)"},
+            "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": nth, "kind": "port",
+                             "sample": cb["sample"] + f"; OpenMP, {nth} threads"},
+            "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-m", type=int, default=24)
+    args = ap.parse_args()
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+
+    import fempar_gb300 as fg
+    from fempar_gb300 import _lib as L
+    import ctypes as C
+
+    n = args.n
+    xyz, coef = workload(n)
+    ctx = fg.Context(local)
+    sp_ptr = C.c_void_p()
+    L.lib().fg_ctx_get_stream(ctx.h, C.byref(sp_ptr))
+    stream = torch.cuda.ExternalStream(sp_ptr.value, device=f"cuda:{local}")
+
+    t0 = time.perf_counter()
+    tri = fg.SerialTriangulation(ctx, [n, n, n], vertex_xyz=xyz)
+    space = fg.SerialFESpace(tri, order=2, dirichlet_ids=fg.ALL_BOUNDARY_IDS)
+    t_symbolic = time.perf_counter() - t0
+    coef_dev = torch.from_numpy(coef).to(f"cuda:{local}")
+    integ_dev = fg.PoissonIntegration(cell_coef=coef_dev, source_fn=fg.FG_FN_CONST, fn_param=[1.0])
+    op = fg.FEAffineOperator(space, integ_dev).compute()
+    nfree = space.num_free_dofs
+    nnz = space.info.nnz_full
+    xbuf = torch.empty(nfree, dtype=torch.float64, device=f"cuda:{local}")
+
+    def solver(precision):
+        s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
+        s.set_parameters_from_pl({"ILS_RTOL": 1e-8, "ILS_MAX_NUM_ITERATIONS": 200000,
+                                  "PRECISION": "mixed" if precision == fg.FG_MIXED else "fp64"})
+        return s
+
+    def sync_all():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    def timed_steps(precision, k, w, e2e=False, host=None):
+        s = solver(precision)
+        times, infos, launches = [], [], 0
+        for it in range(w + k):
+            sync_all()
+            l0 = ctx.kernel_launches()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if e2e:
+                op.integration = host["integ"]
+                op.compute()
+                s.solve(out=host["x"])
+            else:
+                op.integration = integ_dev
+                op.compute()
+                s.solve_device(x=xbuf)
+            e1.record(stream)
+            e1.synchronize()
+            if it >= w:
+                times.append(e0.elapsed_time(e1))
+                infos.append(s.info())
+                launches += ctx.kernel_launches() - l0
+        return times, infos, launches, s
+
+    # ---- FP64 drop-in (reference algorithm) ----
+    t64, i64, _, s64 = timed_steps(fg.FG_FP64, args.fp64_steps, 1)
+    x64 = xbuf.clone()
+    iters64 = i64[-1]["iterations"]
+    # ---- mixed precision (headline) ----
+    clk = ClockSampler(local)
+    clk.start()
+    tmx, imx, launches, smx = timed_steps(fg.FG_MIXED, args.steps, args.warmup)
+    clocks = clk.stop()
+    xmx = xbuf.clone()
+    err_vs_fp64 = float(torch.linalg.norm(xmx - x64) / torch.linalg.norm(x64))
+    # ---- end to end through the public API with pinned host buffers ----
+    coef_pin = torch.from_numpy(coef).pin_memory()
+    x_pin = torch.empty(nfree, dtype=torch.float64).pin_memory()
+    host = {"integ": fg.PoissonIntegration(cell_coef=coef_pin.numpy(), source_fn=fg.FG_FN_CONST, fn_param=[1.0]),
+            "x": x_pin.numpy()}
+    te2e, _, _, _ = timed_steps(fg.FG_MIXED, max(1, args.steps), 1, e2e=True, host=host)
+    op.integration = integ_dev
+    op.compute()
+
+    # ---- dominant kernel: SpMV, timed on the library's stream ----
+    def spmv_ms(precision, reps=10):
+        if precision == fg.FG_MIXED:
+            xv = torch.rand(nfree, dtype=torch.float32, device=f"cuda:{local}")
+        else:
+            xv = torch.rand(nfree, dtype=torch.float64, device=f"cuda:{local}")
+        yv = torch.empty_like(xv)
+        op.apply_device(xv, yv, precision)
+        sync_all()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            op.apply_device(xv, yv, precision)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms32 = spmv_ms(fg.FG_MIXED)
+    ms64 = spmv_ms(fg.FG_FP64)
+    pk = peaks()
+    hbm = pk["hbm_gbs"] if pk else 6800.0
+    b32, b64 = spmv_bytes(nfree, nnz, True), spmv_bytes(nfree, nnz, False)
+    ach32 = b32 / (ms32 * 1e-3) / 1e9
+    ach64 = b64 / (ms64 * 1e-3) / 1e9
+
+    # ---- max over ranks ----
+    def maxr(v):
+        if not dist:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ms_mx = maxr(statistics.mean(tmx))
+    ms_64 = maxr(statistics.mean(t64))
+    ms_e2e = maxr(statistics.mean(te2e))
+    value = world * nfree / (ms_mx * 1e-3)
+    v64 = world * nfree / (ms_64 * 1e-3)
+    ve2e = world * nfree / (ms_e2e * 1e-3)
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    cb = None
+    if not args.no_cpu_baseline:
+        try:
+            cb = cpu_baseline(iters64, n)
+        except Exception as e:  # reported, never silently replaced
+            cb = {"value": None, "unit": "DOF/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+    srt = sorted(tmx)
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mx, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 matrix/SpMV/Jacobi + fp64 residual/dots/refinement",
+        "data": f"synthetic (PCG64 seed {SEED}): perturbed vertices U(+-0.15h), k=exp(N(0,1)) per cell, f=1",
+        "config": {"workload": f"poisson_q2_{n}^3_perturbed_lognormal_jacobi_pcg_1e-8", "n": n, "order": 2,
+                   "num_free_dofs": nfree, "nnz_full": nnz, "nnz_upper": space.info.nnz_upper,
+                   "precond": "jacobi", "rtol": 1e-8, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (FP32 CSR %.1f GB, FP64 CSR %.1f GB)" % (b32 / 1e9, b64 / 1e9),
+                   "symbolic_s": t_symbolic},
+        "p50_ms": srt[len(srt) // 2], "p99_ms": srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))],
+        "iterations": imx[-1]["iterations"], "outer_iterations": imx[-1]["outer_iterations"],
+        "error_vs_fp64": err_vs_fp64,
+        "fp64": {"value": v64, "ms_per_step": ms_64, "iterations": iters64, "dtype": "f64"},
+        "mixed_vs_fp64": value / v64,
+        "e2e": {"value": ve2e, "unit": "DOF/s", "h2d_bytes_per_step": int(coef.nbytes),
+                "d2h_bytes_per_step": int(nfree * 8), "ms_per_step": ms_e2e},
+        "roofline": {"bound": "hbm", "kernel": "k_spmv<float,float,1> (FP32 CSR SpMV + fused <Ap,p>)",
+                     "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
+                     "peak_source": "of measured" if pk else "of fallback", "traffic": None,
+                     "bytes_per_launch": b32, "ms_per_launch": ms32},
+        "roofline_fp64": {"kernel": "k_spmv<double,double,1>", "achieved": ach64, "frac": ach64 / hbm,
+                          "bytes_per_launch": b64, "ms_per_launch": ms64},
+        "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

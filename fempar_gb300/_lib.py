@@ -26,7 +26,7 @@ FG_RES_RES, FG_RES_RHS, FG_DELTA_RHS, FG_DELTA_DELTA, FG_RES_NRMGIVEN_RHS_NRMGIV
 # every symbol include/fempar_gpu.h declares
 EXPORTS = [
     "fg_status_string", "fg_last_error", "fg_version",
-    "fg_ctx_create", "fg_ctx_destroy", "fg_ctx_memory",
+    "fg_ctx_create", "fg_ctx_destroy", "fg_ctx_memory", "fg_ctx_get_stream", "fg_ctx_kernel_launches",
     "fg_mesh_create_structured", "fg_mesh_destroy",
     "fg_space_create", "fg_space_destroy", "fg_space_get_info", "fg_space_get_dof_map",
     "fg_space_get_dirichlet_coords",
@@ -74,6 +74,7 @@ class SolveInfo(C.Structure):
         ("error_estimate", C.c_double),
         ("tolerance", C.c_double),
         ("solve_ms", C.c_double),
+        ("kernel_launches", C.c_int64),
     ]
 
 
@@ -120,6 +121,8 @@ def lib():
         "fg_ctx_create": (i32, [i32, C.c_uint64, pp]),
         "fg_ctx_destroy": (i32, [vp]),
         "fg_ctx_memory": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+        "fg_ctx_get_stream": (i32, [vp, pp]),
+        "fg_ctx_kernel_launches": (i32, [vp, C.POINTER(C.c_int64)]),
         "fg_mesh_create_structured": (i32, [vp, i32, vp, vp, vp, pp]),
         "fg_mesh_destroy": (i32, [vp]),
         "fg_space_create": (i32, [vp, i32, i32, vp, i32, pp]),

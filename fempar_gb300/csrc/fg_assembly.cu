@@ -354,6 +354,7 @@ fg_status system_interpolate_dirichlet(fg_system* sys, int boundary_fn, const do
     for (int i = 0; i < 8; ++i) s.prm[i] = prm[i];
     s.qp = nullptr;
     k_dirichlet_values<<<nblk(sp->ndir, 256), 256, 0, ctx->stream>>>(sp->ndir, xyz, boundary_fn, s, sys->d_gvals);
+    ctx->launches += 2;  // coordinates + values
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { set_error("dirichlet values: %s", cudaGetErrorString(e)); st = FG_ERR_CUDA; }
   }
@@ -380,6 +381,7 @@ static fg_status launch_poisson(fg_system* sys) {
     attr_set = true;
   }
   const unsigned grid = nblk(ncells, S::WARPS);
+  ctx->launches += sp->nfree > 0 ? 2 : 1;
   k_integrate_poisson<P><<<grid, S::WARPS * 32, smem, ctx->stream>>>(
       g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof, sys->d_gvals, sys->d_coef, sys->integ.coef_const, src,
       sys->d_elmat, sys->d_elvec);

@@ -317,6 +317,7 @@ fg_status system_prepare_diag(fg_system* sys) {
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_idiag32, sizeof(float) * (n > 0 ? n : 1)));
   }
   if (n > 0) {
+    ctx->launches += 1;
     k_inv_diag<<<nblk(n, 256), 256, 0, ctx->stream>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, sys->d_idiag,
                                                        sys->d_idiag32);
     FG_CUDA_TRY(cudaGetLastError());

@@ -47,6 +47,17 @@ class Context:
         L.check(L.lib().fg_ctx_memory(self.h, C.byref(used), C.byref(budget)), "fg_ctx_memory")
         return used.value, budget.value
 
+    def stream_handle(self) -> int:
+        """cudaStream_t of the context (e.g. for torch.cuda.ExternalStream)."""
+        s = C.c_void_p()
+        L.check(L.lib().fg_ctx_get_stream(self.h, C.byref(s)), "fg_ctx_get_stream")
+        return s.value or 0
+
+    def kernel_launches(self) -> int:
+        c = C.c_int64()
+        L.check(L.lib().fg_ctx_kernel_launches(self.h, C.byref(c)), "fg_ctx_kernel_launches")
+        return c.value
+
     def close(self):
         if getattr(self, "h", None):
             L.lib().fg_ctx_destroy(self.h)
@@ -285,9 +296,11 @@ class IterativeLinearSolver:
         self.params.precond = L.FG_PREC_JACOBI if str(M).lower() == "jacobi" else L.FG_PREC_NONE
         return self
 
-    def solve(self, b=None, x0=None, raise_on_nonconvergence=False):
+    def solve(self, b=None, x0=None, raise_on_nonconvergence=False, out=None):
         n = self.A.space.num_free_dofs
-        x = np.zeros(n)
+        x = np.zeros(n) if out is None else out
+        if x.dtype != np.float64 or x.size != n or not x.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float64 array of num_free_dofs entries")
         info = L.SolveInfo()
         bb = None if b is None else np.ascontiguousarray(b, dtype=np.float64)
         xx0 = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
