@@ -273,24 +273,36 @@ def main():
     op.compute()
 
     # ---- dominant kernel: SpMV, timed on the library's stream ----
-    def spmv_ms(precision, reps=10):
+    def spmv_ms(precision, reps=20):
+        # the solver's SELL SpMV alone, back to back on the library's stream (matrix >> L2)
         if precision == fg.FG_MIXED:
             xv = torch.rand(nfree, dtype=torch.float32, device=f"cuda:{local}")
         else:
             xv = torch.rand(nfree, dtype=torch.float64, device=f"cuda:{local}")
         yv = torch.empty_like(xv)
-        op.apply_device(xv, yv, precision)
+        sync_all()
+        op.apply_solver_layout_device(xv, yv, precision, reps=2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        op.apply_solver_layout_device(xv, yv, precision, reps=reps)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def assembly_ms(reps=3):
+        op.integration = integ_dev
         sync_all()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(reps):
-            op.apply_device(xv, yv, precision)
+            op.compute()
         e1.record(stream)
         e1.synchronize()
         return e0.elapsed_time(e1) / reps
 
     ms32 = spmv_ms(fg.FG_MIXED)
     ms64 = spmv_ms(fg.FG_FP64)
+    ms_asm = assembly_ms()
     pk = peaks()
     hbm = pk["hbm_gbs"] if pk else 6800.0
     b32, b64 = spmv_bytes(nfree, nnz, True), spmv_bytes(nfree, nnz, False)
@@ -334,16 +346,17 @@ def main():
                    "symbolic_s": t_symbolic},
         "p50_ms": srt[len(srt) // 2], "p99_ms": srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))],
         "iterations": imx[-1]["iterations"], "outer_iterations": imx[-1]["outer_iterations"],
+        "assembly_ms": ms_asm, "solve_ms": imx[-1]["solve_ms"],
         "error_vs_fp64": err_vs_fp64,
         "fp64": {"value": v64, "ms_per_step": ms_64, "iterations": iters64, "dtype": "f64"},
         "mixed_vs_fp64": value / v64,
         "e2e": {"value": ve2e, "unit": "DOF/s", "h2d_bytes_per_step": int(coef.nbytes),
                 "d2h_bytes_per_step": int(nfree * 8), "ms_per_step": ms_e2e},
-        "roofline": {"bound": "hbm", "kernel": "k_spmv<float,float,1> (FP32 CSR SpMV + fused <Ap,p>)",
+        "roofline": {"bound": "hbm", "kernel": "k_sell_spmv<float> (FP32 SELL-32-256 SpMV)",
                      "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
                      "peak_source": "of measured" if pk else "of fallback", "traffic": None,
                      "bytes_per_launch": b32, "ms_per_launch": ms32},
-        "roofline_fp64": {"kernel": "k_spmv<double,double,1>", "achieved": ach64, "frac": ach64 / hbm,
+        "roofline_fp64": {"kernel": "k_sell_spmv<double>", "achieved": ach64, "frac": ach64 / hbm,
                           "bytes_per_launch": b64, "ms_per_launch": ms64},
         "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches,
     }

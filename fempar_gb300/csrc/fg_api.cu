@@ -220,6 +220,10 @@ static void space_free(fg_space* sp) {
   dev_free(ctx, sp->d_dir2lat);
   dev_free(ctx, sp->d_rowptr);
   dev_free(ctx, sp->d_col);
+  dev_free(ctx, sp->d_perm);
+  dev_free(ctx, sp->d_iperm);
+  dev_free(ctx, sp->d_sptr);
+  dev_free(ctx, sp->d_scol);
   delete sp;
 }
 
@@ -256,6 +260,11 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
   fg_status s = upload_tables(ctx, sp->tab, sp->dtab);
   if (s == FG_OK) s = space_number_dofs(sp);
   if (s == FG_OK) s = space_build_pattern(sp);
+  if (s == FG_OK) s = space_build_sell(sp);
+  if (s == FG_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { set_error("space: %s", cudaGetErrorString(e)); s = FG_ERR_CUDA; }
+  }
   if (s != FG_OK) {
     space_free(sp);
     return s;
@@ -312,7 +321,7 @@ fg_status fg_space_get_dirichlet_coords(fg_space* sp, double* xyz) {
 static void system_free(fg_system* sys) {
   fg_ctx* ctx = sys->space->mesh->ctx;
   void* ptrs[] = {sys->d_val, sys->d_val32, sys->d_rhs, sys->d_gvals, sys->d_elmat, sys->d_elvec, sys->d_coef,
-                  sys->d_qpsrc, sys->d_idiag, sys->d_idiag32, sys->d_work, sys->d_work32, sys->d_red, sys->d_ticket};
+                  sys->d_qpsrc, sys->d_sval, sys->d_sval32, sys->d_idiag, sys->d_idiag32, sys->d_work, sys->d_work32, sys->d_red, sys->d_ticket};
   for (void* p : ptrs) dev_free(ctx, p);
   delete sys;
 }
@@ -345,6 +354,7 @@ static fg_status numeric_phase(fg_system* sys, const fg_integrand* g) {
     FG_TRY(system_interpolate_dirichlet(sys, g->boundary_fn, g->fn_param));
   }
   FG_TRY(system_assemble(sys));
+  FG_TRY(system_fill_sell(sys));
   FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return FG_OK;
 }
@@ -360,7 +370,8 @@ fg_status fg_assemble(fg_space* sp, const fg_integrand* g, fg_system** out) {
   fg_status s = FG_OK;
   auto A = [&](void** p, size_t b) { if (s == FG_OK) s = dev_alloc(ctx, p, b); };
   A((void**)&sys->d_val, sizeof(double) * (sp->nnz > 0 ? sp->nnz : 1));
-  A((void**)&sys->d_val32, sizeof(float) * (sp->nnz > 0 ? sp->nnz : 1));
+  A((void**)&sys->d_sval, sizeof(double) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1));
+  A((void**)&sys->d_sval32, sizeof(float) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1));
   A((void**)&sys->d_rhs, sizeof(double) * (sp->nfree > 0 ? sp->nfree : 1));
   A((void**)&sys->d_gvals, sizeof(double) * (sp->ndir > 0 ? sp->ndir : 1));
   A((void**)&sys->d_elmat, sizeof(double) * ncells * nd * nd);
@@ -445,6 +456,13 @@ fg_status fg_system_spmv_device(fg_system* sys, int precision, const void* x, vo
   FG_TRY(system_spmv(sys, precision, x, y, ctx->stream));
   FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return FG_OK;
+}
+
+fg_status fg_system_spmv_solver_layout_device(fg_system* sys, int precision, const void* x_slot, void* y_slot,
+                                              int reps) {
+  FG_CHECK_ARG(sys && x_slot && y_slot && reps >= 0, "system/x/y/reps");
+  FG_DEVICE_GUARD(sys->space->mesh->ctx);
+  return system_spmv_slot(sys, precision, x_slot, y_slot, reps, sys->space->mesh->ctx->stream);
 }
 
 static fg_status check_params(const fg_solver_params* p) {

@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(256)
   for (int t = lane; t < len; t += 32) {
     double v = acc[t];
     val[s + t] = v;
-    val32[s + t] = (float)v;
+    if (val32) val32[s + t] = (float)v;
   }
   if (lane == 0) rhs[r] = rsum;
 }

@@ -102,6 +102,12 @@ struct fg_space {
   int32_t* d_col = nullptr;       // nnz
   int64_t nnz_upper = 0;
   int box_cap = 0;                // power-of-two capacity of a row's neighbour box
+  // SELL-C-sigma pattern of the same matrix (solver layout, slot order)
+  int64_t nslices = 0, sell_nnz = 0;
+  int32_t* d_perm = nullptr;      // slot -> row
+  int32_t* d_iperm = nullptr;     // row -> slot
+  int64_t* d_sptr = nullptr;      // nslices+1 entry offsets
+  int32_t* d_scol = nullptr;      // sell_nnz column slots
 };
 
 struct fg_system {
@@ -114,8 +120,10 @@ struct fg_system {
   double* d_elvec = nullptr;      // ncells*nd
   double* d_coef = nullptr;       // ncells
   double* d_qpsrc = nullptr;      // optional per-qp source
-  double* d_idiag = nullptr;      // nfree inverse diagonal (FP64)
-  float* d_idiag32 = nullptr;     // nfree inverse diagonal (FP32)
+  double* d_sval = nullptr;       // sell_nnz FP64 values (SELL layout)
+  float* d_sval32 = nullptr;      // sell_nnz FP32 values (SELL layout)
+  double* d_idiag = nullptr;      // nfree inverse diagonal (FP64, slot order)
+  float* d_idiag32 = nullptr;     // nfree inverse diagonal (FP32, slot order)
   // solver work vectors (allocated on first solve)
   double* d_work = nullptr;       // FP64 work area
   float* d_work32 = nullptr;      // FP32 work area
@@ -143,9 +151,14 @@ fg_status space_export_upper(fg_space* sp, const double* d_val, int one_based, i
 fg_status system_interpolate_dirichlet(fg_system* sys, int boundary_fn, const double* prm);
 fg_status system_assemble(fg_system* sys);
 
+// fg_sell.cu
+fg_status space_build_sell(fg_space* sp);
+fg_status system_fill_sell(fg_system* sys);
+
 // fg_solver.cu
 fg_status system_prepare_diag(fg_system* sys);
 fg_status system_spmv(fg_system* sys, int precision, const void* x, void* y, cudaStream_t st);
+fg_status system_spmv_slot(fg_system* sys, int precision, const void* x, void* y, int reps, cudaStream_t st);
 fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double* d_b, const double* d_x0,
                        double* d_x, fg_solve_info* info);
 

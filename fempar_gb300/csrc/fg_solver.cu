@@ -1,21 +1,31 @@
-// fg_solver.cu -- CSR SpMV and the preconditioned CG of the reference, on the device.
+// fg_solver.cu -- SELL-C-sigma SpMV and the preconditioned CG, on the device.
 //
-// FP64 path: the operation sequence of cg_solve_body (Sources/Lib/LinearAlgebra/
-// IterativeLinearSolver/cg.f90:101-238) with its stopping criteria (:279-407), Jacobi
-// z = D^-1 r (jacobi_preconditioner.f90:356-412):
+// FP64 path (the drop-in): the operation sequence of cg_solve_body
+// (Sources/Lib/LinearAlgebra/IterativeLinearSolver/cg.f90:101-238) and its stopping
+// criteria (:279-407), with Jacobi z = D^-1 r (jacobi_preconditioner.f90:356-412):
 //   r = b - A x0; z = M r; r_z = <r,z>; p = z
 //   loop: Ap = A p; alpha = r_z/<Ap,p>; x += alpha p; r -= alpha Ap; test;
 //         z = M r; beta = (1/r_z) * <r,z>; r_z = <r,z>; p = z + beta p
-// Each iteration is three kernels: SpMV with the fused <Ap,p>, the x/r update with the
-// fused norms, and the p update.  Scalars (alpha, beta, r_z, the iteration counter and
-// the done flag) stay on the device; kernels of an iteration that follows convergence
-// return at once, so the host polls only every few iterations (CUDA-graph replays of a
-// fixed chunk of iterations).  Reductions are deterministic: fixed grid, fixed
-// per-thread index sets, block partials summed in index order by the last block.
+// Three kernels per iteration: SpMV with the fused <Ap,p>, the x/r update with the fused
+// norms and the convergence test, and the p update.  Scalars and the done flag stay on
+// the device; kernels of iterations after the stop return at once, so the host polls
+// only every few iterations, replaying a CUDA graph of a fixed chunk of iterations.
 //
-// Mixed path: FP64 outer iterative refinement r = b - A x (FP64 matrix), inner PCG on
-// the FP32 copy of the matrix with FP32 vectors and FP32 Jacobi, inner products and
-// norms accumulated in FP64, x += correction in FP64.
+// Mixed path: CG on the FP32 copy of the matrix with FP32 vectors and FP32 Jacobi, with
+// "reliable updates" in FP64: whenever the recursive FP32 residual has dropped by a factor
+// delta (default 0.1) since the last update, or its estimate reaches the tolerance, the
+// FP32 correction is folded into the FP64 solution, the true residual r = b - A x is
+// recomputed with the FP64 matrix, the FP32 residual is replaced by it (rescaled to unit
+// norm) and the search direction is kept (rescaled).  The solve stops on the FP64 true
+// residual.  Keeping the direction keeps the iteration count close to the FP64 CG's, where
+// restarting an inner solve per refinement step would lose the Krylov space each time.
+//
+// Inner products.  GB300 runs FP64 FMA and FP32<->FP64 conversion at about 0.5 Tera-op/s,
+// some 70x below FP32.  FP64-path dots accumulate in FP64.  FP32-path dots form each
+// product exactly as an FP32 pair (p = a*b, e = fma(a,b,-p)) and accumulate it with a
+// compensated (double-float) sum; each thread's sum is converted once and the block and
+// grid totals are added in FP64.  Reductions are deterministic: fixed grid, fixed
+// per-thread index sets, block partials summed in index order by the last block.
 #include <cmath>
 #include <cstring>
 
@@ -25,14 +35,39 @@ namespace fg {
 
 static constexpr int RB = 256;  // threads per block of the vector / SpMV kernels
 
-// device scalar slots
-enum { S_RZ = 0, S_ALPHA, S_BETA, S_ERR, S_TOL, S_APP, S_RNRMM, S_RZNEW, S_BNRM, S_R0NRM, S_COUNT = 16 };
-enum { I_ITER = 0, I_DONE, I_CONV, I_MAXIT, I_COUNT = 8 };
+enum { S_RZ = 0, S_ALPHA, S_BETA, S_ERR, S_TOL, S_APP, S_RNRMM, S_BNRM, S_R0NRM, S_SIGMA, S_RMAX, S_DELTA, S_RNSCALED,
+       S_COUNT = 16 };
+enum { I_ITER = 0, I_DONE, I_CONV, I_MAXIT, I_FLAG, I_COUNT = 8 };
+enum { FLAG_NONE = 0, FLAG_UPDATE = 1, FLAG_CHECK = 2, FLAG_MAXIT = 3 };
 
 struct RedBuf {
-  double* part;       // [4][nblocks]
+  double* part;  // [4][nblocks]
   unsigned* ticket;
   int nblocks;
+};
+
+// per-thread dot accumulators
+template <typename VT>
+struct Acc;
+template <>
+struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct Acc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = fmaf(a, b, -p);  // exact: a*b = p + pe
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));  // TwoSum error
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, pe));
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
 template <int NV>
@@ -87,39 +122,60 @@ __device__ __forceinline__ bool block_reduce_last(double (&v)[NV], const RedBuf&
   return true;
 }
 
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+
 // ---------------------------------------------------------------------------
-// SpMV, warp per row, rows strided over a fixed grid.  MODE 0: y = A x.
-// MODE 1: y = A x and <y,x> reduced; sets alpha = r_z/<Ap,p>.
-// MODE 2: r = b - A x and <r,r> reduced (residual of the refinement loop).
-template <typename MT, typename VT, int MODE>
+// SELL SpMV, warp per slice, lane per row, slices strided over a fixed grid.
+// MODE 0: y = A x.  MODE 1: y = A x, <y,x> reduced, alpha = r_z/<Ap,p>.
+// MODE 2: y = b - A x (b FP64), <y,y> reduced into S_ERR as a norm.
+template <typename T, int MODE>
 __global__ void __launch_bounds__(RB)
-    k_spmv(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci, const MT* __restrict__ av,
-           const VT* __restrict__ x, VT* __restrict__ y, const double* __restrict__ b, RedBuf rb, double* S,
-           const int* I) {
+    k_sell_spmv(int64_t nslices, int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+                const T* __restrict__ sval, const T* __restrict__ x, T* __restrict__ y, const double* __restrict__ b,
+                RedBuf rb, double* S, const int* I) {
   if (MODE == 1 && I[I_DONE]) return;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * RB + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
-  double dsum = 0.0;
-  for (int64_t r = warp; r < n; r += nwarps) {
-    const int64_t s = rp[r], e = rp[r + 1];
-    double acc = 0.0;
-    for (int64_t k = s + lane; k < e; k += 32) acc += (double)av[k] * (double)x[ci[k]];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if (lane == 0) {
+  Acc<T> dot;
+  for (int64_t s = warp; s < nslices; s += nwarps) {
+    const int64_t base = sptr[s];
+    const int w = (int)((sptr[s + 1] - base) >> 5);
+    const T* vp = sval + base + lane;
+    const int32_t* cp = scol + base + lane;
+    T acc = 0;
+    int j = 0;
+    for (; j + 4 <= w; j += 4) {
+      const T v0 = __ldcs(vp), v1 = __ldcs(vp + 32), v2 = __ldcs(vp + 64), v3 = __ldcs(vp + 96);
+      const int32_t c0 = __ldcs(cp), c1 = __ldcs(cp + 32), c2 = __ldcs(cp + 64), c3 = __ldcs(cp + 96);
+      const T x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+      acc = fmaT(v0, x0, acc);
+      acc = fmaT(v1, x1, acc);
+      acc = fmaT(v2, x2, acc);
+      acc = fmaT(v3, x3, acc);
+      vp += 128;
+      cp += 128;
+    }
+    for (; j < w; ++j) {
+      acc = fmaT(__ldcs(vp), __ldg(x + __ldcs(cp)), acc);
+      vp += 32;
+      cp += 32;
+    }
+    const int64_t slot = s * 32 + lane;
+    if (slot < n) {
       if (MODE == 2) {
-        double rr = b[r] - acc;
-        y[r] = (VT)rr;
-        dsum += rr * rr;
+        const T rr = (T)(b[slot] - (double)acc);
+        y[slot] = rr;
+        dot.add(rr, rr);
       } else {
-        y[r] = (VT)acc;
-        if (MODE == 1) dsum += acc * (double)x[r];
+        y[slot] = acc;
+        if (MODE == 1) dot.add(acc, x[slot]);
       }
     }
   }
   if (MODE == 0) return;
-  double v[1] = {dsum}, tot[1];
+  double v[1] = {dot.value()}, tot[1];
   if (block_reduce_last<1>(v, rb, tot) && threadIdx.x == 0) {
     if (MODE == 1) {
       S[S_APP] = tot[0];
@@ -130,30 +186,28 @@ __global__ void __launch_bounds__(RB)
   }
 }
 
-// r = b - r (r holds A x0) or r = b; z = M r; p = z; reductions of <r,r>, <r,z>, <b,b>, <b,Mb>.
-template <typename VT>
+// FP64 path start: r = b - r (r holds A x0) or r = b; z = M r; p = z; <r,r>, <r,z>, <b,b>, <b,Mb>.
 __global__ void __launch_bounds__(RB)
-    k_init(int64_t n, const double* __restrict__ b, int have_x0, VT* __restrict__ r, VT* __restrict__ p,
-           const VT* __restrict__ idiag, int precond, int criterion, double rtol, double atol, int maxit, RedBuf rb,
-           double* S, int* I) {
-  double rr = 0.0, rz = 0.0, bb = 0.0, bmb = 0.0;
+    k_init64(int64_t n, const double* __restrict__ b, int have_x0, double* __restrict__ r, double* __restrict__ p,
+             const double* __restrict__ idiag, int precond, int criterion, double rtol, double atol, int maxit,
+             RedBuf rb, double* S, int* I) {
+  Acc<double> rr, rz, bb, bmb;
   for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
-    double bi = b[i];
-    VT ri = have_x0 ? (VT)(bi - (double)r[i]) : (VT)bi;
-    VT zi = precond ? idiag[i] * ri : ri;
-    VT mbi = precond ? (VT)((double)idiag[i] * bi) : (VT)bi;
+    const double bi = b[i];
+    const double ri = have_x0 ? bi - r[i] : bi;
+    const double zi = precond ? idiag[i] * ri : ri;
     r[i] = ri;
     p[i] = zi;
-    rr += (double)ri * (double)ri;
-    rz += (double)ri * (double)zi;
-    bb += bi * bi;
-    bmb += bi * (double)mbi;
+    rr.add(ri, ri);
+    rz.add(ri, zi);
+    bb.add(bi, bi);
+    bmb.add(bi, precond ? idiag[i] * bi : bi);
   }
-  double v[4] = {rr, rz, bb, bmb}, tot[4];
+  double v[4] = {rr.value(), rz.value(), bb.value(), bmb.value()}, tot[4];
   if (block_reduce_last<4>(v, rb, tot) && threadIdx.x == 0) {
     S[S_RZ] = tot[1];
     S[S_RNRMM] = sqrt(tot[1]);
-    double rn = sqrt(tot[0]), bn = sqrt(tot[2]), bnm = sqrt(tot[3]);
+    const double rn = sqrt(tot[0]), bn = sqrt(tot[2]), bnm = sqrt(tot[3]);
     S[S_R0NRM] = rn;
     S[S_BNRM] = bn;
     double tol = 0.0;
@@ -170,41 +224,40 @@ __global__ void __launch_bounds__(RB)
     I[I_DONE] = 0;
     I[I_CONV] = 0;
     I[I_MAXIT] = maxit;
+    I[I_FLAG] = FLAG_NONE;
   }
 }
 
-// x += alpha p; r -= alpha Ap; convergence test; beta and r_z for the next iteration.
-template <typename VT>
+// FP64 path: x += alpha p; r -= alpha Ap; the reference's convergence test; beta, r_z.
+template <bool PRECOND, bool NEED_PP>
 __global__ void __launch_bounds__(RB)
-    k_update(int64_t n, VT* __restrict__ x, VT* __restrict__ r, const VT* __restrict__ p, const VT* __restrict__ Ap,
-             const VT* __restrict__ idiag, int precond, int criterion, double rtol, double atol, RedBuf rb, double* S,
-             int* I) {
+    k_update64(int64_t n, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+               const double* __restrict__ Ap, const double* __restrict__ idiag, int criterion, double rtol,
+               double atol, RedBuf rb, double* S, int* I) {
   if (I[I_DONE]) return;
-  const double alpha = S[S_ALPHA];
-  const VT a = (VT)alpha;
-  double rr = 0.0, rz = 0.0, pp = 0.0;
+  const double a = S[S_ALPHA];
+  Acc<double> rr, rz, pp;
   for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
-    VT pi = p[i];
-    x[i] = a * pi + x[i];
-    VT ri = -a * Ap[i] + r[i];
+    const double pi = p[i];
+    x[i] = fma(a, pi, x[i]);
+    const double ri = fma(-a, Ap[i], r[i]);
     r[i] = ri;
-    VT zi = precond ? idiag[i] * ri : ri;
-    rr += (double)ri * (double)ri;
-    rz += (double)ri * (double)zi;
-    pp += (double)pi * (double)pi;
+    rr.add(ri, ri);
+    if (PRECOND) rz.add(ri, idiag[i] * ri);
+    if (NEED_PP) pp.add(pi, pi);
   }
-  double v[3] = {rr, rz, pp}, tot[3];
+  double v[3] = {rr.value(), PRECOND ? rz.value() : rr.value(), pp.value()}, tot[3];
   if (block_reduce_last<3>(v, rb, tot) && threadIdx.x == 0) {
     const int it = I[I_ITER] + 1;
     I[I_ITER] = it;
     double err = S[S_ERR];
     if (it == 1 && (criterion == FG_DELTA_RHS || criterion == FG_DELTA_DELTA)) {
-      err = alpha * sqrt(tot[2]);
+      err = a * sqrt(tot[2]);
       if (criterion == FG_DELTA_DELTA) S[S_TOL] = rtol * err + atol;
     }
     switch (criterion) {
       case FG_RES_RES: case FG_RES_RHS: err = sqrt(tot[0]); break;
-      case FG_DELTA_RHS: case FG_DELTA_DELTA: if (it != 1) err = alpha * sqrt(tot[2]); break;
+      case FG_DELTA_RHS: case FG_DELTA_DELTA: if (it != 1) err = a * sqrt(tot[2]); break;
       default: err = S[S_RNRMM]; break;
     }
     S[S_ERR] = err;
@@ -223,88 +276,168 @@ __global__ void __launch_bounds__(RB)
 }
 
 // p = z + beta p
-template <typename VT>
+template <typename T, bool PRECOND>
 __global__ void __launch_bounds__(RB)
-    k_pupdate(int64_t n, VT* __restrict__ p, const VT* __restrict__ r, const VT* __restrict__ idiag, int precond,
-              const double* S, const int* I) {
+    k_pupdate(int64_t n, T* __restrict__ p, const T* __restrict__ r, const T* __restrict__ idiag, const double* S,
+              const int* I) {
   if (I[I_DONE]) return;
-  const VT beta = (VT)S[S_BETA];
+  const T beta = (T)S[S_BETA];
   for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
-    VT ri = r[i];
-    VT zi = precond ? idiag[i] * ri : ri;
-    p[i] = zi + beta * p[i];
+    const T ri = r[i];
+    const T zi = PRECOND ? idiag[i] * ri : ri;
+    p[i] = fmaT(beta, p[i], zi);
   }
 }
 
-// inverse diagonal (extract_diagonal by binary search, csr_sparse_matrix.f90:4231-4256)
-__global__ void k_inv_diag(int64_t n, const int64_t* rp, const int32_t* ci, const double* av, double* d64, float* d32) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= n) return;
+// Mixed path, FP32 iteration: x += alpha p; r -= alpha Ap; reliable-update / stop decision.
+template <bool PRECOND>
+__global__ void __launch_bounds__(RB)
+    k_update32(int64_t n, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
+               const float* __restrict__ Ap, const float* __restrict__ idiag, RedBuf rb, double* S, int* I) {
+  if (I[I_DONE]) return;
+  const float a = (float)S[S_ALPHA];
+  Acc<float> rr, rz;
+  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+    x[i] = fmaf(a, p[i], x[i]);
+    const float ri = fmaf(-a, Ap[i], r[i]);
+    r[i] = ri;
+    rr.add(ri, ri);
+    if (PRECOND) rz.add(ri, idiag[i] * ri);
+  }
+  double v[2] = {rr.value(), PRECOND ? rz.value() : rr.value()}, tot[2];
+  if (block_reduce_last<2>(v, rb, tot) && threadIdx.x == 0) {
+    const int it = I[I_ITER] + 1;
+    I[I_ITER] = it;
+    const double rn = sqrt(tot[0]);  // residual norm in the current scale
+    S[S_RNSCALED] = rn;
+    const double est = rn * S[S_SIGMA];
+    int flag = FLAG_NONE;
+    if (est <= S[S_TOL]) flag = FLAG_CHECK;
+    else if (rn < S[S_DELTA] * S[S_RMAX]) flag = FLAG_UPDATE;
+    else if (it >= I[I_MAXIT]) flag = FLAG_MAXIT;
+    if (rn > S[S_RMAX]) S[S_RMAX] = rn;
+    S[S_APP] = tot[1];  // r_z of the new residual (used by the reliable update for beta)
+    if (flag != FLAG_NONE) {
+      I[I_FLAG] = flag;
+      I[I_DONE] = 1;
+    } else {
+      const double beta = tot[1] / S[S_RZ];
+      S[S_RZ] = tot[1];
+      S[S_BETA] = beta;
+    }
+  }
+}
+
+// x64 += sigma * x32; x32 = 0
+__global__ void k_fold(int64_t n, double sigma, float* __restrict__ x32, double* __restrict__ x64) {
+  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+    x64[i] = fma(sigma, (double)x32[i], x64[i]);
+    x32[i] = 0.f;
+  }
+}
+
+// r32 = r64/sigma_new; r_z of it; beta for keeping the direction (first: p = z).
+template <bool PRECOND>
+__global__ void __launch_bounds__(RB)
+    k_refresh(int64_t n, const double* __restrict__ r64, float* __restrict__ r32, const float* __restrict__ idiag,
+              int first, RedBuf rb, double* S, int* I) {
+  const double inv = 1.0 / S[S_ERR];  // S_ERR = ||b - A x64|| from the FP64 residual SpMV
+  Acc<float> rz;
+  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+    const float ri = (float)(r64[i] * inv);
+    r32[i] = ri;
+    rz.add(ri, PRECOND ? idiag[i] * ri : ri);
+  }
+  double v[1] = {rz.value()}, tot[1];
+  if (block_reduce_last<1>(v, rb, tot) && threadIdx.x == 0) {
+    const double sig_old = S[S_SIGMA], sig_new = S[S_ERR];
+    if (first) {
+      S[S_BETA] = 0.0;
+    } else {
+      // old r_z and direction expressed in the new scale: rz*(s_old/s_new)^2, p*(s_old/s_new)
+      const double q = sig_old / sig_new;
+      const double beta = tot[0] / (S[S_RZ] * q * q);
+      S[S_BETA] = beta * q;
+    }
+    S[S_RZ] = tot[0];
+    S[S_SIGMA] = sig_new;
+    S[S_RMAX] = 1.0;
+    I[I_DONE] = 0;
+    I[I_FLAG] = FLAG_NONE;
+  }
+}
+
+// inverse diagonal in slot order (extract_diagonal by binary search, csr_sparse_matrix.f90:4231-4256)
+__global__ void k_inv_diag(int64_t n, const int64_t* rp, const int32_t* ci, const double* av, const int32_t* perm,
+                           double* d64, float* d32) {
+  int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (slot >= n) return;
+  const int64_t r = perm[slot];
   int64_t lo = rp[r], hi = rp[r + 1];
   while (lo < hi) {
     int64_t m = (lo + hi) >> 1;
     if (ci[m] < r) lo = m + 1;
     else hi = m;
   }
-  double d = (lo < rp[r + 1] && ci[lo] == r) ? av[lo] : 0.0;
-  double inv = 1.0 / d;
-  d64[r] = inv;
-  d32[r] = (float)inv;
+  const double d = (lo < rp[r + 1] && ci[lo] == r) ? av[lo] : 0.0;
+  const double inv = 1.0 / d;
+  d64[slot] = inv;
+  d32[slot] = (float)inv;
 }
 
-__global__ void k_axpy_f2d(int64_t n, double s, const float* d, double* x) {
-  int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x;
-  if (i < n) x[i] = x[i] + s * (double)d[i];
+template <typename TS, typename TD>
+__global__ void k_to_slot(int64_t n, const int32_t* __restrict__ perm, const TS* __restrict__ src, TD* __restrict__ dst) {
+  int64_t s = blockIdx.x * (int64_t)RB + threadIdx.x;
+  if (s < n) dst[s] = (TD)src[perm[s]];
 }
-__global__ void k_scale(int64_t n, const double* a, double s, double* o) {
-  int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x;
-  if (i < n) o[i] = a[i] * s;
-}
-__global__ void __launch_bounds__(RB) k_nrm2(int64_t n, const double* a, RedBuf rb, double* S) {
-  double s = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) s += a[i] * a[i];
-  double v[1] = {s}, tot[1];
-  if (block_reduce_last<1>(v, rb, tot) && threadIdx.x == 0) S[S_BNRM] = sqrt(tot[0]);
+template <typename TS, typename TD>
+__global__ void k_from_slot(int64_t n, const int32_t* __restrict__ perm, const TS* __restrict__ src,
+                            TD* __restrict__ dst) {
+  int64_t s = blockIdx.x * (int64_t)RB + threadIdx.x;
+  if (s < n) dst[perm[s]] = (TD)src[s];
 }
 template <typename T>
 __global__ void k_fill(int64_t n, T* a, T v) {
   int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x;
   if (i < n) a[i] = v;
 }
+__global__ void k_set_flags(int* I, int done, int flag) {
+  I[I_DONE] = done;
+  I[I_FLAG] = flag;
+}
+__global__ void k_set_scalar(double* S, int slot, double v) { S[slot] = v; }
 
 static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 struct Work {
-  double *x, *r, *p, *Ap;   // FP64
+  double *x, *r, *p, *Ap, *b, *t;  // FP64, slot order
   float *x32, *r32, *p32, *Ap32;
   double* S;
   int* I;
   RedBuf rb;
-  unsigned grid_vec, grid_spmv;
+  unsigned grid;
 };
 
 static fg_status ensure_work(fg_system* sys, Work& w) {
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
   const int64_t n = sp->nfree > 0 ? sp->nfree : 1;
-  const unsigned gv = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nblk(n, RB), (int64_t)ctx->sm_count * 8));
   if (!sys->d_work) {
-    FG_TRY(dev_alloc(ctx, (void**)&sys->d_work, sizeof(double) * 4 * n));
+    FG_TRY(dev_alloc(ctx, (void**)&sys->d_work, sizeof(double) * 6 * n));
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_work32, sizeof(float) * 4 * n));
-    sys->red_blocks = (int)std::max<unsigned>(gv, (unsigned)ctx->sm_count * 8);
+    sys->red_blocks = ctx->sm_count * 8;
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_red, sizeof(double) * (4 * sys->red_blocks + S_COUNT) + sizeof(int) * I_COUNT));
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_ticket, sizeof(unsigned) * 4));
     FG_CUDA_TRY(cudaMemsetAsync(sys->d_ticket, 0, sizeof(unsigned) * 4, ctx->stream));
   }
-  w.x = sys->d_work; w.r = w.x + n; w.p = w.r + n; w.Ap = w.p + n;
+  w.x = sys->d_work; w.r = w.x + n; w.p = w.r + n; w.Ap = w.p + n; w.b = w.Ap + n; w.t = w.b + n;
   w.x32 = sys->d_work32; w.r32 = w.x32 + n; w.p32 = w.r32 + n; w.Ap32 = w.p32 + n;
   w.S = sys->d_red + 4 * sys->red_blocks;
   w.I = (int*)(w.S + S_COUNT);
   w.rb.part = sys->d_red;
   w.rb.ticket = sys->d_ticket;
   w.rb.nblocks = sys->red_blocks;
-  w.grid_vec = (unsigned)sys->red_blocks;
-  w.grid_spmv = (unsigned)sys->red_blocks;
+  w.grid = (unsigned)sys->red_blocks;
   return FG_OK;
 }
 
@@ -318,71 +451,120 @@ fg_status system_prepare_diag(fg_system* sys) {
   }
   if (n > 0) {
     ctx->launches += 1;
-    k_inv_diag<<<nblk(n, 256), 256, 0, ctx->stream>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, sys->d_idiag,
+    k_inv_diag<<<nblk(n, 256), 256, 0, ctx->stream>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, sp->d_perm, sys->d_idiag,
                                                        sys->d_idiag32);
     FG_CUDA_TRY(cudaGetLastError());
   }
   return FG_OK;
 }
 
+// y = A x in row order (device pointers): permute in, SELL SpMV, permute out.
 fg_status system_spmv(fg_system* sys, int precision, const void* x, void* y, cudaStream_t st) {
   fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
   Work w;
   FG_TRY(ensure_work(sys, w));
   const int64_t n = sp->nfree;
   if (n == 0) return FG_OK;
-  if (precision == FG_MIXED)
-    k_spmv<float, float, 0><<<w.grid_spmv, RB, 0, st>>>(n, sp->d_rowptr, sp->d_col, sys->d_val32, (const float*)x,
-                                                         (float*)y, nullptr, w.rb, w.S, w.I);
-  else
-    k_spmv<double, double, 0><<<w.grid_spmv, RB, 0, st>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, (const double*)x,
-                                                           (double*)y, nullptr, w.rb, w.S, w.I);
+  if (precision == FG_MIXED) {
+    k_to_slot<float, float><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, (const float*)x, w.p32);
+    k_sell_spmv<float, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval32, w.p32, w.Ap32,
+                                                nullptr, w.rb, w.S, w.I);
+    k_from_slot<float, float><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, w.Ap32, (float*)y);
+  } else {
+    k_to_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, (const double*)x, w.p);
+    k_sell_spmv<double, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.p, w.Ap,
+                                                 nullptr, w.rb, w.S, w.I);
+    k_from_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, w.Ap, (double*)y);
+  }
+  ctx->launches += 3;
   FG_CUDA_TRY(cudaGetLastError());
   return FG_OK;
 }
 
-// One CG iteration (3 kernels) for matrix type MT / vector type VT.
-template <typename MT, typename VT>
-static void launch_iteration(fg_system* sys, const Work& w, const MT* av, VT* x, VT* r, VT* p, VT* Ap, const VT* idiag,
-                             int precond, int criterion, double rtol, double atol, cudaStream_t st) {
+// SpMV of the solver layout alone (slot-order device vectors; timing of the dominant kernel).
+fg_status system_spmv_slot(fg_system* sys, int precision, const void* x, void* y, int reps, cudaStream_t st) {
   fg_space* sp = sys->space;
+  Work w;
+  FG_TRY(ensure_work(sys, w));
   const int64_t n = sp->nfree;
-  k_spmv<MT, VT, 1><<<w.grid_spmv, RB, 0, st>>>(n, sp->d_rowptr, sp->d_col, av, p, Ap, nullptr, w.rb, w.S, w.I);
-  k_update<VT><<<w.grid_vec, RB, 0, st>>>(n, x, r, p, Ap, idiag, precond, criterion, rtol, atol, w.rb, w.S, w.I);
-  k_pupdate<VT><<<w.grid_vec, RB, 0, st>>>(n, p, r, idiag, precond, w.S, w.I);
+  for (int k = 0; k < reps && n > 0; ++k) {
+    if (precision == FG_MIXED)
+      k_sell_spmv<float, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval32,
+                                                  (const float*)x, (float*)y, nullptr, w.rb, w.S, w.I);
+    else
+      k_sell_spmv<double, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval,
+                                                   (const double*)x, (double*)y, nullptr, w.rb, w.S, w.I);
+  }
+  sp->mesh->ctx->launches += reps;
+  FG_CUDA_TRY(cudaGetLastError());
+  return FG_OK;
 }
 
-// Run CG iterations until the device done flag is set.  Returns iterations / converged.
-template <typename MT, typename VT>
-static fg_status run_cg_loop(fg_system* sys, const Work& w, const MT* av, VT* x, VT* r, VT* p, VT* Ap, const VT* idiag,
-                             int precond, int criterion, double rtol, double atol, int check_every, int* h_I,
-                             double* h_S) {
-  fg_ctx* ctx = sys->space->mesh->ctx;
+// Launch one FP64 CG iteration (3 kernels).
+static void iter64(fg_system* sys, const Work& w, int precond, bool need_pp, int criterion, double rtol, double atol,
+                   cudaStream_t st) {
+  fg_space* sp = sys->space;
+  const int64_t n = sp->nfree;
+  k_sell_spmv<double, 1><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.p, w.Ap,
+                                               nullptr, w.rb, w.S, w.I);
+#define FG_UPD(P, Q) k_update64<P, Q><<<w.grid, RB, 0, st>>>(n, w.x, w.r, w.p, w.Ap, sys->d_idiag, criterion, rtol, atol, w.rb, w.S, w.I)
+  if (precond) { if (need_pp) FG_UPD(true, true); else FG_UPD(true, false); }
+  else { if (need_pp) FG_UPD(false, true); else FG_UPD(false, false); }
+#undef FG_UPD
+  if (precond) k_pupdate<double, true><<<w.grid, RB, 0, st>>>(n, w.p, w.r, sys->d_idiag, w.S, w.I);
+  else k_pupdate<double, false><<<w.grid, RB, 0, st>>>(n, w.p, w.r, sys->d_idiag, w.S, w.I);
+}
+
+// Launch one FP32 CG iteration of the mixed path (3 kernels).
+static void iter32(fg_system* sys, const Work& w, int precond, cudaStream_t st) {
+  fg_space* sp = sys->space;
+  const int64_t n = sp->nfree;
+  k_sell_spmv<float, 1><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval32, w.p32, w.Ap32,
+                                              nullptr, w.rb, w.S, w.I);
+  if (precond) {
+    k_update32<true><<<w.grid, RB, 0, st>>>(n, w.x32, w.r32, w.p32, w.Ap32, sys->d_idiag32, w.rb, w.S, w.I);
+    k_pupdate<float, true><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
+  } else {
+    k_update32<false><<<w.grid, RB, 0, st>>>(n, w.x32, w.r32, w.p32, w.Ap32, sys->d_idiag32, w.rb, w.S, w.I);
+    k_pupdate<float, false><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
+  }
+}
+
+// Capture `chunk` iterations into a graph and replay it until the device done flag is set.
+template <typename F>
+static fg_status run_chunks(fg_ctx* ctx, const Work& w, int chunk, F launch_iter, int* h_I, double* h_S) {
   cudaStream_t st = ctx->stream;
-  // capture a chunk of iterations into a graph, replay until done
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  for (int k = 0; k < check_every; ++k)
-    launch_iteration<MT, VT>(sys, w, av, x, r, p, Ap, idiag, precond, criterion, rtol, atol, st);
+  for (int k = 0; k < chunk; ++k) launch_iter();
   cudaError_t e = cudaStreamEndCapture(st, &graph);
   if (e != cudaSuccess) { set_error("graph capture: %s", cudaGetErrorString(e)); return FG_ERR_CUDA; }
   e = cudaGraphInstantiate(&exec, graph, 0);
-  if (e != cudaSuccess) { cudaGraphDestroy(graph); set_error("graph instantiate: %s", cudaGetErrorString(e)); return FG_ERR_CUDA; }
-  fg_status st_out = FG_OK;
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    set_error("graph instantiate: %s", cudaGetErrorString(e));
+    return FG_ERR_CUDA;
+  }
+  fg_status out = FG_OK;
   for (;;) {
     e = cudaGraphLaunch(exec, st);
-    ctx->launches += 3 * check_every;
+    ctx->launches += 3 * chunk;
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_I, w.I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) { set_error("cg loop: %s", cudaGetErrorString(e)); st_out = FG_ERR_CUDA; break; }
+    if (e != cudaSuccess) { set_error("cg loop: %s", cudaGetErrorString(e)); out = FG_ERR_CUDA; break; }
     if (h_I[I_DONE]) break;
-    if (!std::isfinite(h_S[S_ERR])) { st_out = FG_ERR_NUMERIC; set_error("non-finite residual"); break; }
+    if (!std::isfinite(h_S[S_ALPHA]) || !std::isfinite(h_S[S_RZ])) {
+      out = FG_ERR_NUMERIC;
+      set_error("non-finite CG scalars");
+      break;
+    }
   }
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
-  return st_out;
+  return out;
 }
 
 fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double* d_b, const double* d_x0,
@@ -393,13 +575,17 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
   const int64_t n = sp->nfree;
   fg_solve_info out;
   std::memset(&out, 0, sizeof(out));
-  if (n == 0) { out.converged = 1; if (info) *info = out; return FG_OK; }
+  if (n == 0) {
+    out.converged = 1;
+    if (info) *info = out;
+    return FG_OK;
+  }
   Work w;
   FG_TRY(ensure_work(sys, w));
   if (!sys->d_idiag) FG_TRY(system_prepare_diag(sys));
-  const double* b = d_b ? d_b : sys->d_rhs;
+  const double* b_row = d_b ? d_b : sys->d_rhs;
   const int precond = prm->precond == FG_PREC_JACOBI ? 1 : 0;
-  int check_every = prm->check_every > 0 ? prm->check_every : (n < 200000 ? 64 : 16);
+  const int chunk = prm->check_every > 0 ? prm->check_every : (n < 200000 ? 64 : 16);
   int h_I[I_COUNT];
   double h_S[S_COUNT];
   cudaEvent_t e0, e1;
@@ -408,74 +594,131 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
   cudaEventRecord(e0, st);
   const int64_t launches0 = ctx->launches;
   fg_status status = FG_OK;
+  // right-hand side and initial guess into slot order
+  k_to_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, b_row, w.b);
+  if (d_x0) k_to_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, d_x0, w.x);
+  else k_fill<double><<<nblk(n, RB), RB, 0, st>>>(n, w.x, 0.0);
+  ctx->launches += 2;
+  FG_CUDA_TRY(cudaGetLastError());
   if (prm->precision == FG_FP64) {
     if (d_x0) {
-      FG_CUDA_TRY(cudaMemcpyAsync(w.x, d_x0, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-      k_spmv<double, double, 0><<<w.grid_spmv, RB, 0, st>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, w.x, w.r, nullptr,
-                                                             w.rb, w.S, w.I);
-    } else {
-      k_fill<double><<<nblk(n, RB), RB, 0, st>>>(n, w.x, 0.0);
+      k_sell_spmv<double, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.x, w.r,
+                                                   nullptr, w.rb, w.S, w.I);
+      ctx->launches += 1;
     }
-    ctx->launches += 2;
-    k_init<double><<<w.grid_vec, RB, 0, st>>>(n, b, d_x0 ? 1 : 0, w.r, w.p, sys->d_idiag, precond, prm->criterion,
-                                              prm->rtol, prm->atol, prm->max_iters, w.rb, w.S, w.I);
+    k_init64<<<w.grid, RB, 0, st>>>(n, w.b, d_x0 ? 1 : 0, w.r, w.p, sys->d_idiag, precond, prm->criterion, prm->rtol,
+                                    prm->atol, prm->max_iters, w.rb, w.S, w.I);
+    ctx->launches += 1;
     FG_CUDA_TRY(cudaGetLastError());
-    status = run_cg_loop<double, double>(sys, w, sys->d_val, w.x, w.r, w.p, w.Ap, sys->d_idiag, precond, prm->criterion,
-                                         prm->rtol, prm->atol, check_every, h_I, h_S);
+    const bool need_pp = prm->criterion == FG_DELTA_RHS || prm->criterion == FG_DELTA_DELTA;
+    status = run_chunks(ctx, w, chunk,
+                        [&]() { iter64(sys, w, precond, need_pp, prm->criterion, prm->rtol, prm->atol, st); }, h_I, h_S);
     out.iterations = h_I[I_ITER];
-    out.outer_iterations = 0;
     out.converged = h_I[I_CONV];
     out.error_estimate = h_S[S_ERR];
     out.tolerance = h_S[S_TOL];
-    FG_CUDA_TRY(cudaMemcpyAsync(d_x, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   } else {
-    // FP64 iterative refinement around FP32 PCG (res_res on the true FP64 residual)
-    const double inner_rtol = prm->inner_rtol > 0 ? prm->inner_rtol : 1e-4;
-    const int inner_max = prm->inner_max_iters > 0 ? prm->inner_max_iters : prm->max_iters;
-    if (d_x0) FG_CUDA_TRY(cudaMemcpyAsync(w.x, d_x0, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    else k_fill<double><<<nblk(n, RB), RB, 0, st>>>(n, w.x, 0.0);
-    double tol = -1.0;
-    int total_inner = 0, outer = 0;
-    for (;;) {
-      k_spmv<double, double, 2><<<w.grid_spmv, RB, 0, st>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, w.x, w.r, b, w.rb,
-                                                             w.S, w.I);
+    const double delta = prm->inner_rtol > 0 ? prm->inner_rtol : 0.1;
+    // true residual of the initial guess and the tolerance
+    k_sell_spmv<double, 2><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.x, w.r, w.b,
+                                                 w.rb, w.S, w.I);
+    ctx->launches += 1;
+    FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+    FG_CUDA_TRY(cudaStreamSynchronize(st));
+    double rn = h_S[S_ERR];
+    double tol;
+    if (prm->criterion == FG_RES_RHS) {
+      k_init64<<<w.grid, RB, 0, st>>>(n, w.b, 0, w.t, w.Ap, sys->d_idiag, 0, FG_RES_RHS, prm->rtol, prm->atol, 1, w.rb,
+                                      w.S, w.I);
       ctx->launches += 1;
-      FG_CUDA_TRY(cudaGetLastError());
-      if (tol < 0 && prm->criterion == FG_RES_RHS) {
-        ctx->launches += 1;
-        k_nrm2<<<w.grid_vec, RB, 0, st>>>(n, b, w.rb, w.S);
-        FG_CUDA_TRY(cudaGetLastError());
-      }
       FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
       FG_CUDA_TRY(cudaStreamSynchronize(st));
-      const double rn = h_S[S_ERR];
-      if (!std::isfinite(rn)) { status = FG_ERR_NUMERIC; set_error("non-finite residual"); break; }
-      if (tol < 0) tol = prm->rtol * (prm->criterion == FG_RES_RHS ? h_S[S_BNRM] : rn) + prm->atol;
-      out.error_estimate = rn;
-      out.tolerance = tol;
-      if (rn <= tol) { out.converged = 1; break; }
-      if (total_inner >= prm->max_iters) break;
-      ++outer;
-      // inner FP32 PCG on A d = r/|r| to a relative reduction inner_rtol
-      ctx->launches += 4;  // scale, init, fill, correction
-      k_scale<<<nblk(n, RB), RB, 0, st>>>(n, w.r, 1.0 / rn, w.Ap);
-      k_init<float><<<w.grid_vec, RB, 0, st>>>(n, w.Ap, 0, w.r32, w.p32, sys->d_idiag32, precond, FG_RES_RES,
-                                               inner_rtol, 0.0,
-                                               std::max(1, std::min(inner_max, prm->max_iters - total_inner)), w.rb,
-                                               w.S, w.I);
-      k_fill<float><<<nblk(n, RB), RB, 0, st>>>(n, w.x32, 0.0f);
-      FG_CUDA_TRY(cudaGetLastError());
-      status = run_cg_loop<float, float>(sys, w, sys->d_val32, w.x32, w.r32, w.p32, w.Ap32, sys->d_idiag32, precond,
-                                         FG_RES_RES, inner_rtol, 0.0, check_every, h_I, h_S);
-      if (status != FG_OK) break;
-      total_inner += h_I[I_ITER];
-      k_axpy_f2d<<<nblk(n, RB), RB, 0, st>>>(n, rn, w.x32, w.x);
-      FG_CUDA_TRY(cudaGetLastError());
+      tol = prm->rtol * h_S[S_BNRM] + prm->atol;
+      k_sell_spmv<double, 2><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.x, w.r,
+                                                   w.b, w.rb, w.S, w.I);
+      ctx->launches += 1;
+    } else {
+      tol = prm->rtol * rn + prm->atol;
     }
-    out.iterations = total_inner;
+    int outer = 0;
+    if (!std::isfinite(rn)) {
+      status = FG_ERR_NUMERIC;
+      set_error("non-finite initial residual");
+    } else if (rn <= tol) {
+      out.converged = 1;
+    } else {
+      // start: r32 = r/|r|, p = z, counters
+      k_set_scalar<<<1, 1, 0, st>>>(w.S, S_TOL, tol);
+      k_set_scalar<<<1, 1, 0, st>>>(w.S, S_DELTA, delta);
+      k_set_scalar<<<1, 1, 0, st>>>(w.S, S_SIGMA, rn);
+      k_fill<float><<<nblk(n, RB), RB, 0, st>>>(n, w.x32, 0.0f);
+      k_fill<float><<<nblk(n, RB), RB, 0, st>>>(n, w.p32, 0.0f);
+      k_fill<int><<<1, 32, 0, st>>>(I_COUNT, w.I, 0);
+      ctx->launches += 6;
+      int hI0[I_COUNT] = {0};
+      hI0[I_MAXIT] = prm->max_iters;
+      FG_CUDA_TRY(cudaMemcpyAsync(w.I, hI0, sizeof(hI0), cudaMemcpyHostToDevice, st));
+      if (precond) k_refresh<true><<<w.grid, RB, 0, st>>>(n, w.r, w.r32, sys->d_idiag32, 1, w.rb, w.S, w.I);
+      else k_refresh<false><<<w.grid, RB, 0, st>>>(n, w.r, w.r32, sys->d_idiag32, 1, w.rb, w.S, w.I);
+      if (precond) k_pupdate<float, true><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
+      else k_pupdate<float, false><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
+      ctx->launches += 2;
+      FG_CUDA_TRY(cudaGetLastError());
+      // graph of `chunk` FP32 iterations, replayed; reliable updates on the host's cue
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < chunk; ++k) iter32(sys, w, precond, st);
+      cudaError_t e = cudaStreamEndCapture(st, &graph);
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+      if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        set_error("graph: %s", cudaGetErrorString(e));
+        return FG_ERR_CUDA;
+      }
+      for (;;) {
+        e = cudaGraphLaunch(exec, st);
+        ctx->launches += 3 * chunk;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h_I, w.I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { set_error("mixed loop: %s", cudaGetErrorString(e)); status = FG_ERR_CUDA; break; }
+        if (!h_I[I_DONE]) continue;
+        // reliable update: fold the FP32 correction into x64 and recompute the true residual
+        FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+        FG_CUDA_TRY(cudaStreamSynchronize(st));
+        const double sigma = h_S[S_SIGMA];
+        k_fold<<<w.grid, RB, 0, st>>>(n, sigma, w.x32, w.x);
+        k_sell_spmv<double, 2><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.x, w.r,
+                                                     w.b, w.rb, w.S, w.I);
+        ctx->launches += 2;
+        ++outer;
+        FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+        FG_CUDA_TRY(cudaStreamSynchronize(st));
+        rn = h_S[S_ERR];
+        if (!std::isfinite(rn)) { status = FG_ERR_NUMERIC; set_error("non-finite residual"); break; }
+        if (rn <= tol) { out.converged = 1; break; }
+        if (h_I[I_ITER] >= prm->max_iters) break;
+        if (precond) k_refresh<true><<<w.grid, RB, 0, st>>>(n, w.r, w.r32, sys->d_idiag32, 0, w.rb, w.S, w.I);
+        else k_refresh<false><<<w.grid, RB, 0, st>>>(n, w.r, w.r32, sys->d_idiag32, 0, w.rb, w.S, w.I);
+        if (precond) k_pupdate<float, true><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
+        else k_pupdate<float, false><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
+        ctx->launches += 2;
+        FG_CUDA_TRY(cudaGetLastError());
+      }
+      cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+      FG_CUDA_TRY(cudaMemcpyAsync(h_I, w.I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, st));
+      FG_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    out.iterations = h_I[I_ITER];
     out.outer_iterations = outer;
-    FG_CUDA_TRY(cudaMemcpyAsync(d_x, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    out.error_estimate = rn;
+    out.tolerance = tol;
   }
+  // solution back to row order
+  k_from_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, w.x, d_x);
+  ctx->launches += 1;
+  FG_CUDA_TRY(cudaGetLastError());
   cudaEventRecord(e1, st);
   cudaEventSynchronize(e1);
   float ms = 0.f;

@@ -239,6 +239,12 @@ class FEAffineOperator:
         L.check(L.lib().fg_system_spmv_device(self.h, precision, _ptr(x), _ptr(y)), "fg_system_spmv_device")
         return y
 
+    def apply_solver_layout_device(self, x_slot, y_slot, precision=L.FG_FP64, reps=1):
+        """reps launches of the solver's SELL SpMV on slot-order vectors, not synchronised."""
+        L.check(L.lib().fg_system_spmv_solver_layout_device(self.h, precision, _ptr(x_slot), _ptr(y_slot), reps),
+                "fg_system_spmv_solver_layout_device")
+        return y_slot
+
     def close(self):
         if getattr(self, "h", None):
             L.lib().fg_system_destroy(self.h)

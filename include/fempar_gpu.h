@@ -86,8 +86,10 @@ typedef struct {
   double rtol;          /* default 1e-6 (iterative_solver_parameters.f90:168-178)    */
   double atol;          /* default 0                                                  */
   int max_iters;        /* default 1000                                               */
-  double inner_rtol;    /* FG_MIXED: relative reduction per inner FP32 solve (0 = auto) */
-  int inner_max_iters;  /* FG_MIXED: cap per inner solve (0 = auto)                    */
+  double inner_rtol;    /* FG_MIXED: reliable-update threshold delta: the FP32 recursive residual
+                           is replaced by the FP64 true residual each time it has dropped by
+                           this factor (0 = 0.1)                                          */
+  int inner_max_iters;  /* reserved (0)                                                   */
   int check_every;      /* iterations between host-side convergence polls (0 = auto)  */
 } fg_solver_params;
 
@@ -179,6 +181,12 @@ fg_status fg_system_export_dirichlet_values(fg_system* sys, double* g);
 /* y = A x on the device (precision FG_FP64 or FG_MIXED for the FP32 copy), device pointers.
  * Replaces sparse_matrix_t%apply (sparse_matrix.f90:1264-1276, csr_sparse_matrix.f90:626-672). */
 fg_status fg_system_spmv_device(fg_system* sys, int precision, const void* x, void* y);
+/* reps launches of the solver's own SpMV kernel on vectors already in the solver's row order
+ * (SELL-C-sigma slot order, num_free entries, FP64 or FP32 per precision), queued on the
+ * context's stream without synchronising; for timing the kernel alone.  Same operator as
+ * sparse_matrix_t%apply in a permuted basis. */
+fg_status fg_system_spmv_solver_layout_device(fg_system* sys, int precision, const void* x_slot, void* y_slot,
+                                              int reps);
 
 /* PCG solve of A x = b.  b == NULL uses the assembled right-hand side; x0 == NULL is the zero
  * initial guess (base_iterative_linear_solver.f90:281-282).  Host pointers.
