@@ -55,6 +55,13 @@ def workload(n, seed=SEED):
 
 
 def spmv_bytes(n, nnz, fp32):
+    """Algorithmic HBM bytes of one SpMV: every nonzero value read once, x read once, y written
+    once (no index bytes: the lattice-implicit layout stores none)."""
+    return (4 * nnz + 8 * n) if fp32 else (8 * nnz + 16 * n)
+
+
+def csr_bytes(n, nnz, fp32):
+    """The same for a full CSR matrix with int32 columns (the explicit-index reference figure)."""
     return (8 * nnz + 4 * (n + 1) + 8 * n) if fp32 else (12 * nnz + 4 * (n + 1) + 16 * n)
 
 
@@ -274,11 +281,13 @@ def main():
 
     # ---- dominant kernel: SpMV, timed on the library's stream ----
     def spmv_ms(precision, reps=20):
-        # the solver's SELL SpMV alone, back to back on the library's stream (matrix >> L2)
+        # the solver's SpMV alone, back to back on the library's stream (matrix >> L2);
+        # vectors in the solver layout (solver_vec_len entries)
+        nvec = space.info.solver_vec_len
         if precision == fg.FG_MIXED:
-            xv = torch.rand(nfree, dtype=torch.float32, device=f"cuda:{local}")
+            xv = torch.rand(nvec, dtype=torch.float32, device=f"cuda:{local}")
         else:
-            xv = torch.rand(nfree, dtype=torch.float64, device=f"cuda:{local}")
+            xv = torch.rand(nvec, dtype=torch.float64, device=f"cuda:{local}")
         yv = torch.empty_like(xv)
         sync_all()
         op.apply_solver_layout_device(xv, yv, precision, reps=2)
@@ -308,6 +317,11 @@ def main():
     b32, b64 = spmv_bytes(nfree, nnz, True), spmv_bytes(nfree, nnz, False)
     ach32 = b32 / (ms32 * 1e-3) / 1e9
     ach64 = b64 / (ms64 * 1e-3) / 1e9
+    nent, nvec = space.info.solver_entries, space.info.solver_vec_len
+    layout = "lattice-implicit SELL-32x4 (no column indices)" if space.info.solver_layout == 0 else "SELL-32x4-256"
+    kname = "k_stencil_spmv" if space.info.solver_layout == 0 else "k_sell_spmv"
+    fmt32 = 4 * nent + 8 * nvec + (0 if space.info.solver_layout == 0 else 4 * nent)
+    fmt64 = 8 * nent + 16 * nvec + (0 if space.info.solver_layout == 0 else 4 * nent)
 
     # ---- max over ranks ----
     def maxr(v):
@@ -352,12 +366,18 @@ def main():
         "mixed_vs_fp64": value / v64,
         "e2e": {"value": ve2e, "unit": "DOF/s", "h2d_bytes_per_step": int(coef.nbytes),
                 "d2h_bytes_per_step": int(nfree * 8), "ms_per_step": ms_e2e},
-        "roofline": {"bound": "hbm", "kernel": "k_sell_spmv<float> (FP32 SELL-32-256 SpMV)",
+        "roofline": {"bound": "hbm", "kernel": f"{kname}<float,0> (FP32 SpMV, {layout})",
                      "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
                      "peak_source": "of measured" if pk else "of fallback", "traffic": None,
-                     "bytes_per_launch": b32, "ms_per_launch": ms32},
-        "roofline_fp64": {"kernel": "k_sell_spmv<double>", "achieved": ach64, "frac": ach64 / hbm,
-                          "bytes_per_launch": b64, "ms_per_launch": ms64},
+                     "bytes_per_launch": b32, "ms_per_launch": ms32,
+                     "bytes_def": "4*nnz + 8*n (values once, x once, y once)",
+                     "format_bytes_per_launch": fmt32, "format_frac": fmt32 / (ms32 * 1e-3) / 1e9 / hbm,
+                     "csr_bytes_per_launch": csr_bytes(nfree, nnz, True),
+                     "csr_equivalent_gbs": csr_bytes(nfree, nnz, True) / (ms32 * 1e-3) / 1e9},
+        "roofline_fp64": {"kernel": f"{kname}<double,0>", "bound": "fp64 pipe (1 DFMA per stored entry)",
+                          "achieved_gbs": ach64, "frac_hbm": ach64 / hbm, "bytes_per_launch": b64,
+                          "ms_per_launch": ms64, "dfma_per_s": nent / (ms64 * 1e-3),
+                          "format_bytes_per_launch": fmt64},
         "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches,
     }
     print(json.dumps(line), flush=True)

@@ -83,7 +83,8 @@ class SpaceInfo(C.Structure):
         ("num_dims", C.c_int), ("order", C.c_int), ("ncomp", C.c_int),
         ("dofs_per_cell", C.c_int), ("qp_per_cell", C.c_int),
         ("num_cells", C.c_int64), ("num_free", C.c_int64), ("num_dirichlet", C.c_int64),
-        ("nnz_full", C.c_int64), ("nnz_upper", C.c_int64),
+        ("nnz_full", C.c_int64), ("nnz_upper", C.c_int64), ("solver_vec_len", C.c_int64),
+        ("solver_entries", C.c_int64), ("solver_layout", C.c_int32),
     ]
 
 

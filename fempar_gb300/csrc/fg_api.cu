@@ -1,5 +1,6 @@
 // fg_api.cu -- the extern "C" entry points of libfempar_gpu.so (include/fempar_gpu.h).
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 
 #include "fg_internal.h"
@@ -224,6 +225,12 @@ static void space_free(fg_space* sp) {
   dev_free(ctx, sp->d_iperm);
   dev_free(ctx, sp->d_sptr);
   dev_free(ctx, sp->d_scol);
+  if (sp->layout == FG_LAYOUT_STENCIL) dev_free(ctx, sp->d_row2vec);
+  dev_free(ctx, sp->d_st_cls);
+  dev_free(ctx, sp->d_st_off);
+  dev_free(ctx, sp->d_st_scls);
+  dev_free(ctx, sp->d_st_row);
+  dev_free(ctx, sp->d_row2st);
   delete sp;
 }
 
@@ -260,7 +267,20 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
   fg_status s = upload_tables(ctx, sp->tab, sp->dtab);
   if (s == FG_OK) s = space_number_dofs(sp);
   if (s == FG_OK) s = space_build_pattern(sp);
-  if (s == FG_OK) s = space_build_sell(sp);
+  {
+    // solver layout: lattice-implicit SELL unless FG_SOLVER_LAYOUT=sell asks for explicit columns
+    const char* lay = getenv("FG_SOLVER_LAYOUT");
+    sp->layout = (lay && std::strcmp(lay, "sell") == 0) ? FG_LAYOUT_SELL : FG_LAYOUT_STENCIL;
+  }
+  if (s == FG_OK) {
+    if (sp->layout == FG_LAYOUT_SELL) {
+      s = space_build_sell(sp);
+      sp->nvec = sp->nfree;
+      sp->d_row2vec = sp->d_iperm;
+    } else {
+      s = space_build_stencil(sp);
+    }
+  }
   if (s == FG_OK) {
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) { set_error("space: %s", cudaGetErrorString(e)); s = FG_ERR_CUDA; }
@@ -292,6 +312,9 @@ fg_status fg_space_get_info(fg_space* sp, fg_space_info* info) {
   info->num_dirichlet = sp->ndir;
   info->nnz_full = sp->nnz;
   info->nnz_upper = sp->nnz_upper;
+  info->solver_vec_len = sp->nvec;
+  info->solver_entries = sp->layout == FG_LAYOUT_SELL ? sp->sell_nnz : sp->st_nvals;
+  info->solver_layout = sp->layout;
   return FG_OK;
 }
 
@@ -321,7 +344,7 @@ fg_status fg_space_get_dirichlet_coords(fg_space* sp, double* xyz) {
 static void system_free(fg_system* sys) {
   fg_ctx* ctx = sys->space->mesh->ctx;
   void* ptrs[] = {sys->d_val, sys->d_val32, sys->d_rhs, sys->d_gvals, sys->d_elmat, sys->d_elvec, sys->d_coef,
-                  sys->d_qpsrc, sys->d_sval, sys->d_sval32, sys->d_idiag, sys->d_idiag32, sys->d_work, sys->d_work32, sys->d_red, sys->d_ticket};
+                  sys->d_qpsrc, sys->d_sval, sys->d_sval32, sys->d_tval, sys->d_tval32, sys->d_idiag, sys->d_idiag32, sys->d_work, sys->d_work32, sys->d_red, sys->d_ticket};
   for (void* p : ptrs) dev_free(ctx, p);
   delete sys;
 }
@@ -354,7 +377,8 @@ static fg_status numeric_phase(fg_system* sys, const fg_integrand* g) {
     FG_TRY(system_interpolate_dirichlet(sys, g->boundary_fn, g->fn_param));
   }
   FG_TRY(system_assemble(sys));
-  FG_TRY(system_fill_sell(sys));
+  if (sp->layout == FG_LAYOUT_SELL) FG_TRY(system_fill_sell(sys));
+  else FG_TRY(system_fill_stencil(sys));
   FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return FG_OK;
 }
@@ -370,8 +394,13 @@ fg_status fg_assemble(fg_space* sp, const fg_integrand* g, fg_system** out) {
   fg_status s = FG_OK;
   auto A = [&](void** p, size_t b) { if (s == FG_OK) s = dev_alloc(ctx, p, b); };
   A((void**)&sys->d_val, sizeof(double) * (sp->nnz > 0 ? sp->nnz : 1));
-  A((void**)&sys->d_sval, sizeof(double) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1));
-  A((void**)&sys->d_sval32, sizeof(float) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1));
+  if (sp->layout == FG_LAYOUT_SELL) {
+    A((void**)&sys->d_sval, sizeof(double) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1));
+    A((void**)&sys->d_sval32, sizeof(float) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1));
+  } else {
+    A((void**)&sys->d_tval, sizeof(double) * (sp->st_nvals > 0 ? sp->st_nvals : 1));
+    A((void**)&sys->d_tval32, sizeof(float) * (sp->st_nvals > 0 ? sp->st_nvals : 1));
+  }
   A((void**)&sys->d_rhs, sizeof(double) * (sp->nfree > 0 ? sp->nfree : 1));
   A((void**)&sys->d_gvals, sizeof(double) * (sp->ndir > 0 ? sp->ndir : 1));
   A((void**)&sys->d_elmat, sizeof(double) * ncells * nd * nd);

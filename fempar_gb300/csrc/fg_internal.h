@@ -51,6 +51,18 @@ struct RefTables {
   void build(int order, int ncomp);
 };
 
+// One row class of the lattice-implicit SELL layout (fg_stencil.cu).
+struct StencilClass {
+  int64_t vbase;   // first value of the class
+  int64_t sbase;   // first slice of the class
+  int64_t nrows;   // rows of the class
+  int lo[3], w[3]; // box start (relative to the row's node) and width per direction
+  int B, Bp;       // box entries (all components) and the 4-padded count
+  int offbase;     // first entry of the class in the offset table
+};
+
+enum { FG_LAYOUT_STENCIL = 0, FG_LAYOUT_SELL = 1 };
+
 // Device copy of the tables in one buffer.
 struct DevTables {
   double* base = nullptr;
@@ -108,6 +120,20 @@ struct fg_space {
   int32_t* d_iperm = nullptr;     // row -> slot
   int64_t* d_sptr = nullptr;      // nslices+1 entry offsets
   int32_t* d_scol = nullptr;      // sell_nnz column slots
+  // solver layout: FG_LAYOUT_STENCIL (lattice-implicit SELL, default) or FG_LAYOUT_SELL
+  int layout = 0;
+  int64_t nvec = 0;               // solver vector length
+  int32_t* d_row2vec = nullptr;   // free row -> solver vector index
+  // lattice-implicit SELL
+  int halo = 0, Pn[3] = {0, 0, 0};
+  int st_ncls = 0;
+  int64_t st_nslices = 0, st_nvals = 0;
+  fg::StencilClass* d_st_cls = nullptr;
+  int32_t* d_st_off = nullptr;    // box offsets per class
+  uint8_t* d_st_scls = nullptr;   // class of each slice
+  int32_t* d_st_row = nullptr;    // 32*st_nslices: solver vector index of each row slot
+  int32_t* d_row2st = nullptr;    // free row -> row slot
+  std::vector<fg::StencilClass> h_st_cls;
 };
 
 struct fg_system {
@@ -122,6 +148,8 @@ struct fg_system {
   double* d_qpsrc = nullptr;      // optional per-qp source
   double* d_sval = nullptr;       // sell_nnz FP64 values (SELL layout)
   float* d_sval32 = nullptr;      // sell_nnz FP32 values (SELL layout)
+  double* d_tval = nullptr;       // st_nvals FP64 values (lattice-implicit SELL layout)
+  float* d_tval32 = nullptr;      // st_nvals FP32 values (lattice-implicit SELL layout)
   double* d_idiag = nullptr;      // nfree inverse diagonal (FP64, slot order)
   float* d_idiag32 = nullptr;     // nfree inverse diagonal (FP32, slot order)
   // solver work vectors (allocated on first solve)
@@ -154,6 +182,10 @@ fg_status system_assemble(fg_system* sys);
 // fg_sell.cu
 fg_status space_build_sell(fg_space* sp);
 fg_status system_fill_sell(fg_system* sys);
+
+// fg_stencil.cu
+fg_status space_build_stencil(fg_space* sp);
+fg_status system_fill_stencil(fg_system* sys);
 
 // fg_solver.cu
 fg_status system_prepare_diag(fg_system* sys);

@@ -1,10 +1,12 @@
 // fg_sell.cu -- SELL-C-sigma copy of the free-dof matrix for the solver.
 //
 // Layout: rows are grouped in windows of SIGMA = 256 rows; inside a window they are
-// stably sorted by decreasing length, then cut into slices of C = 32 rows.  Slice s holds
-// width w_s = its longest row; entry j of the row in lane l sits at sptr[s] + 32 j + l,
-// so a warp that owns a slice (lane = row) reads its values and column indices with
-// fully coalesced 128/256-byte loads and needs no cross-lane reduction.  Padding entries
+// stably sorted by decreasing length, then cut into slices of C = 32 rows.  Slice s has
+// width w_s = its longest row rounded up to a multiple of 4, and entry j of the row in
+// lane l sits at sptr[s] + 128 (j/4) + 4 l + (j%4): each lane's entries come in runs of
+// 4, so a warp that owns a slice (lane = row) reads 4 values per lane with one 128-bit
+// (FP32 values, int32 columns) or 256-bit (FP64 values) load -- 512 B to 1 KB per warp
+// instruction, fully coalesced -- and needs no cross-lane reduction.  Padding entries
 // have value 0 and point at the row itself.
 //
 // The solver runs in the SELL row order ("slot" order): perm[slot] = row, iperm[row] =
@@ -61,7 +63,7 @@ __global__ void k_slice_width(int64_t n, int64_t nslices, const int64_t* rowptr,
       if (len > m) m = len;
     }
   }
-  w[s] = m * SELL_C;  // entries of the slice (scanned into slice pointers)
+  w[s] = ((m + 3) / 4 * 4) * SELL_C;  // entries of the slice (scanned into slice pointers)
 }
 
 // warp per slice: lane = row.  Columns converted to slot numbering.
@@ -82,7 +84,7 @@ __global__ void k_sell_cols(int64_t n, int64_t nslices, const int64_t* rowptr, c
   const int32_t self = (int32_t)(slot < n ? slot : 0);
   for (int j = 0; j < width; ++j) {
     int32_t c = j < len ? iperm[col[rs + j]] : self;
-    scol[base + (int64_t)j * SELL_C + lane] = c;
+    scol[base + (int64_t)(j >> 2) * (4 * SELL_C) + 4 * lane + (j & 3)] = c;
   }
 }
 
@@ -103,7 +105,7 @@ __global__ void k_sell_vals(int64_t n, int64_t nslices, const int64_t* rowptr, c
   }
   for (int j = 0; j < width; ++j) {
     double v = j < len ? val[rs + j] : 0.0;
-    const int64_t o = base + (int64_t)j * SELL_C + lane;
+    const int64_t o = base + (int64_t)(j >> 2) * (4 * SELL_C) + 4 * lane + (j & 3);
     sval[o] = v;
     sval32[o] = (float)v;
   }

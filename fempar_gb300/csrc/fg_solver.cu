@@ -28,6 +28,8 @@
 // per-thread index sets, block partials summed in index order by the last block.
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "fg_internal.h"
 
@@ -100,7 +102,7 @@ __device__ __forceinline__ bool block_reduce_last(double (&v)[NV], const RedBuf&
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
     double s = 0.0;
-    for (int i = threadIdx.x; i < rb.nblocks; i += RB) s += __ldcg(rb.part + k * rb.nblocks + i);
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += RB) s += __ldcg(rb.part + k * rb.nblocks + i);
     v[k] = s;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
@@ -125,6 +127,15 @@ __device__ __forceinline__ bool block_reduce_last(double (&v)[NV], const RedBuf&
 __device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
 
+// 4 consecutive matrix entries of one lane: one 128-bit (FP32) or 256-bit (FP64) streaming load
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+  const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+  asm("ld.global.cs.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3]) : "l"(p));
+}
+
 // ---------------------------------------------------------------------------
 // SELL SpMV, warp per slice, lane per row, slices strided over a fixed grid.
 // MODE 0: y = A x.  MODE 1: y = A x, <y,x> reduced, alpha = r_z/<Ap,p>.
@@ -141,26 +152,22 @@ __global__ void __launch_bounds__(RB)
   Acc<T> dot;
   for (int64_t s = warp; s < nslices; s += nwarps) {
     const int64_t base = sptr[s];
-    const int w = (int)((sptr[s + 1] - base) >> 5);
-    const T* vp = sval + base + lane;
-    const int32_t* cp = scol + base + lane;
+    const int w4 = (int)((sptr[s + 1] - base) >> 7);  // groups of 4 entries per lane
+    const T* vp = sval + base + 4 * lane;
+    const int32_t* cp = scol + base + 4 * lane;
     T acc = 0;
-    int j = 0;
-    for (; j + 4 <= w; j += 4) {
-      const T v0 = __ldcs(vp), v1 = __ldcs(vp + 32), v2 = __ldcs(vp + 64), v3 = __ldcs(vp + 96);
-      const int32_t c0 = __ldcs(cp), c1 = __ldcs(cp + 32), c2 = __ldcs(cp + 64), c3 = __ldcs(cp + 96);
-      const T x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-      acc = fmaT(v0, x0, acc);
-      acc = fmaT(v1, x1, acc);
-      acc = fmaT(v2, x2, acc);
-      acc = fmaT(v3, x3, acc);
+#pragma unroll 2
+    for (int j = 0; j < w4; ++j) {
+      T v[4];
+      ld4(vp, v);
+      const int4 c = __ldcs(reinterpret_cast<const int4*>(cp));
+      const T x0 = __ldg(x + c.x), x1 = __ldg(x + c.y), x2 = __ldg(x + c.z), x3 = __ldg(x + c.w);
+      acc = fmaT(v[0], x0, acc);
+      acc = fmaT(v[1], x1, acc);
+      acc = fmaT(v[2], x2, acc);
+      acc = fmaT(v[3], x3, acc);
       vp += 128;
       cp += 128;
-    }
-    for (; j < w; ++j) {
-      acc = fmaT(__ldcs(vp), __ldg(x + __ldcs(cp)), acc);
-      vp += 32;
-      cp += 32;
     }
     const int64_t slot = s * 32 + lane;
     if (slot < n) {
@@ -367,12 +374,73 @@ __global__ void __launch_bounds__(RB)
   }
 }
 
-// inverse diagonal in slot order (extract_diagonal by binary search, csr_sparse_matrix.f90:4231-4256)
-__global__ void k_inv_diag(int64_t n, const int64_t* rp, const int32_t* ci, const double* av, const int32_t* perm,
+// ---------------------------------------------------------------------------
+// Lattice-implicit SELL SpMV: warp per slice, lane per row, 4 values per lane per load;
+// the column of box position k is the row's node plus the class offset k.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(RB)
+    k_stencil_spmv(int64_t nslices, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
+                   const int32_t* __restrict__ soff, const int32_t* __restrict__ st_row, const T* __restrict__ tval,
+                   int ncomp, const T* __restrict__ x, T* __restrict__ y, const double* __restrict__ b, RedBuf rb,
+                   double* S, const int* I) {
+  if (MODE == 1 && I[I_DONE]) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * RB + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
+  Acc<T> dot;
+  for (int64_t s = warp; s < nslices; s += nwarps) {
+    const int k = scls[s];
+    const int64_t sbase = cls[k].sbase, nrows = cls[k].nrows, vbase = cls[k].vbase;
+    const int Bp = cls[k].Bp, offbase = cls[k].offbase;
+    const int64_t rowid = (s - sbase) * 32 + lane;
+    const int32_t vec = st_row[s * 32 + lane];
+    const int32_t base = ncomp == 1 ? vec : vec - vec % ncomp;
+    const T* vp = tval + vbase + (s - sbase) * 32 * (int64_t)Bp + 4 * lane;
+    const int4* op = reinterpret_cast<const int4*>(soff + offbase);
+    const T* xb = x + base;
+    T acc = 0;
+    const int w4 = Bp >> 2;
+#pragma unroll 2
+    for (int j = 0; j < w4; ++j) {
+      T v[4];
+      ld4(vp, v);
+      const int4 o = __ldg(op + j);
+      const T x0 = __ldg(xb + o.x), x1 = __ldg(xb + o.y), x2 = __ldg(xb + o.z), x3 = __ldg(xb + o.w);
+      acc = fmaT(v[0], x0, acc);
+      acc = fmaT(v[1], x1, acc);
+      acc = fmaT(v[2], x2, acc);
+      acc = fmaT(v[3], x3, acc);
+      vp += 128;
+    }
+    if (rowid < nrows) {
+      if (MODE == 2) {
+        const T rr = (T)(b[vec] - (double)acc);
+        y[vec] = rr;
+        dot.add(rr, rr);
+      } else {
+        y[vec] = acc;
+        if (MODE == 1) dot.add(acc, x[vec]);
+      }
+    }
+  }
+  if (MODE == 0) return;
+  double v[1] = {dot.value()}, tot[1];
+  if (block_reduce_last<1>(v, rb, tot) && threadIdx.x == 0) {
+    if (MODE == 1) {
+      S[S_APP] = tot[0];
+      S[S_ALPHA] = tot[0] != 0.0 ? S[S_RZ] / tot[0] : 0.0;
+    } else {
+      S[S_ERR] = sqrt(tot[0]);
+    }
+  }
+}
+
+// inverse diagonal in the solver layout (extract_diagonal by binary search,
+// csr_sparse_matrix.f90:4231-4256); entries of non-free vector slots stay 0
+__global__ void k_inv_diag(int64_t n, const int64_t* rp, const int32_t* ci, const double* av, const int32_t* row2vec,
                            double* d64, float* d32) {
-  int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (slot >= n) return;
-  const int64_t r = perm[slot];
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
   int64_t lo = rp[r], hi = rp[r + 1];
   while (lo < hi) {
     int64_t m = (lo + hi) >> 1;
@@ -381,50 +449,77 @@ __global__ void k_inv_diag(int64_t n, const int64_t* rp, const int32_t* ci, cons
   }
   const double d = (lo < rp[r + 1] && ci[lo] == r) ? av[lo] : 0.0;
   const double inv = 1.0 / d;
-  d64[slot] = inv;
-  d32[slot] = (float)inv;
+  const int32_t v = row2vec[r];
+  d64[v] = inv;
+  d32[v] = (float)inv;
 }
 
+// row order <-> solver layout
 template <typename TS, typename TD>
-__global__ void k_to_slot(int64_t n, const int32_t* __restrict__ perm, const TS* __restrict__ src, TD* __restrict__ dst) {
-  int64_t s = blockIdx.x * (int64_t)RB + threadIdx.x;
-  if (s < n) dst[s] = (TD)src[perm[s]];
+__global__ void k_rows_to_vec(int64_t n, const int32_t* __restrict__ row2vec, const TS* __restrict__ src,
+                              TD* __restrict__ dst) {
+  int64_t r = blockIdx.x * (int64_t)RB + threadIdx.x;
+  if (r < n) dst[row2vec[r]] = (TD)src[r];
 }
 template <typename TS, typename TD>
-__global__ void k_from_slot(int64_t n, const int32_t* __restrict__ perm, const TS* __restrict__ src,
-                            TD* __restrict__ dst) {
-  int64_t s = blockIdx.x * (int64_t)RB + threadIdx.x;
-  if (s < n) dst[perm[s]] = (TD)src[s];
+__global__ void k_vec_to_rows(int64_t n, const int32_t* __restrict__ row2vec, const TS* __restrict__ src,
+                              TD* __restrict__ dst) {
+  int64_t r = blockIdx.x * (int64_t)RB + threadIdx.x;
+  if (r < n) dst[r] = (TD)src[row2vec[r]];
 }
 template <typename T>
 __global__ void k_fill(int64_t n, T* a, T v) {
   int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x;
   if (i < n) a[i] = v;
 }
-__global__ void k_set_flags(int* I, int done, int flag) {
-  I[I_DONE] = done;
-  I[I_FLAG] = flag;
-}
 __global__ void k_set_scalar(double* S, int slot, double v) { S[slot] = v; }
 
 static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 struct Work {
-  double *x, *r, *p, *Ap, *b, *t;  // FP64, slot order
+  double *x, *r, *p, *Ap, *b, *t;  // FP64, solver layout
   float *x32, *r32, *p32, *Ap32;
+  double *io;                       // FP64 row-order staging (x0 of spmv)
   double* S;
   int* I;
   RedBuf rb;
-  unsigned grid;
+  int sms;
 };
+
+// Grid of a grid-stride kernel: exactly the blocks that are co-resident (one wave), from
+// the occupancy of that kernel.  Every block does the same share of the work, so a
+// second wave would double the kernel's time; the grid is fixed per kernel, which keeps
+// the block-partial reductions deterministic.
+static unsigned grid_for(const void* k, int sms) {
+  static std::mutex mu;
+  static std::map<const void*, unsigned> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(k);
+  if (it != cache.end()) return it->second;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, RB, 0) != cudaSuccess) { cudaGetLastError(); nb = 1; }
+  if (nb < 1) nb = 1;
+  if (nb > 8) nb = 8;
+  const unsigned g = (unsigned)(nb * sms);
+  cache[k] = g;
+  return g;
+}
+
+template <typename... KA, typename... A>
+static inline void launch_k(void (*k)(KA...), const Work& w, cudaStream_t st, A... args) {
+  k<<<grid_for((const void*)k, w.sms), RB, 0, st>>>(args...);
+}
 
 static fg_status ensure_work(fg_system* sys, Work& w) {
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
-  const int64_t n = sp->nfree > 0 ? sp->nfree : 1;
+  const int64_t n = sp->nvec > 0 ? sp->nvec : 1;
   if (!sys->d_work) {
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_work, sizeof(double) * 6 * n));
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_work32, sizeof(float) * 4 * n));
+    // entries of non-free vector slots must read zero for the whole life of the buffers
+    FG_CUDA_TRY(cudaMemsetAsync(sys->d_work, 0, sizeof(double) * 6 * n, ctx->stream));
+    FG_CUDA_TRY(cudaMemsetAsync(sys->d_work32, 0, sizeof(float) * 4 * n, ctx->stream));
     sys->red_blocks = ctx->sm_count * 8;
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_red, sizeof(double) * (4 * sys->red_blocks + S_COUNT) + sizeof(int) * I_COUNT));
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_ticket, sizeof(unsigned) * 4));
@@ -432,33 +527,60 @@ static fg_status ensure_work(fg_system* sys, Work& w) {
   }
   w.x = sys->d_work; w.r = w.x + n; w.p = w.r + n; w.Ap = w.p + n; w.b = w.Ap + n; w.t = w.b + n;
   w.x32 = sys->d_work32; w.r32 = w.x32 + n; w.p32 = w.r32 + n; w.Ap32 = w.p32 + n;
+  w.io = nullptr;
   w.S = sys->d_red + 4 * sys->red_blocks;
   w.I = (int*)(w.S + S_COUNT);
   w.rb.part = sys->d_red;
   w.rb.ticket = sys->d_ticket;
   w.rb.nblocks = sys->red_blocks;
-  w.grid = (unsigned)sys->red_blocks;
+  w.sms = ctx->sm_count;
   return FG_OK;
 }
 
 fg_status system_prepare_diag(fg_system* sys) {
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
-  const int64_t n = sp->nfree;
+  const int64_t n = sp->nfree, nv = sp->nvec > 0 ? sp->nvec : 1;
   if (!sys->d_idiag) {
-    FG_TRY(dev_alloc(ctx, (void**)&sys->d_idiag, sizeof(double) * (n > 0 ? n : 1)));
-    FG_TRY(dev_alloc(ctx, (void**)&sys->d_idiag32, sizeof(float) * (n > 0 ? n : 1)));
+    FG_TRY(dev_alloc(ctx, (void**)&sys->d_idiag, sizeof(double) * nv));
+    FG_TRY(dev_alloc(ctx, (void**)&sys->d_idiag32, sizeof(float) * nv));
+    FG_CUDA_TRY(cudaMemsetAsync(sys->d_idiag, 0, sizeof(double) * nv, ctx->stream));
+    FG_CUDA_TRY(cudaMemsetAsync(sys->d_idiag32, 0, sizeof(float) * nv, ctx->stream));
   }
   if (n > 0) {
     ctx->launches += 1;
-    k_inv_diag<<<nblk(n, 256), 256, 0, ctx->stream>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, sp->d_perm, sys->d_idiag,
-                                                       sys->d_idiag32);
+    k_inv_diag<<<nblk(n, 256), 256, 0, ctx->stream>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, sp->d_row2vec,
+                                                       sys->d_idiag, sys->d_idiag32);
     FG_CUDA_TRY(cudaGetLastError());
   }
   return FG_OK;
 }
 
-// y = A x in row order (device pointers): permute in, SELL SpMV, permute out.
+// SpMV of the active solver layout on solver-layout vectors
+template <typename T, int MODE>
+static void spmv_k(fg_system* sys, const Work& w, const T* x, T* y, const double* b, cudaStream_t st);
+
+#define FG_SPMV_IMPL(T, MODE, VALS, TVALS)                                                                          \
+  template <>                                                                                                       \
+  void spmv_k<T, MODE>(fg_system * sys, const Work& w, const T* x, T* y, const double* b, cudaStream_t st) {       \
+    fg_space* sp = sys->space;                                                                                      \
+    if (sp->layout == FG_LAYOUT_STENCIL)                                                                            \
+      launch_k(k_stencil_spmv<T, MODE>, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls,                       \
+               (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row,       \
+               (const T*)sys->TVALS, sp->ncomp, x, y, b, w.rb, w.S, (const int*)w.I);                               \
+    else                                                                                                            \
+      launch_k(k_sell_spmv<T, MODE>, w, st, sp->nslices, sp->nfree, (const int64_t*)sp->d_sptr,                     \
+               (const int32_t*)sp->d_scol, (const T*)sys->VALS, x, y, b, w.rb, w.S, (const int*)w.I);              \
+    sp->mesh->ctx->launches += 1;                                                                                   \
+  }
+FG_SPMV_IMPL(double, 0, d_sval, d_tval)
+FG_SPMV_IMPL(double, 1, d_sval, d_tval)
+FG_SPMV_IMPL(double, 2, d_sval, d_tval)
+FG_SPMV_IMPL(float, 0, d_sval32, d_tval32)
+FG_SPMV_IMPL(float, 1, d_sval32, d_tval32)
+#undef FG_SPMV_IMPL
+
+// y = A x in row order (device pointers): into the solver layout, SpMV, back.
 fg_status system_spmv(fg_system* sys, int precision, const void* x, void* y, cudaStream_t st) {
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
@@ -467,67 +589,60 @@ fg_status system_spmv(fg_system* sys, int precision, const void* x, void* y, cud
   const int64_t n = sp->nfree;
   if (n == 0) return FG_OK;
   if (precision == FG_MIXED) {
-    k_to_slot<float, float><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, (const float*)x, w.p32);
-    k_sell_spmv<float, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval32, w.p32, w.Ap32,
-                                                nullptr, w.rb, w.S, w.I);
-    k_from_slot<float, float><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, w.Ap32, (float*)y);
+    k_rows_to_vec<float, float><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_row2vec, (const float*)x, w.p32);
+    spmv_k<float, 0>(sys, w, w.p32, w.Ap32, nullptr, st);
+    k_vec_to_rows<float, float><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_row2vec, w.Ap32, (float*)y);
   } else {
-    k_to_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, (const double*)x, w.p);
-    k_sell_spmv<double, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.p, w.Ap,
-                                                 nullptr, w.rb, w.S, w.I);
-    k_from_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, w.Ap, (double*)y);
+    k_rows_to_vec<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_row2vec, (const double*)x, w.p);
+    spmv_k<double, 0>(sys, w, w.p, w.Ap, nullptr, st);
+    k_vec_to_rows<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_row2vec, w.Ap, (double*)y);
   }
-  ctx->launches += 3;
+  ctx->launches += 2;
   FG_CUDA_TRY(cudaGetLastError());
   return FG_OK;
 }
 
-// SpMV of the solver layout alone (slot-order device vectors; timing of the dominant kernel).
+// reps launches of the solver-layout SpMV alone on solver-layout vectors (timing)
 fg_status system_spmv_slot(fg_system* sys, int precision, const void* x, void* y, int reps, cudaStream_t st) {
-  fg_space* sp = sys->space;
   Work w;
   FG_TRY(ensure_work(sys, w));
-  const int64_t n = sp->nfree;
-  for (int k = 0; k < reps && n > 0; ++k) {
-    if (precision == FG_MIXED)
-      k_sell_spmv<float, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval32,
-                                                  (const float*)x, (float*)y, nullptr, w.rb, w.S, w.I);
-    else
-      k_sell_spmv<double, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval,
-                                                   (const double*)x, (double*)y, nullptr, w.rb, w.S, w.I);
+  if (sys->space->nfree == 0) return FG_OK;
+  for (int k = 0; k < reps; ++k) {
+    if (precision == FG_MIXED) spmv_k<float, 0>(sys, w, (const float*)x, (float*)y, nullptr, st);
+    else spmv_k<double, 0>(sys, w, (const double*)x, (double*)y, nullptr, st);
   }
-  sp->mesh->ctx->launches += reps;
   FG_CUDA_TRY(cudaGetLastError());
   return FG_OK;
 }
+
+int64_t system_vec_len(fg_system* sys) { return sys->space->nvec; }
 
 // Launch one FP64 CG iteration (3 kernels).
 static void iter64(fg_system* sys, const Work& w, int precond, bool need_pp, int criterion, double rtol, double atol,
                    cudaStream_t st) {
   fg_space* sp = sys->space;
-  const int64_t n = sp->nfree;
-  k_sell_spmv<double, 1><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.p, w.Ap,
-                                               nullptr, w.rb, w.S, w.I);
-#define FG_UPD(P, Q) k_update64<P, Q><<<w.grid, RB, 0, st>>>(n, w.x, w.r, w.p, w.Ap, sys->d_idiag, criterion, rtol, atol, w.rb, w.S, w.I)
+  const int64_t n = sp->nvec;
+  spmv_k<double, 1>(sys, w, w.p, w.Ap, nullptr, st);
+#define FG_UPD(P, Q) \
+  launch_k(k_update64<P, Q>, w, st, n, w.x, w.r, (const double*)w.p, (const double*)w.Ap, (const double*)sys->d_idiag, criterion, rtol, atol, w.rb, w.S, w.I)
   if (precond) { if (need_pp) FG_UPD(true, true); else FG_UPD(true, false); }
   else { if (need_pp) FG_UPD(false, true); else FG_UPD(false, false); }
 #undef FG_UPD
-  if (precond) k_pupdate<double, true><<<w.grid, RB, 0, st>>>(n, w.p, w.r, sys->d_idiag, w.S, w.I);
-  else k_pupdate<double, false><<<w.grid, RB, 0, st>>>(n, w.p, w.r, sys->d_idiag, w.S, w.I);
+  if (precond) launch_k(k_pupdate<double, true>, w, st, n, w.p, (const double*)w.r, (const double*)sys->d_idiag, (const double*)w.S, (const int*)w.I);
+  else launch_k(k_pupdate<double, false>, w, st, n, w.p, (const double*)w.r, (const double*)sys->d_idiag, (const double*)w.S, (const int*)w.I);
 }
 
 // Launch one FP32 CG iteration of the mixed path (3 kernels).
 static void iter32(fg_system* sys, const Work& w, int precond, cudaStream_t st) {
   fg_space* sp = sys->space;
-  const int64_t n = sp->nfree;
-  k_sell_spmv<float, 1><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval32, w.p32, w.Ap32,
-                                              nullptr, w.rb, w.S, w.I);
+  const int64_t n = sp->nvec;
+  spmv_k<float, 1>(sys, w, w.p32, w.Ap32, nullptr, st);
   if (precond) {
-    k_update32<true><<<w.grid, RB, 0, st>>>(n, w.x32, w.r32, w.p32, w.Ap32, sys->d_idiag32, w.rb, w.S, w.I);
-    k_pupdate<float, true><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
+    launch_k(k_update32<true>, w, st, n, w.x32, w.r32, (const float*)w.p32, (const float*)w.Ap32, (const float*)sys->d_idiag32, w.rb, w.S, w.I);
+    launch_k(k_pupdate<float, true>, w, st, n, w.p32, (const float*)w.r32, (const float*)sys->d_idiag32, (const double*)w.S, (const int*)w.I);
   } else {
-    k_update32<false><<<w.grid, RB, 0, st>>>(n, w.x32, w.r32, w.p32, w.Ap32, sys->d_idiag32, w.rb, w.S, w.I);
-    k_pupdate<float, false><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
+    launch_k(k_update32<false>, w, st, n, w.x32, w.r32, (const float*)w.p32, (const float*)w.Ap32, (const float*)sys->d_idiag32, w.rb, w.S, w.I);
+    launch_k(k_pupdate<float, false>, w, st, n, w.p32, (const float*)w.r32, (const float*)sys->d_idiag32, (const double*)w.S, (const int*)w.I);
   }
 }
 
@@ -550,7 +665,6 @@ static fg_status run_chunks(fg_ctx* ctx, const Work& w, int chunk, F launch_iter
   fg_status out = FG_OK;
   for (;;) {
     e = cudaGraphLaunch(exec, st);
-    ctx->launches += 3 * chunk;
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_I, w.I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -572,7 +686,7 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
   cudaStream_t st = ctx->stream;
-  const int64_t n = sp->nfree;
+  const int64_t n = sp->nfree, nv = sp->nvec;
   fg_solve_info out;
   std::memset(&out, 0, sizeof(out));
   if (n == 0) {
@@ -594,25 +708,22 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
   cudaEventRecord(e0, st);
   const int64_t launches0 = ctx->launches;
   fg_status status = FG_OK;
-  // right-hand side and initial guess into slot order
-  k_to_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, b_row, w.b);
-  if (d_x0) k_to_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, d_x0, w.x);
-  else k_fill<double><<<nblk(n, RB), RB, 0, st>>>(n, w.x, 0.0);
+  // right-hand side and initial guess into the solver layout (other entries are zero)
+  k_rows_to_vec<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_row2vec, b_row, w.b);
+  if (d_x0) k_rows_to_vec<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_row2vec, d_x0, w.x);
+  else k_fill<double><<<nblk(nv, RB), RB, 0, st>>>(nv, w.x, 0.0);
   ctx->launches += 2;
   FG_CUDA_TRY(cudaGetLastError());
   if (prm->precision == FG_FP64) {
-    if (d_x0) {
-      k_sell_spmv<double, 0><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.x, w.r,
-                                                   nullptr, w.rb, w.S, w.I);
-      ctx->launches += 1;
-    }
-    k_init64<<<w.grid, RB, 0, st>>>(n, w.b, d_x0 ? 1 : 0, w.r, w.p, sys->d_idiag, precond, prm->criterion, prm->rtol,
-                                    prm->atol, prm->max_iters, w.rb, w.S, w.I);
+    if (d_x0) spmv_k<double, 0>(sys, w, w.x, w.r, nullptr, st);
+    launch_k(k_init64, w, st, nv, (const double*)w.b, d_x0 ? 1 : 0, w.r, w.p, (const double*)sys->d_idiag, precond,
+             prm->criterion, prm->rtol, prm->atol, prm->max_iters, w.rb, w.S, w.I);
     ctx->launches += 1;
     FG_CUDA_TRY(cudaGetLastError());
     const bool need_pp = prm->criterion == FG_DELTA_RHS || prm->criterion == FG_DELTA_DELTA;
     status = run_chunks(ctx, w, chunk,
                         [&]() { iter64(sys, w, precond, need_pp, prm->criterion, prm->rtol, prm->atol, st); }, h_I, h_S);
+    ctx->launches += (int64_t)3 * chunk * (((int64_t)h_I[I_ITER] + chunk - 1) / chunk + 0);
     out.iterations = h_I[I_ITER];
     out.converged = h_I[I_CONV];
     out.error_estimate = h_S[S_ERR];
@@ -620,49 +731,47 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
   } else {
     const double delta = prm->inner_rtol > 0 ? prm->inner_rtol : 0.1;
     // true residual of the initial guess and the tolerance
-    k_sell_spmv<double, 2><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.x, w.r, w.b,
-                                                 w.rb, w.S, w.I);
-    ctx->launches += 1;
+    spmv_k<double, 2>(sys, w, w.x, w.r, w.b, st);
     FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
     FG_CUDA_TRY(cudaStreamSynchronize(st));
     double rn = h_S[S_ERR];
     double tol;
     if (prm->criterion == FG_RES_RHS) {
-      k_init64<<<w.grid, RB, 0, st>>>(n, w.b, 0, w.t, w.Ap, sys->d_idiag, 0, FG_RES_RHS, prm->rtol, prm->atol, 1, w.rb,
-                                      w.S, w.I);
+      launch_k(k_init64, w, st, nv, (const double*)w.b, 0, w.t, w.Ap, (const double*)sys->d_idiag, 0, (int)FG_RES_RHS,
+               prm->rtol, prm->atol, 1, w.rb, w.S, w.I);
       ctx->launches += 1;
       FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
       FG_CUDA_TRY(cudaStreamSynchronize(st));
       tol = prm->rtol * h_S[S_BNRM] + prm->atol;
-      k_sell_spmv<double, 2><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.x, w.r,
-                                                   w.b, w.rb, w.S, w.I);
-      ctx->launches += 1;
+      spmv_k<double, 2>(sys, w, w.x, w.r, w.b, st);
     } else {
       tol = prm->rtol * rn + prm->atol;
     }
     int outer = 0;
+    int64_t graph_launches = 0;
     if (!std::isfinite(rn)) {
       status = FG_ERR_NUMERIC;
       set_error("non-finite initial residual");
     } else if (rn <= tol) {
       out.converged = 1;
     } else {
-      // start: r32 = r/|r|, p = z, counters
       k_set_scalar<<<1, 1, 0, st>>>(w.S, S_TOL, tol);
       k_set_scalar<<<1, 1, 0, st>>>(w.S, S_DELTA, delta);
       k_set_scalar<<<1, 1, 0, st>>>(w.S, S_SIGMA, rn);
-      k_fill<float><<<nblk(n, RB), RB, 0, st>>>(n, w.x32, 0.0f);
-      k_fill<float><<<nblk(n, RB), RB, 0, st>>>(n, w.p32, 0.0f);
-      k_fill<int><<<1, 32, 0, st>>>(I_COUNT, w.I, 0);
-      ctx->launches += 6;
+      k_fill<float><<<nblk(nv, RB), RB, 0, st>>>(nv, w.x32, 0.0f);
+      k_fill<float><<<nblk(nv, RB), RB, 0, st>>>(nv, w.p32, 0.0f);
+      ctx->launches += 5;
       int hI0[I_COUNT] = {0};
       hI0[I_MAXIT] = prm->max_iters;
       FG_CUDA_TRY(cudaMemcpyAsync(w.I, hI0, sizeof(hI0), cudaMemcpyHostToDevice, st));
-      if (precond) k_refresh<true><<<w.grid, RB, 0, st>>>(n, w.r, w.r32, sys->d_idiag32, 1, w.rb, w.S, w.I);
-      else k_refresh<false><<<w.grid, RB, 0, st>>>(n, w.r, w.r32, sys->d_idiag32, 1, w.rb, w.S, w.I);
-      if (precond) k_pupdate<float, true><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
-      else k_pupdate<float, false><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
-      ctx->launches += 2;
+      auto refresh = [&](int first) {
+        if (precond) launch_k(k_refresh<true>, w, st, nv, (const double*)w.r, w.r32, (const float*)sys->d_idiag32, first, w.rb, w.S, w.I);
+        else launch_k(k_refresh<false>, w, st, nv, (const double*)w.r, w.r32, (const float*)sys->d_idiag32, first, w.rb, w.S, w.I);
+        if (precond) launch_k(k_pupdate<float, true>, w, st, nv, w.p32, (const float*)w.r32, (const float*)sys->d_idiag32, (const double*)w.S, (const int*)w.I);
+        else launch_k(k_pupdate<float, false>, w, st, nv, w.p32, (const float*)w.r32, (const float*)sys->d_idiag32, (const double*)w.S, (const int*)w.I);
+        ctx->launches += 2;
+      };
+      refresh(1);
       FG_CUDA_TRY(cudaGetLastError());
       // graph of `chunk` FP32 iterations, replayed; reliable updates on the host's cue
       cudaGraph_t graph = nullptr;
@@ -678,7 +787,7 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
       }
       for (;;) {
         e = cudaGraphLaunch(exec, st);
-        ctx->launches += 3 * chunk;
+        ++graph_launches;
         if (e == cudaSuccess) e = cudaMemcpyAsync(h_I, w.I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { set_error("mixed loop: %s", cudaGetErrorString(e)); status = FG_ERR_CUDA; break; }
@@ -687,10 +796,9 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
         FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
         FG_CUDA_TRY(cudaStreamSynchronize(st));
         const double sigma = h_S[S_SIGMA];
-        k_fold<<<w.grid, RB, 0, st>>>(n, sigma, w.x32, w.x);
-        k_sell_spmv<double, 2><<<w.grid, RB, 0, st>>>(sp->nslices, n, sp->d_sptr, sp->d_scol, sys->d_sval, w.x, w.r,
-                                                     w.b, w.rb, w.S, w.I);
-        ctx->launches += 2;
+        launch_k(k_fold, w, st, nv, sigma, w.x32, w.x);
+        ctx->launches += 1;
+        spmv_k<double, 2>(sys, w, w.x, w.r, w.b, st);
         ++outer;
         FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
         FG_CUDA_TRY(cudaStreamSynchronize(st));
@@ -698,17 +806,14 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
         if (!std::isfinite(rn)) { status = FG_ERR_NUMERIC; set_error("non-finite residual"); break; }
         if (rn <= tol) { out.converged = 1; break; }
         if (h_I[I_ITER] >= prm->max_iters) break;
-        if (precond) k_refresh<true><<<w.grid, RB, 0, st>>>(n, w.r, w.r32, sys->d_idiag32, 0, w.rb, w.S, w.I);
-        else k_refresh<false><<<w.grid, RB, 0, st>>>(n, w.r, w.r32, sys->d_idiag32, 0, w.rb, w.S, w.I);
-        if (precond) k_pupdate<float, true><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
-        else k_pupdate<float, false><<<w.grid, RB, 0, st>>>(n, w.p32, w.r32, sys->d_idiag32, w.S, w.I);
-        ctx->launches += 2;
+        refresh(0);
         FG_CUDA_TRY(cudaGetLastError());
       }
       cudaGraphExecDestroy(exec);
       cudaGraphDestroy(graph);
       FG_CUDA_TRY(cudaMemcpyAsync(h_I, w.I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, st));
       FG_CUDA_TRY(cudaStreamSynchronize(st));
+      ctx->launches += graph_launches * 3 * chunk;
     }
     out.iterations = h_I[I_ITER];
     out.outer_iterations = outer;
@@ -716,7 +821,7 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
     out.tolerance = tol;
   }
   // solution back to row order
-  k_from_slot<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_perm, w.x, d_x);
+  k_vec_to_rows<double, double><<<nblk(n, RB), RB, 0, st>>>(n, sp->d_row2vec, w.x, d_x);
   ctx->launches += 1;
   FG_CUDA_TRY(cudaGetLastError());
   cudaEventRecord(e1, st);

@@ -236,11 +236,23 @@ class FEAffineOperator:
 
     def apply_device(self, x, y, precision=L.FG_FP64):
         """y = A x with torch CUDA tensors (float64, or float32 for precision=FG_MIXED)."""
+        import torch
+        n = self.space.num_free_dofs
+        want = torch.float32 if precision == L.FG_MIXED else torch.float64
+        for t in (x, y):
+            if not (t.is_cuda and t.is_contiguous() and t.dtype == want and t.numel() == n):
+                raise ValueError(f"x and y must be contiguous CUDA {want} tensors of {n} entries")
         L.check(L.lib().fg_system_spmv_device(self.h, precision, _ptr(x), _ptr(y)), "fg_system_spmv_device")
         return y
 
     def apply_solver_layout_device(self, x_slot, y_slot, precision=L.FG_FP64, reps=1):
-        """reps launches of the solver's SELL SpMV on slot-order vectors, not synchronised."""
+        """reps launches of the solver's SpMV on solver-layout vectors, not synchronised."""
+        import torch
+        n = self.space.info.solver_vec_len
+        want = torch.float32 if precision == L.FG_MIXED else torch.float64
+        for t in (x_slot, y_slot):
+            if not (t.is_cuda and t.is_contiguous() and t.dtype == want and t.numel() == n):
+                raise ValueError(f"solver-layout vectors must be contiguous CUDA {want} tensors of {n} entries")
         L.check(L.lib().fg_system_spmv_solver_layout_device(self.h, precision, _ptr(x_slot), _ptr(y_slot), reps),
                 "fg_system_spmv_solver_layout_device")
         return y_slot

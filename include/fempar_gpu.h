@@ -108,6 +108,9 @@ typedef struct {
   int dofs_per_cell, qp_per_cell;
   int64_t num_cells, num_free, num_dirichlet;
   int64_t nnz_full, nnz_upper;
+  int64_t solver_vec_len;  /* entries of a vector in the solver's own layout (>= num_free) */
+  int64_t solver_entries;  /* matrix entries stored by the solver's layout (>= nnz_full: padding) */
+  int32_t solver_layout;   /* 0 = lattice-implicit SELL (no column indices), 1 = explicit-column SELL */
 } fg_space_info;
 
 const char* fg_status_string(fg_status s);
@@ -181,10 +184,11 @@ fg_status fg_system_export_dirichlet_values(fg_system* sys, double* g);
 /* y = A x on the device (precision FG_FP64 or FG_MIXED for the FP32 copy), device pointers.
  * Replaces sparse_matrix_t%apply (sparse_matrix.f90:1264-1276, csr_sparse_matrix.f90:626-672). */
 fg_status fg_system_spmv_device(fg_system* sys, int precision, const void* x, void* y);
-/* reps launches of the solver's own SpMV kernel on vectors already in the solver's row order
- * (SELL-C-sigma slot order, num_free entries, FP64 or FP32 per precision), queued on the
- * context's stream without synchronising; for timing the kernel alone.  Same operator as
- * sparse_matrix_t%apply in a permuted basis. */
+/* reps launches of the solver's own SpMV kernel on vectors already in the solver's layout
+ * (fg_space_info.solver_vec_len entries each, FP64 or FP32 per precision; entries that are
+ * not free dofs must be finite), queued on the context's stream without synchronising; for
+ * timing the kernel alone.  Same operator as sparse_matrix_t%apply in a permuted basis.
+ * The caller guarantees the buffer lengths: the library cannot check raw pointers. */
 fg_status fg_system_spmv_solver_layout_device(fg_system* sys, int precision, const void* x_slot, void* y_slot,
                                               int reps);
 

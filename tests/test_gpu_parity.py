@@ -233,3 +233,29 @@ def test_errors_are_status_codes(fg, ctx):
     assert not s.info()["converged"] and s.info()["iterations"] == 1
     with pytest.raises(FGError):
         s.solve(raise_on_nonconvergence=True)
+
+
+@pytest.mark.parametrize("layout", ["stencil", "sell"])
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_solver_layouts(fg, ctx, layout, order, monkeypatch):
+    """Both solver layouts (lattice-implicit SELL, explicit-column SELL) give the oracle's
+    operator and CG solution, on a partly Dirichlet boundary (box positions outside the
+    domain and on free boundary nodes)."""
+    import torch
+    monkeypatch.setenv("FG_SOLVER_LAYOUT", layout)
+    n = (5, 3, 4)
+    P, tri, sp, op = build_pair(fg, ctx, n, order, dirichlet=CLAMP, source_fn=O.FN_CONST, fn_param=[1.0])
+    x = np.random.default_rng(order).standard_normal(P.nfree)
+    y_ref = P.spmv(x)
+    xd = torch.tensor(x, device="cuda")
+    yd = torch.empty_like(xd)
+    op.apply_device(xd, yd)
+    assert np.max(np.abs(yd.cpu().numpy() - y_ref)) <= 1e-13 * np.max(np.abs(y_ref))
+    ref = P.cg(precond=1, rtol=1e-13, maxit=20000)
+    for prec in ("fp64", "mixed"):
+        s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
+        s.set_parameters_from_pl({"ILS_RTOL": 1e-12, "ILS_MAX_NUM_ITERATIONS": 20000, "PRECISION": prec})
+        xs = s.solve()
+        assert s.info()["converged"], (layout, prec)
+        err = np.linalg.norm(xs - ref["x"]) / np.linalg.norm(ref["x"])
+        assert err <= 1e-9, (layout, prec, err)
