@@ -32,7 +32,8 @@ EXPORTS = [
     "fg_space_get_dirichlet_coords",
     "fg_assemble", "fg_system_reassemble", "fg_system_destroy",
     "fg_system_export_csr", "fg_system_export_rhs", "fg_system_export_dirichlet_values",
-    "fg_system_spmv_device", "fg_system_spmv_solver_layout_device", "fg_solve", "fg_solve_device",
+    "fg_system_spmv_device", "fg_system_spmv_device_noalloc", "fg_system_spmv_solver_layout_device",
+    "fg_solve", "fg_solve_device",
     "fg_solver_params_default", "fg_integrand_default",
 ]
 
@@ -139,6 +140,7 @@ def lib():
         "fg_system_export_dirichlet_values": (i32, [vp, vp]),
         "fg_system_spmv_device": (i32, [vp, i32, vp, vp]),
         "fg_system_spmv_solver_layout_device": (i32, [vp, i32, vp, vp, i32]),
+        "fg_system_spmv_device_noalloc": (i32, [vp, i32, vp, vp]),
         "fg_solve": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
         "fg_solve_device": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
         "fg_solver_params_default": (None, [C.POINTER(SolverParams)]),

@@ -191,6 +191,7 @@ fg_status system_fill_stencil(fg_system* sys);
 fg_status system_prepare_diag(fg_system* sys);
 fg_status system_spmv(fg_system* sys, int precision, const void* x, void* y, cudaStream_t st);
 fg_status system_spmv_slot(fg_system* sys, int precision, const void* x, void* y, int reps, cudaStream_t st);
+fg_status system_spmv_layout_noalloc(fg_system* sys, int precision, const void* xvec, void* yvec, cudaStream_t st);
 fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double* d_b, const double* d_x0,
                        double* d_x, fg_solve_info* info);
 

@@ -617,6 +617,20 @@ fg_status system_spmv_slot(fg_system* sys, int precision, const void* x, void* y
 
 int64_t system_vec_len(fg_system* sys) { return sys->space->nvec; }
 
+// One SpMV of the active solver layout on caller-provided solver-layout vectors, without
+// touching the system's work buffers (no allocation).  The MODE 0 kernels take no
+// reduction buffers.
+fg_status system_spmv_layout_noalloc(fg_system* sys, int precision, const void* xvec, void* yvec, cudaStream_t st) {
+  Work w;
+  std::memset(&w, 0, sizeof(w));
+  w.sms = sys->space->mesh->ctx->sm_count;
+  if (sys->space->nfree == 0) return FG_OK;
+  if (precision == FG_MIXED) spmv_k<float, 0>(sys, w, (const float*)xvec, (float*)yvec, nullptr, st);
+  else spmv_k<double, 0>(sys, w, (const double*)xvec, (double*)yvec, nullptr, st);
+  FG_CUDA_TRY(cudaGetLastError());
+  return FG_OK;
+}
+
 // Launch one FP64 CG iteration (3 kernels).
 static void iter64(fg_system* sys, const Work& w, int precond, bool need_pp, int criterion, double rtol, double atol,
                    cudaStream_t st) {
