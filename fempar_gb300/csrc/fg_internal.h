@@ -59,6 +59,7 @@ struct StencilClass {
   int lo[3], w[3]; // box start (relative to the row's node) and width per direction
   int B, Bp;       // box entries (all components) and the 4-padded count
   int offbase;     // first entry of the class in the offset table
+  int64_t ownoff;  // start of the class's sub-lattice in the solver vector
 };
 
 enum { FG_LAYOUT_STENCIL = 0, FG_LAYOUT_SELL = 1 };

@@ -393,8 +393,11 @@ __global__ void __launch_bounds__(RB)
     const int64_t sbase = cls[k].sbase, nrows = cls[k].nrows, vbase = cls[k].vbase;
     const int Bp = cls[k].Bp, offbase = cls[k].offbase;
     const int64_t rowid = (s - sbase) * 32 + lane;
-    const int32_t vec = st_row[s * 32 + lane];
-    const int32_t base = ncomp == 1 ? vec : vec - vec % ncomp;
+    // st = node index in the class sub-lattice * ncomp + component; the row's own entry is
+    // in the class's sub-lattice, its box columns are base + table offsets
+    const int32_t st = st_row[s * 32 + lane];
+    const int32_t base = ncomp == 1 ? st : st - st % ncomp;
+    const int64_t vec = st + cls[k].ownoff;
     const T* vp = tval + vbase + (s - sbase) * 32 * (int64_t)Bp + 4 * lane;
     const int4* op = reinterpret_cast<const int4*>(soff + offbase);
     const T* xb = x + base;

@@ -47,12 +47,15 @@ __global__ void k_stencil_rows(int64_t nfree, int ncomp, int p, const int Ln[3],
   const int64_t L = s / ncomp;
   const int c = (int)(s % ncomp);
   const int I = (int)(L % Ln[0]), J = (int)((L / Ln[0]) % Ln[1]), K = (int)(L / ((int64_t)Ln[0] * Ln[1]));
-  const int64_t vec = (((int64_t)(I + halo) + (int64_t)Pn[0] * ((J + halo) + (int64_t)Pn[1] * (K + halo))) * ncomp) + c;
+  // node's index inside its class sub-lattice (padded coordinates divided by p)
+  const int S0 = Pn[0] / p, S1 = Pn[1] / p;
+  const int64_t sub = (int64_t)((I + halo) / p) + (int64_t)S0 * (((J + halo) / p) + (int64_t)S1 * ((K + halo) / p));
+  const int64_t st = sub * ncomp + c;
   const int64_t slot = (int64_t)cls[k].sbase * 32 + (i - cls_start[k]);
   const int32_t r = latdof[s] - 1;
-  st_row[slot] = (int32_t)vec;
+  st_row[slot] = (int32_t)st;
   row2st[r] = (int32_t)slot;
-  row2vec[r] = (int32_t)vec;
+  row2vec[r] = (int32_t)(st + cls[k].ownoff);
 }
 
 // padding lanes of a class's last slice: point at the slice's first row (values are 0)
@@ -99,9 +102,16 @@ fg_status space_build_stencil(fg_space* sp) {
   fg_ctx* ctx = sp->mesh->ctx;
   const int p = sp->order, ncomp = sp->ncomp;
   const int ncls = p * p * p;
+  // Solver vectors: the node lattice padded by p nodes per side (so every box position is
+  // an address), rounded up to a multiple of p per direction and split into the p^3 class
+  // sub-lattices (residues of the padded coordinates mod p), one after the other.  Rows of
+  // a class are consecutive in their sub-lattice, so the 32 lanes of a slice gather 32
+  // consecutive entries for every box position.
   sp->halo = p;
-  for (int d = 0; d < 3; ++d) sp->Pn[d] = sp->Ln[d] + 2 * p;
-  sp->nvec = (int64_t)sp->Pn[0] * sp->Pn[1] * sp->Pn[2] * ncomp;
+  for (int d = 0; d < 3; ++d) sp->Pn[d] = (sp->Ln[d] + 2 * p + p - 1) / p * p;
+  const int64_t S0 = sp->Pn[0] / p, S1 = sp->Pn[1] / p, S2 = sp->Pn[2] / p;
+  const int64_t ssize = S0 * S1 * S2;
+  sp->nvec = (int64_t)ncls * ssize * ncomp;
   if (sp->nvec >= (int64_t)0x7fffffff) { set_error("padded lattice exceeds int32 indices"); return FG_ERR_UNSUPPORTED; }
   // classes: box and offsets
   std::vector<StencilClass> cls(ncls);
@@ -116,12 +126,21 @@ fg_status space_build_stencil(fg_space* sp) {
     C.B = C.w[0] * C.w[1] * C.w[2] * ncomp;
     C.Bp = (C.B + 3) / 4 * 4;
     C.offbase = (int)offs.size();
+    C.ownoff = (int64_t)k * ssize * ncomp;
     for (int pos = 0; pos < C.Bp; ++pos) {
       if (pos >= C.B) { offs.push_back(0); continue; }
       int c2 = pos % ncomp, q = pos / ncomp;
-      int mx = q % C.w[0], my = (q / C.w[0]) % C.w[1], mz = q / (C.w[0] * C.w[1]);
-      int64_t o = ((int64_t)(C.lo[0] + mx) + (int64_t)sp->Pn[0] * ((C.lo[1] + my) + (int64_t)sp->Pn[1] * (C.lo[2] + mz))) *
-                      ncomp + c2;
+      int m[3] = {q % C.w[0], (q / C.w[0]) % C.w[1], q / (C.w[0] * C.w[1])};
+      // column node = row node + (lo + m); split into its sub-lattice and the index shift
+      int res[3], shift[3];
+      for (int d = 0; d < 3; ++d) {
+        int t = rr[d] + C.lo[d] + m[d];  // residue of the row is rr[d]
+        int fl = t >= 0 ? t / p : -((-t + p - 1) / p);
+        shift[d] = fl;
+        res[d] = t - fl * p;
+      }
+      const int64_t kk = res[0] + p * (res[1] + p * res[2]);
+      const int64_t o = (kk * ssize + shift[0] + S0 * (shift[1] + S1 * shift[2])) * ncomp + c2;
       offs.push_back((int32_t)o);
     }
   }
