@@ -377,6 +377,7 @@ __global__ void __launch_bounds__(RB)
 // ---------------------------------------------------------------------------
 // Lattice-implicit SELL SpMV: warp per slice, lane per row, 4 values per lane per load;
 // the column of box position k is the row's node plus the class offset k.
+static constexpr int kPrefetch = 8;  // value groups (of 4 entries per lane) prefetched ahead
 template <typename T, int MODE>
 __global__ void __launch_bounds__(RB)
     k_stencil_spmv(int64_t nslices, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
@@ -405,6 +406,10 @@ __global__ void __launch_bounds__(RB)
     const int w4 = Bp >> 2;
 #pragma unroll 2
     for (int j = 0; j < w4; ++j) {
+      // FP32: keep the value stream ahead of the gathers by asking L2 for this lane's values
+      // kPrefetch groups ahead (no registers held; a hint only, kept inside the slice).  The
+      // FP64 variant is bound by the FP64 pipe and runs slower with it.
+      if (sizeof(T) == 4 && j + kPrefetch < w4) asm volatile("prefetch.global.L2 [%0];" ::"l"(vp + kPrefetch * 128));
       T v[4];
       ld4(vp, v);
       const int4 o = __ldg(op + j);
