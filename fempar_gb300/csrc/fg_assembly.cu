@@ -88,10 +88,10 @@ struct PoissonShape {
   static constexpr int NPAIR = ND * (ND + 1) / 2;
   static constexpr int CH = P == 1 ? 2 : (P == 2 ? 12 : 16);  // pairs per lane per pass
   static constexpr int WARPS = P == 1 ? 8 : (P == 2 ? 4 : 1);
-  // shared doubles per warp: xv, invj, fac, xq, fsrc, grads, elmat
-  static constexpr int SM_XV = 24, SM_INVJ = NQ * 9, SM_FAC = NQ, SM_XQ = NQ * 3, SM_F = NQ, SM_G = NQ * NN * 3,
-                       SM_EL = ND * ND;
-  static constexpr int SM_DOUBLES = SM_XV + SM_INVJ + SM_FAC + SM_XQ + SM_F + SM_G + SM_EL;
+  // shared doubles per warp: xv, invj, fac, xq, fsrc, sqrt(fac*k), grads, elmat
+  static constexpr int SM_XV = 24, SM_INVJ = NQ * 9, SM_FAC = NQ, SM_XQ = NQ * 3, SM_F = NQ, SM_SQ = NQ,
+                       SM_G = NQ * NN * 3, SM_EL = ND * ND;
+  static constexpr int SM_DOUBLES = SM_XV + SM_INVJ + SM_FAC + SM_XQ + SM_F + SM_SQ + SM_G + SM_EL;
   static constexpr int SM_INTS = ND;  // cell gids
   // per-warp stride, rounded to 16 bytes so that the next warp's doubles stay aligned
   // and the int tail of one warp never reaches into the next warp's region
@@ -122,7 +122,8 @@ __global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
   double* fac = invj + S::SM_INVJ;
   double* xq = fac + S::SM_FAC;
   double* fsrc = xq + S::SM_XQ;
-  double* sg = fsrc + S::SM_F;
+  double* sq = fsrc + S::SM_F;
+  double* sg = sq + S::SM_SQ;
   double* el = sg + S::SM_G;
   int32_t* gid = (int32_t*)(el + S::SM_EL);
 
@@ -198,15 +199,19 @@ __global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
     else if (src.fn == FG_FN_CONST) f = src.prm[0];
     else f = 0.0;
     fsrc[q] = f;
+    sq[q] = sqrt(fac[q] * kc);  // |det J| w k > 0
   }
-  // physical gradients sg[(q*NN + a)*3 + i] = sum_j invJ(j,i) grad_ref_j
+  __syncwarp();
+  // physical gradients scaled by sqrt(|det J| w k): s_a = sqrt(fk) J^-T grad_ref(phi_a), so an
+  // element entry is sum_q s_a . s_b, 3 FP64 FMAs per Gauss point (FP64 is GB300's scarce pipe)
   for (int idx = lane; idx < NQ * NN; idx += 32) {
     int q = idx / NN, a = idx % NN;
     const double* rg = tb.shg + ((size_t)a * NQ + q) * 3;
     const double* b = invj + q * 9;
+    const double s = sq[q];
     double r0 = rg[0], r1 = rg[1], r2 = rg[2];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) sg[idx * 3 + i] = b[0 + 3 * i] * r0 + b[1 + 3 * i] * r1 + b[2 + 3 * i] * r2;
+    for (int i = 0; i < 3; ++i) sg[idx * 3 + i] = s * (b[0 + 3 * i] * r0 + b[1 + 3 * i] * r1 + b[2 + 3 * i] * r2);
   }
   __syncwarp();
   // element matrix, upper triangle by pairs
@@ -221,14 +226,14 @@ __global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
       else { pa[t] = 0; pb[t] = 0; }
     }
     for (int q = 0; q < NQ; ++q) {
-      const double fk = fac[q] * kc;
       const double* gq = sg + q * NN * 3;
 #pragma unroll
       for (int t = 0; t < S::CH; ++t) {
         const double* ga = gq + pa[t] * 3;
         const double* gb = gq + pb[t] * 3;
-        double dot = gb[0] * ga[0] + gb[1] * ga[1] + gb[2] * ga[2];
-        acc[t] = acc[t] + fk * dot;
+        acc[t] = fma(gb[0], ga[0], acc[t]);
+        acc[t] = fma(gb[1], ga[1], acc[t]);
+        acc[t] = fma(gb[2], ga[2], acc[t]);
       }
     }
 #pragma unroll
