@@ -402,8 +402,245 @@ static fg_status launch_poisson(fg_system* sys) {
   return FG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Linear elasticity (vector Q_P, 3 components), one warp per cell.
+// Reference integrand (Sources/Tests/Par/par_test_pb_bddc_linear_elasticity/modules/
+// sbm_irreducible_heterogeneous_discrete_integration.i90:57-84): per Gauss point and dof
+// pair, elmat(i,j) += dV grad(phi_i) : (lambda tr(eps_j) I + 2 mu eps_j), eps_j =
+// sym(grad(phi_j)), with lambda = nu E/((1+nu)(1-2nu)), mu = E/(2(1+nu)) per cell.  For
+// dofs (node a, component ci) and (node b, component cj) this is
+//   dV [lambda g_a[ci] g_b[cj] + mu g_a[cj] g_b[ci] + mu delta_{ci cj} g_a.g_b],
+// so with s = sqrt(dV) g and A_ab = sum_q s_a s_b^T (3x3, 9 FP64 FMAs per node pair and
+// Gauss point) the 3x3 block of the node pair is lambda A + mu A^T + mu tr(A) I.
+// Cell-local dof order: node + component*NN (component-major), as in the reference.
+template <int P>
+struct ElastShape {
+  static constexpr int NP1 = P + 1;
+  static constexpr int NN = NP1 * NP1 * NP1;
+  static constexpr int NQ = NN;
+  static constexpr int ND = 3 * NN;
+  static constexpr int NPAIR = NN * (NN + 1) / 2;
+  static constexpr int CH = P == 1 ? 2 : 4;  // node pairs per lane per pass
+  static constexpr int WARPS = P == 1 ? 8 : 3;
+  static constexpr int SM_XV = 24, SM_INVJ = NQ * 9, SM_FAC = NQ, SM_XQ = NQ * 3, SM_F = NQ * 3, SM_SQ = NQ,
+                       SM_G = NQ * NN * 3, SM_EL = ND * ND;
+  static constexpr int SM_DOUBLES = SM_XV + SM_INVJ + SM_FAC + SM_XQ + SM_F + SM_SQ + SM_G + SM_EL;
+  static constexpr int SM_INTS = ND;
+  static constexpr size_t SM_BYTES_WARP = ((size_t)SM_DOUBLES * 8 + SM_INTS * 4 + 15) / 16 * 16;
+};
+
+template <int P>
+__global__ void __launch_bounds__(ElastShape<P>::WARPS * 32)
+    k_integrate_elasticity(AsmGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
+                           const int32_t* __restrict__ latdof, const double* __restrict__ gvals,
+                           const double* __restrict__ coef, double coef_const, double nu, SourceSpec src,
+                           double* __restrict__ E, double* __restrict__ EV) {
+  using S = ElastShape<P>;
+  constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND, NP1 = S::NP1;
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double* base = smem + (size_t)wib * (S::SM_BYTES_WARP / 8);
+  double* xv = base;
+  double* invj = xv + S::SM_XV;
+  double* fac = invj + S::SM_INVJ;
+  double* xq = fac + S::SM_FAC;
+  double* fsrc = xq + S::SM_XQ;
+  double* sq = fsrc + S::SM_F;
+  double* sg = sq + S::SM_SQ;
+  double* el = sg + S::SM_G;
+  int32_t* gid = (int32_t*)(el + S::SM_EL);
+
+  const int64_t c = (int64_t)blockIdx.x * S::WARPS + wib;
+  if (c >= ncells) return;
+  const int ci = (int)(c % g.n[0]);
+  const int cj = (int)((c / g.n[0]) % g.n[1]);
+  const int ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
+  const double Ev = coef ? coef[c] : coef_const;
+  const double lambda = (nu * Ev) / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  const double mu = Ev / (2.0 * (1.0 + nu));
+
+  if (lane < 24) {
+    int k = lane / 3, l = lane % 3;
+    int64_t v = (int64_t)(ci + (k & 1)) +
+                (int64_t)(g.n[0] + 1) * ((cj + ((k >> 1) & 1)) + (int64_t)(g.n[1] + 1) * (ck + ((k >> 2) & 1)));
+    xv[lane] = coords[v * 3 + l];
+  }
+  for (int s = lane; s < ND; s += 32) {
+    const int a = s % NN, comp = s / NN;
+    const int ai = a % NP1, aj = (a / NP1) % NP1, ak = a / (NP1 * NP1);
+    const int64_t L = (int64_t)(P * ci + ai) + (int64_t)g.Ln[0] * ((P * cj + aj) + (int64_t)g.Ln[1] * (P * ck + ak));
+    gid[s] = latdof[L * 3 + comp];
+  }
+  __syncwarp();
+  for (int q = lane; q < NQ; q += 32) {
+    double J[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        double alpha = tb.gshg[(k * NQ + q) * 3 + j];
+        a0 = a0 + alpha * xv[k * 3 + 0];
+        a1 = a1 + alpha * xv[k * 3 + 1];
+        a2 = a2 + alpha * xv[k * 3 + 2];
+      }
+      J[0 + 3 * j] = a0; J[1 + 3 * j] = a1; J[2 + 3 * j] = a2;
+    }
+    double t1 = J[4] * J[8] - J[5] * J[7];
+    double t2 = -J[1] * J[8] + J[2] * J[7];
+    double t3 = J[1] * J[5] - J[2] * J[4];
+    double det = J[0] * t1 + J[3] * t2 + J[6] * t3;
+    double denom = 1.0 / det;
+    double* b = invj + q * 9;
+    b[0] = t1 * denom;
+    b[1] = t2 * denom;
+    b[2] = t3 * denom;
+    b[4] = (J[0] * J[8] - J[2] * J[6]) * denom;
+    b[5] = (-J[0] * J[5] + J[3] * J[2]) * denom;
+    b[8] = (J[0] * J[4] - J[1] * J[3]) * denom;
+    b[3] = (-J[3] * J[8] + J[5] * J[6]) * denom;
+    b[6] = (J[3] * J[7] - J[4] * J[6]) * denom;
+    b[7] = (-J[0] * J[7] + J[1] * J[6]) * denom;
+    fac[q] = det;
+    double x0 = 0.0, x1 = 0.0, x2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      double a = tb.gshp[k * NQ + q];
+      x0 = x0 + a * xv[k * 3 + 0];
+      x1 = x1 + a * xv[k * 3 + 1];
+      x2 = x2 + a * xv[k * 3 + 2];
+    }
+    xq[q * 3 + 0] = x0; xq[q * 3 + 1] = x1; xq[q * 3 + 2] = x2;
+  }
+  __syncwarp();
+  const bool neg = fac[0] < 0.0;
+  __syncwarp();
+  for (int q = lane; q < NQ; q += 32) {
+    double d = neg ? fabs(fac[q]) : fac[q];
+    fac[q] = d * tb.qw[q];
+    for (int comp = 0; comp < 3; ++comp) {
+      double f;
+      if (src.fn == FG_FN_QP_VALUES) f = src.qp[(c * NQ + q) * 3 + comp];
+      else if (src.fn == FG_FN_CONST) f = src.prm[comp];
+      else f = 0.0;
+      fsrc[q * 3 + comp] = f;
+    }
+    sq[q] = sqrt(fac[q]);
+  }
+  __syncwarp();
+  for (int idx = lane; idx < NQ * NN; idx += 32) {
+    int q = idx / NN, a = idx % NN;
+    const double* rg = tb.shg + ((size_t)a * NQ + q) * 3;
+    const double* b = invj + q * 9;
+    const double s = sq[q];
+    double r0 = rg[0], r1 = rg[1], r2 = rg[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) sg[idx * 3 + i] = s * (b[0 + 3 * i] * r0 + b[1 + 3 * i] * r1 + b[2 + 3 * i] * r2);
+  }
+  __syncwarp();
+  for (int pbase = 0; pbase < S::NPAIR; pbase += 32 * S::CH) {
+    double A[S::CH][9];
+    int pa[S::CH], pb[S::CH];
+#pragma unroll
+    for (int t = 0; t < S::CH; ++t) {
+#pragma unroll
+      for (int e = 0; e < 9; ++e) A[t][e] = 0.0;
+      int p = pbase + lane + 32 * t;
+      if (p < S::NPAIR) pair_ab(p, NN, pa[t], pb[t]);
+      else { pa[t] = 0; pb[t] = 0; }
+    }
+    for (int q = 0; q < NQ; ++q) {
+      const double* gq = sg + q * NN * 3;
+#pragma unroll
+      for (int t = 0; t < S::CH; ++t) {
+        const double* sa = gq + pa[t] * 3;
+        const double* sb = gq + pb[t] * 3;
+        const double a0 = sa[0], a1 = sa[1], a2 = sa[2], b0 = sb[0], b1 = sb[1], b2 = sb[2];
+        A[t][0] = fma(a0, b0, A[t][0]); A[t][1] = fma(a0, b1, A[t][1]); A[t][2] = fma(a0, b2, A[t][2]);
+        A[t][3] = fma(a1, b0, A[t][3]); A[t][4] = fma(a1, b1, A[t][4]); A[t][5] = fma(a1, b2, A[t][5]);
+        A[t][6] = fma(a2, b0, A[t][6]); A[t][7] = fma(a2, b1, A[t][7]); A[t][8] = fma(a2, b2, A[t][8]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < S::CH; ++t) {
+      int p = pbase + lane + 32 * t;
+      if (p >= S::NPAIR) continue;
+      const double tr = A[t][0] + A[t][4] + A[t][8];
+#pragma unroll
+      for (int u = 0; u < 3; ++u)
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+          double m = lambda * A[t][u * 3 + v] + mu * A[t][v * 3 + u];
+          if (u == v) m = m + mu * tr;
+          const int i = pa[t] + u * NN, j = pb[t] + v * NN;
+          el[i * ND + j] = m;
+          el[j * ND + i] = m;
+        }
+    }
+  }
+  __syncwarp();
+  bool any_dir = false;
+  for (int s = lane; s < ND; s += 32) any_dir |= gid[s] < 0;
+  any_dir = __any_sync(0xffffffffu, any_dir);
+  for (int i = lane; i < ND; i += 32) {
+    const int a = i % NN, comp = i / NN;
+    double ev = 0.0;
+    for (int q = 0; q < NQ; ++q) ev = ev + fac[q] * (fsrc[q * 3 + comp] * tb.shp[(size_t)a * NQ + q]);
+    if (any_dir)
+      for (int j = 0; j < ND; ++j) {
+        int32_t gj = gid[j];
+        if (gj < 0) ev = ev - el[i * ND + j] * gvals[-gj - 1];
+      }
+    EV[c * ND + i] = ev;
+  }
+  double* Ec = E + (size_t)c * ND * ND;
+  for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = el[idx];
+}
+
+template <int P>
+static fg_status launch_elasticity(fg_system* sys) {
+  using S = ElastShape<P>;
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  AsmGeom g = make_geom(sp);
+  const int64_t ncells = sp->mesh->ncells;
+  SourceSpec src;
+  src.fn = sys->integ.source_fn;
+  for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
+  src.qp = sys->d_qpsrc;
+  const size_t smem = S::SM_BYTES_WARP * S::WARPS;
+  static bool attr_set = false;
+  if (!attr_set) {
+    FG_CUDA_TRY(cudaFuncSetAttribute(k_integrate_elasticity<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  ctx->launches += sp->nfree > 0 ? 2 : 1;
+  k_integrate_elasticity<P><<<nblk(ncells, S::WARPS), S::WARPS * 32, smem, ctx->stream>>>(
+      g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof, sys->d_gvals, sys->d_coef, sys->integ.coef_const,
+      sys->integ.nu, src, sys->d_elmat, sys->d_elvec);
+  FG_CUDA_TRY(cudaGetLastError());
+  const int64_t n = sp->nfree;
+  if (n > 0) {
+    constexpr int CAP = P == 1 ? 128 : 512;  // (2P+1)^3 * 3 box entries
+    k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,
+                                                                 sp->d_col, sys->d_elmat, sys->d_elvec, sys->d_val,
+                                                                 sys->d_val32, sys->d_rhs);
+    FG_CUDA_TRY(cudaGetLastError());
+  }
+  return FG_OK;
+}
+
 fg_status system_assemble(fg_system* sys) {
   fg_space* sp = sys->space;
+  if (sys->integ.kind == FG_ELASTICITY && sp->ncomp == 3) {
+    switch (sp->order) {
+      case 1: return launch_elasticity<1>(sys);
+      case 2: return launch_elasticity<2>(sys);
+      default:
+        set_error("elasticity of order %d is not built on the device (orders 1-2)", sp->order);
+        return FG_ERR_UNSUPPORTED;
+    }
+  }
   if (sys->integ.kind != FG_POISSON || sp->ncomp != 1) {
     set_error("integrand kind %d with %d components is not built", sys->integ.kind, sp->ncomp);
     return FG_ERR_UNSUPPORTED;

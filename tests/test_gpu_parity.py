@@ -259,3 +259,62 @@ def test_solver_layouts(fg, ctx, layout, order, monkeypatch):
         assert s.info()["converged"], (layout, prec)
         err = np.linalg.norm(xs - ref["x"]) / np.linalg.norm(ref["x"])
         assert err <= 1e-9, (layout, prec, err)
+
+
+# ---------------------------------------------------------------------------------------
+# Linear elasticity (3 components): the heterogeneous irreducible integrand of
+# par_test_pb_bddc_linear_elasticity with E per cell, nu = 0.3, body force (0,0,-1).
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("dirichlet", ["clamp", "all"])
+def test_vector_dof_map_bit_exact(fg, ctx, order, dirichlet):
+    ids = CLAMP if dirichlet == "clamp" else list(range(1, 27))
+    n = (3, 2, 4)
+    P = O.Problem(n, order=order, kind=O.ELASTICITY, dirichlet_ids=ids)
+    tri = fg.SerialTriangulation(ctx, n)
+    sp = fg.SerialFESpace(tri, order=order, ncomp=3, dirichlet_ids=ids)
+    assert sp.num_free_dofs == P.nfree and sp.num_dirichlet_dofs == P.ndir
+    assert np.array_equal(sp.get_dof_map(), P.dof_map())
+
+
+def build_elasticity_pair(fg, ctx, n, order, seed=3, perturb=True):
+    xyz = perturbed_vertices(n, 0.15, seed=seed) if perturb else None
+    E = np.exp(np.random.default_rng(seed).normal(0.0, 1.5, size=n[0] * n[1] * n[2]))
+    P = O.Problem(n, order=order, kind=O.ELASTICITY, dirichlet_ids=CLAMP, vertex_xyz=xyz, cell_coef=E, nu=0.3,
+                  source_fn=O.FN_CONST, fn_param=[0.0, 0.0, -1.0])
+    tri = fg.SerialTriangulation(ctx, n, vertex_xyz=xyz)
+    sp = fg.SerialFESpace(tri, order=order, ncomp=3, dirichlet_ids=CLAMP)
+    op = fg.FEAffineOperator(sp, fg.ElasticityIntegration(cell_coef=E, nu=0.3, source_fn=O.FN_CONST,
+                                                          fn_param=[0.0, 0.0, -1.0])).compute()
+    return P, tri, sp, op
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_elasticity_assembly(fg, ctx, order):
+    P, tri, sp, op = build_elasticity_pair(fg, ctx, (4, 3, 3), order)
+    irp, ja, val = op.get_matrix()
+    assert_matrix_close(irp, ja, val, P)
+    b, ob = op.get_translation(), P.rhs()
+    assert np.max(np.abs(b - ob)) <= RHS_TOL * np.max(np.abs(ob))
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_elasticity_solution(fg, ctx, order):
+    P, tri, sp, op = build_elasticity_pair(fg, ctx, (5, 3, 4), order, seed=8)
+    ref = P.cg(precond=1, rtol=1e-13, maxit=50000)
+    for prec, tol in (("fp64", SOL_TOL), ("mixed", 1e-9)):
+        s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
+        s.set_parameters_from_pl({"ILS_RTOL": 1e-13 if prec == "fp64" else 1e-12, "ILS_MAX_NUM_ITERATIONS": 50000,
+                                  "PRECISION": prec})
+        x = s.solve()
+        assert s.info()["converged"], prec
+        err = np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"])
+        assert err <= tol, (prec, err)
+
+
+def test_elasticity_q3_reported_unsupported(fg, ctx):
+    from fempar_gb300 import FGError
+    tri = fg.SerialTriangulation(ctx, (2, 2, 2))
+    sp = fg.SerialFESpace(tri, order=3, ncomp=3, dirichlet_ids=CLAMP)
+    with pytest.raises(FGError):
+        fg.FEAffineOperator(sp, fg.ElasticityIntegration(cell_coef=np.ones(8), nu=0.3)).compute()
