@@ -35,6 +35,8 @@ EXPORTS = [
     "fg_system_spmv_device", "fg_system_spmv_device_noalloc", "fg_system_spmv_solver_layout_device",
     "fg_solve", "fg_solve_device",
     "fg_solver_params_default", "fg_integrand_default",
+    "fg_request_footprint", "fg_server_create", "fg_server_submit", "fg_server_wait", "fg_server_take_solution",
+    "fg_server_stats", "fg_server_destroy",
 ]
 
 
@@ -86,6 +88,36 @@ class SpaceInfo(C.Structure):
         ("num_cells", C.c_int64), ("num_free", C.c_int64), ("num_dirichlet", C.c_int64),
         ("nnz_full", C.c_int64), ("nnz_upper", C.c_int64), ("solver_vec_len", C.c_int64),
         ("solver_entries", C.c_int64), ("solver_layout", C.c_int32),
+    ]
+
+
+class Request(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("n", C.c_int32 * 3),
+        ("order", C.c_int),
+        ("cell_coef", C.c_void_p),
+        ("coef_const", C.c_double),
+        ("nu", C.c_double),
+        ("source_fn", C.c_int),
+        ("fn_param", C.c_double * 8),
+        ("dirichlet_ids", C.c_void_p),
+        ("n_ids", C.c_int),
+        ("solver", SolverParams),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("iterations", C.c_int),
+        ("outer_iterations", C.c_int),
+        ("num_free", C.c_int64),
+        ("t_queue_ms", C.c_double),
+        ("t_run_ms", C.c_double),
+        ("t_total_ms", C.c_double),
+        ("solve_ms", C.c_double),
+        ("footprint_bytes", C.c_uint64),
     ]
 
 
@@ -144,6 +176,13 @@ def lib():
         "fg_solve": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
         "fg_solve_device": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
         "fg_solver_params_default": (None, [C.POINTER(SolverParams)]),
+        "fg_request_footprint": (i32, [C.POINTER(Request), C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
+        "fg_server_create": (i32, [i32, C.c_uint64, i32, pp]),
+        "fg_server_submit": (i32, [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+        "fg_server_wait": (i32, [vp, C.c_uint64, i32, C.POINTER(Result)]),
+        "fg_server_take_solution": (i32, [vp, C.c_uint64, vp]),
+        "fg_server_stats": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
+        "fg_server_destroy": (i32, [vp]),
         "fg_integrand_default": (None, [C.POINTER(Integrand)]),
     }
     for name, (res, args) in sig.items():

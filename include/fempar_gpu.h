@@ -224,6 +224,54 @@ fg_status fg_solve(fg_system* sys, const fg_solver_params* params, const double*
 fg_status fg_solve_device(fg_system* sys, const fg_solver_params* params, const double* b_dev,
                           const double* x0_dev, double* x_dev, fg_solve_info* info);
 
+/* ---------------------------------------------------------------------------------------
+ * Serving: a device-resident request loop.  No counterpart in the reference (FEMPAR runs
+ * one problem per program); built from the entry points above.  Worker threads each own a
+ * context (its own CUDA stream) on one device; a request (mesh, FE space, integrand,
+ * solver parameters) is admitted when its estimated device footprint fits the remaining
+ * HBM budget, queued per size class (log2 of its dofs) and taken oldest-first among the
+ * classes whose head fits; admitted requests run concurrently and overlap on the GPU.
+ * Each request's mesh, matrix and Krylov state live on the device until its solution is
+ * copied out; a request whose footprint exceeds the whole budget is refused at submit.
+ * Results do not depend on what else runs: kernels use fixed grids and reductions. */
+typedef struct fg_server fg_server;
+
+typedef struct {
+  int kind;                     /* FG_POISSON / FG_ELASTICITY                          */
+  int32_t n[3];                 /* cells per direction (unit cube)                     */
+  int order;                    /* 1..3 (elasticity 1..2)                              */
+  const double* cell_coef;      /* host, ncells (copied at submit); NULL = coef_const  */
+  double coef_const, nu;
+  int source_fn;                /* FG_FN_ZERO / FG_FN_CONST                            */
+  double fn_param[8];
+  const int32_t* dirichlet_ids; /* copied at submit                                    */
+  int n_ids;
+  fg_solver_params solver;
+} fg_request;
+
+typedef struct {
+  fg_status status;             /* of the request's own calls                          */
+  int iterations, outer_iterations;
+  int64_t num_free;
+  double t_queue_ms;            /* submit -> start                                     */
+  double t_run_ms;              /* start -> solution on the host                       */
+  double t_total_ms;            /* submit -> solution on the host                      */
+  double solve_ms;              /* device time of the solve                            */
+  uint64_t footprint_bytes;
+} fg_result;
+
+/* Estimated device bytes of a request (admission unit) and its free-dof count. */
+fg_status fg_request_footprint(const fg_request* req, uint64_t* bytes, int64_t* num_free);
+fg_status fg_server_create(int device, uint64_t hbm_budget_bytes, int nworkers, fg_server** out);
+fg_status fg_server_submit(fg_server* srv, const fg_request* req, uint64_t* ticket);
+/* Wait up to timeout_ms (< 0: forever) for a request; FG_ERR_TIMEOUT if not finished. */
+fg_status fg_server_wait(fg_server* srv, uint64_t ticket, int timeout_ms, fg_result* res);
+/* Copy the solution (num_free doubles, reference dof order) and release the request. */
+fg_status fg_server_take_solution(fg_server* srv, uint64_t ticket, double* x);
+/* Peak device bytes reserved by admitted requests so far. */
+fg_status fg_server_stats(fg_server* srv, uint64_t* peak_reserved, int64_t* completed);
+fg_status fg_server_destroy(fg_server* srv);
+
 /* Default parameters (reference defaults: CG, res_res, rtol 1e-6, 1000 iterations). */
 void fg_solver_params_default(fg_solver_params* p);
 void fg_integrand_default(fg_integrand* g);
