@@ -24,11 +24,13 @@ fg_status dev_alloc(fg_ctx* ctx, void** p, size_t bytes) {
               (unsigned long long)bytes, (unsigned long long)ctx->budget);
     return FG_ERR_OOM;
   }
-  cudaError_t e = cudaMalloc(p, bytes);
+  // stream-ordered pool allocation on the context's stream: no device-wide
+  // synchronisation on free, so contexts on other threads keep running
+  cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     *p = nullptr;
-    set_error("cudaMalloc(%llu): %s", (unsigned long long)bytes, cudaGetErrorString(e));
+    set_error("cudaMallocAsync(%llu): %s", (unsigned long long)bytes, cudaGetErrorString(e));
     return FG_ERR_OOM;
   }
   ctx->allocs[*p] = bytes;
@@ -43,7 +45,7 @@ void dev_free(fg_ctx* ctx, void* p) {
     ctx->in_use -= it->second;
     ctx->allocs.erase(it);
   }
-  cudaFree(p);
+  cudaFreeAsync(p, ctx->stream);
 }
 
 }  // namespace fg
@@ -120,6 +122,15 @@ fg_status fg_ctx_create(int device, uint64_t hbm_budget_bytes, fg_ctx** out) {
     set_error("stream: %s", cudaGetErrorString(e));
     return FG_ERR_CUDA;
   }
+  {
+    // keep freed blocks in the device's pool (reused by later allocations of any context)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    cudaGetLastError();
+  }
   size_t freeb = 0, totalb = 0;
   cudaMemGetInfo(&freeb, &totalb);
   c->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)freeb;
@@ -131,8 +142,15 @@ fg_status fg_ctx_destroy(fg_ctx* ctx) {
   if (!ctx) return FG_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  for (auto& kv : ctx->allocs) cudaFree(kv.first);
+  for (auto& kv : ctx->allocs) cudaFreeAsync(kv.first, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
   ctx->allocs.clear();
+  {
+    // hand the pool's unused blocks back to the device when a context ends
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    cudaGetLastError();
+  }
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return FG_OK;
