@@ -19,7 +19,8 @@ FG_ERR_NOT_CONVERGED = -4
 FG_POISSON, FG_ELASTICITY = 0, 1
 FG_FN_ZERO, FG_FN_CONST, FG_FN_SHARP_WAVE, FG_FN_LINEAR, FG_FN_QP_VALUES = 0, 1, 2, 3, 4
 FG_INPUTS_ON_DEVICE = 1
-FG_PREC_NONE, FG_PREC_JACOBI = 0, 1
+FG_PREC_NONE, FG_PREC_JACOBI, FG_PREC_BDDC = 0, 1, 2
+FG_BDDC_WEIGHT_MULTIPLICITY, FG_BDDC_WEIGHT_STIFFNESS = 0, 1
 FG_FP64, FG_MIXED = 0, 1
 FG_RES_RES, FG_RES_RHS, FG_DELTA_RHS, FG_DELTA_DELTA, FG_RES_NRMGIVEN_RHS_NRMGIVEN, FG_RES_NRMGIVEN_RES_NRMGIVEN = range(6)
 
@@ -35,6 +36,8 @@ EXPORTS = [
     "fg_system_spmv_device", "fg_system_spmv_device_noalloc", "fg_system_spmv_solver_layout_device",
     "fg_solve", "fg_solve_device",
     "fg_solver_params_default", "fg_integrand_default",
+    "fg_bddc_params_default", "fg_bddc_create", "fg_bddc_numerical_setup", "fg_bddc_get_info",
+    "fg_bddc_apply_device", "fg_bddc_solve", "fg_bddc_solve_device", "fg_bddc_destroy",
     "fg_request_footprint", "fg_server_create", "fg_server_submit", "fg_server_wait", "fg_server_take_solution",
     "fg_server_stats", "fg_server_destroy",
 ]
@@ -88,6 +91,29 @@ class SpaceInfo(C.Structure):
         ("num_cells", C.c_int64), ("num_free", C.c_int64), ("num_dirichlet", C.c_int64),
         ("nnz_full", C.c_int64), ("nnz_upper", C.c_int64), ("solver_vec_len", C.c_int64),
         ("solver_entries", C.c_int64), ("solver_layout", C.c_int32),
+    ]
+
+
+class BddcParams(C.Structure):
+    _fields_ = [
+        ("nsub", C.c_int32 * 3),
+        ("cuts", C.c_void_p),
+        ("use_vertices", C.c_int32),
+        ("use_edges", C.c_int32),
+        ("use_faces", C.c_int32),
+        ("weighting", C.c_int32),
+    ]
+
+
+class BddcInfo(C.Structure):
+    _fields_ = [
+        ("num_subdomains", C.c_int32),
+        ("max_local_dofs", C.c_int32),
+        ("num_interface_dofs", C.c_int64),
+        ("num_coarse_dofs", C.c_int64),
+        ("symbolic_ms", C.c_double),
+        ("numeric_ms", C.c_double),
+        ("device_bytes", C.c_uint64),
     ]
 
 
@@ -184,6 +210,14 @@ def lib():
         "fg_server_stats": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
         "fg_server_destroy": (i32, [vp]),
         "fg_integrand_default": (None, [C.POINTER(Integrand)]),
+        "fg_bddc_params_default": (None, [C.POINTER(BddcParams)]),
+        "fg_bddc_create": (i32, [vp, C.POINTER(BddcParams), pp]),
+        "fg_bddc_numerical_setup": (i32, [vp]),
+        "fg_bddc_get_info": (i32, [vp, C.POINTER(BddcInfo)]),
+        "fg_bddc_apply_device": (i32, [vp, i32, vp, vp]),
+        "fg_bddc_solve": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
+        "fg_bddc_solve_device": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
+        "fg_bddc_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

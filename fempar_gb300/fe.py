@@ -268,6 +268,82 @@ _CRITERIA = {"RES_RES": L.FG_RES_RES, "RES_RHS": L.FG_RES_RHS, "DELTA_RHS": L.FG
              "RES_NRMGIVEN_RES_NRMGIVEN": L.FG_RES_NRMGIVEN_RES_NRMGIVEN}
 
 
+def bddc_cuts(n, nsub, jitter=0.0, seed=20261203):
+    """Cell cut positions of a box partition: nsub[d] slabs per direction, widths jittered
+    by up to +-jitter (fraction of the even width) with a seeded generator, each >= 1."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cuts = []
+    for d in range(3):
+        nd, ns = int(n[d]), int(nsub[d])
+        base = nd / ns
+        w = np.full(ns, base)
+        if jitter > 0 and ns > 1:
+            w = w * (1.0 + rng.uniform(-jitter, jitter, size=ns))
+        c = np.concatenate([[0.0], np.cumsum(w)])
+        c = np.round(c * nd / c[-1]).astype(np.int64)
+        for k in range(1, ns + 1):
+            c[k] = max(c[k], c[k - 1] + 1)
+        for k in range(ns - 1, -1, -1):
+            c[k] = min(c[k], c[k + 1] - 1)
+        c[0], c[-1] = 0, nd
+        cuts.append(c.astype(np.int32))
+    return cuts
+
+
+class MLBDDC:
+    """mlbddc_t on box subdomains (two levels; coarse problem solved directly).
+
+    Mirrors mlbddc_t's life cycle (sbm_base_mlbddc.i90:162-474): construction does the
+    symbolic and numerical setup from the operator's element matrices;
+    ``numerical_setup()`` refreshes it after ``FEAffineOperator.compute()`` on new data.
+    Parameters follow the reference's coarse-space switches (coarse_space_use_vertices /
+    edges / faces) and the standard handler's multiplicity weighting."""
+
+    def __init__(self, A: FEAffineOperator, nsub=(2, 2, 2), cuts=None, use_vertices=True, use_edges=True,
+                 use_faces=False, weighting=L.FG_BDDC_WEIGHT_MULTIPLICITY):
+        p = L.BddcParams()
+        L.lib().fg_bddc_params_default(C.byref(p))
+        for d in range(3):
+            p.nsub[d] = int(nsub[d])
+        self._cuts = None
+        if cuts is not None:
+            self._cuts = np.ascontiguousarray(np.concatenate([np.asarray(c, dtype=np.int32) for c in cuts]))
+            p.cuts = self._cuts.ctypes.data
+        p.use_vertices, p.use_edges, p.use_faces = int(use_vertices), int(use_edges), int(use_faces)
+        p.weighting = int(weighting)
+        self.A = A
+        h = C.c_void_p()
+        L.check(L.lib().fg_bddc_create(A.h, C.byref(p), C.byref(h)), "fg_bddc_create")
+        self.h = h
+
+    def numerical_setup(self):
+        L.check(L.lib().fg_bddc_numerical_setup(self.h), "fg_bddc_numerical_setup")
+
+    def info(self):
+        i = L.BddcInfo()
+        L.check(L.lib().fg_bddc_get_info(self.h, C.byref(i)), "fg_bddc_get_info")
+        return {k: getattr(i, k) for k, _ in L.BddcInfo._fields_}
+
+    def apply_device(self, r, z, precision=L.FG_FP64):
+        """z = M^-1 r on torch CUDA float64 tensors of num_free_dofs entries."""
+        n = self.A.space.num_free_dofs
+        for t in (r, z):
+            if t.numel() != n or t.dtype.itemsize != 8 or not t.is_contiguous():
+                raise ValueError("r and z must be contiguous float64 tensors of num_free_dofs entries")
+        L.check(L.lib().fg_bddc_apply_device(self.h, precision, _ptr(r), _ptr(z)), "fg_bddc_apply_device")
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().fg_bddc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class IterativeLinearSolver:
     """iterative_linear_solver_t with the CG type (FP64 reference CG or mixed precision)."""
 
@@ -276,6 +352,7 @@ class IterativeLinearSolver:
         L.lib().fg_solver_params_default(C.byref(p))
         self.params = p
         self.A = None
+        self.M = None
         self.last_info = None
 
     def set_type_from_string(self, name: str):
@@ -310,8 +387,13 @@ class IterativeLinearSolver:
         return self
 
     def set_operators(self, A: FEAffineOperator, M="identity"):
+        """M: "identity", "jacobi" or an MLBDDC built on A."""
         self.A = A
-        self.params.precond = L.FG_PREC_JACOBI if str(M).lower() == "jacobi" else L.FG_PREC_NONE
+        self.M = M if isinstance(M, MLBDDC) else None
+        if self.M is not None:
+            self.params.precond = L.FG_PREC_BDDC
+        else:
+            self.params.precond = L.FG_PREC_JACOBI if str(M).lower() == "jacobi" else L.FG_PREC_NONE
         return self
 
     def solve(self, b=None, x0=None, raise_on_nonconvergence=False, out=None):
@@ -322,7 +404,10 @@ class IterativeLinearSolver:
         info = L.SolveInfo()
         bb = None if b is None else np.ascontiguousarray(b, dtype=np.float64)
         xx0 = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
-        st = L.lib().fg_solve(self.A.h, C.byref(self.params), _ptr(bb), _ptr(xx0), _ptr(x), C.byref(info))
+        if self.M is not None:
+            st = L.lib().fg_bddc_solve(self.M.h, C.byref(self.params), _ptr(bb), _ptr(xx0), _ptr(x), C.byref(info))
+        else:
+            st = L.lib().fg_solve(self.A.h, C.byref(self.params), _ptr(bb), _ptr(xx0), _ptr(x), C.byref(info))
         if st != L.FG_OK and (st != L.FG_ERR_NOT_CONVERGED or raise_on_nonconvergence):
             raise L.FGError(st, "fg_solve")
         self.last_info = info
@@ -335,7 +420,11 @@ class IterativeLinearSolver:
         if x is None:
             x = torch.empty(n, dtype=torch.float64, device=f"cuda:{self.A.space.triangulation.ctx.device}")
         info = L.SolveInfo()
-        st = L.lib().fg_solve_device(self.A.h, C.byref(self.params), _ptr(b), _ptr(x0), _ptr(x), C.byref(info))
+        if self.M is not None:
+            st = L.lib().fg_bddc_solve_device(self.M.h, C.byref(self.params), _ptr(b), _ptr(x0), _ptr(x),
+                                              C.byref(info))
+        else:
+            st = L.lib().fg_solve_device(self.A.h, C.byref(self.params), _ptr(b), _ptr(x0), _ptr(x), C.byref(info))
         if st not in (L.FG_OK, L.FG_ERR_NOT_CONVERGED):
             raise L.FGError(st, "fg_solve_device")
         self.last_info = info

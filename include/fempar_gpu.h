@@ -225,6 +225,62 @@ fg_status fg_solve_device(fg_system* sys, const fg_solver_params* params, const 
                           const double* x0_dev, double* x_dev, fg_solve_info* info);
 
 /* ---------------------------------------------------------------------------------------
+ * BDDC preconditioner (two levels: box subdomains of cells and a coarse problem).
+ * Replaces mlbddc_t (Sources/Lib/LinearAlgebra/Preconditioner/mlbddc.f90,
+ * sbm_base_mlbddc.i90:162-1527) built on a par_fe_space_t with the standard coarse FE
+ * handler (Sources/Lib/Integration/FESpace/sbm_standard_coarse_fe_handler.i90): the same
+ * apply (interior correction, weighted coarse + constrained-Neumann correction, weighted
+ * sum, harmonic extension; sbm_base_mlbddc.i90:909-1009), one coarse dof per object and
+ * component with per-component averages as constraints (:121-219), multiplicity weights
+ * (:221-295).  The subdomain and coarse matrices are factorised by FP64 Cholesky on the
+ * device (the reference calls a sparse direct solver).  Objects come from the box grid:
+ * interface nodes on slab planes in all three directions are vertices (they are always
+ * primal: use_vertices must be 1), nodes on two interior cut planes edge points, on one
+ * a face point.  Subdomain matrices are dense: the library refuses (FG_ERR_OOM) a
+ * partition whose dense local matrices do not fit the context's HBM budget. */
+typedef struct fg_bddc fg_bddc;
+enum { FG_PREC_BDDC = 2 };
+enum { FG_BDDC_WEIGHT_MULTIPLICITY = 0, FG_BDDC_WEIGHT_STIFFNESS = 1 };
+typedef struct {
+  int32_t nsub[3];         /* subdomains per direction                                     */
+  const int32_t* cuts;     /* NULL: even split; else nsub[0]+1, nsub[1]+1, nsub[2]+1 increasing
+                              cell indices per direction, from 0 to n[d]                   */
+  int32_t use_vertices;    /* coarse_space_use_vertices (must be 1)                       */
+  int32_t use_edges;       /* coarse_space_use_edges                                       */
+  int32_t use_faces;       /* coarse_space_use_faces                                       */
+  int32_t weighting;       /* FG_BDDC_WEIGHT_MULTIPLICITY (reference standard handler) or
+                              FG_BDDC_WEIGHT_STIFFNESS (diag(A_i) / sum_j diag(A_j))        */
+} fg_bddc_params;
+typedef struct {
+  int32_t num_subdomains;
+  int32_t max_local_dofs;
+  int64_t num_interface_dofs;
+  int64_t num_coarse_dofs;
+  double symbolic_ms, numeric_ms;
+  uint64_t device_bytes;
+} fg_bddc_info;
+void fg_bddc_params_default(fg_bddc_params* p);
+/* symbolic_setup + numerical_setup (sbm_base_mlbddc.i90:162-201,437-474) on the system's
+ * current element matrices.  The system must stay alive while the preconditioner does. */
+fg_status fg_bddc_create(fg_system* sys, const fg_bddc_params* params, fg_bddc** out);
+/* numerical_setup again after fg_system_reassemble (same mesh, space and partition). */
+fg_status fg_bddc_numerical_setup(fg_bddc* bddc);
+fg_status fg_bddc_get_info(fg_bddc* bddc, fg_bddc_info* info);
+/* z = M^-1 r (base_mlbddc_apply, sbm_base_mlbddc.i90:853-1009) on device vectors of
+ * num_free FP64 entries in free-dof order.  precision FG_MIXED applies the FP32 copies of
+ * the factors (inputs and outputs stay FP64). */
+fg_status fg_bddc_apply_device(fg_bddc* bddc, int precision, const double* r_dev, double* z_dev);
+/* PCG preconditioned by the BDDC (cg.f90:101-407 with mlbddc_t as the preconditioner):
+ * params as for fg_solve (precond is ignored; every stopping criterion is supported).
+ * FG_FP64: all FP64.  FG_MIXED: FP64 Krylov vectors, SpMV and dots; FP32 preconditioner
+ * (factors, local vectors and the two SpMVs inside the apply). */
+fg_status fg_bddc_solve(fg_bddc* bddc, const fg_solver_params* params, const double* b, const double* x0,
+                        double* x, fg_solve_info* info);
+fg_status fg_bddc_solve_device(fg_bddc* bddc, const fg_solver_params* params, const double* b_dev,
+                               const double* x0_dev, double* x_dev, fg_solve_info* info);
+fg_status fg_bddc_destroy(fg_bddc* bddc);
+
+/* ---------------------------------------------------------------------------------------
  * Serving: a device-resident request loop.  No counterpart in the reference (FEMPAR runs
  * one problem per program); built from the entry points above.  Worker threads each own a
  * context (its own CUDA stream) on one device; a request (mesh, FE space, integrand,
