@@ -114,6 +114,9 @@ class BddcInfo(C.Structure):
         ("symbolic_ms", C.c_double),
         ("numeric_ms", C.c_double),
         ("device_bytes", C.c_uint64),
+        ("factor_flops", C.c_double),
+        ("factor_ms", C.c_double),
+        ("coarse_ms", C.c_double),
     ]
 
 

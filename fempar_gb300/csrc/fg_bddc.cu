@@ -110,7 +110,7 @@ struct fg_bddc {
   double* dPart = nullptr;                                     // reduction partials
   int* dErr = nullptr;
   int nred = 0;
-  double symbolic_ms = 0.0, numeric_ms = 0.0;
+  double symbolic_ms = 0.0, numeric_ms = 0.0, factor_flops = 0.0, factor_ms = 0.0, coarse_ms = 0.0;
   uint64_t bytes = 0;
   std::vector<void*> owned;
 };
@@ -1090,6 +1090,7 @@ static fg_status bddc_symbolic(fg_bddc* B) {
         goff += (int64_t)ne * ne + (int64_t)ne * nV;
         S.boff = boff;
         boff += nbox;
+        B->factor_flops += ((double)S.N * S.N * S.N - (double)(S.N - S.nr) * (S.N - S.nr) * (S.N - S.nr)) / 3.0;
         B->maxN = std::max(B->maxN, S.N);
         B->maxnr = std::max(B->maxnr, S.nr);
         B->maxnI = std::max(B->maxnI, S.nI);
@@ -1245,10 +1246,21 @@ static fg_status bddc_numeric(fg_bddc* B) {
   if (B->nIface > 0)
     k_bddc_weights<<<nblk(B->nIface, 256), 256, 0, st>>>(B->nIface, B->dIptr, B->dIsrc, B->dDiag,
                                                          B->prm.weighting == FG_BDDC_WEIGHT_STIFFNESS, B->dW);
+  cudaEvent_t ev[4];
+  for (auto& e : ev) FG_CUDA_TRY(cudaEventCreate(&e));
+  FG_CUDA_TRY(cudaEventRecord(ev[0], st));
   k_bddc_potrf<<<ns, 256, 0, st>>>(B->d_subs, B->dA, B->dErr);
+  FG_CUDA_TRY(cudaEventRecord(ev[1], st));
   ctx->launches += 3;
   FG_CUDA_TRY(cudaGetLastError());
-  FG_TRY(check_err(B, "a subdomain matrix with its vertex dofs removed"));
+  fg_status sf = check_err(B, "a subdomain matrix with its vertex dofs removed");
+  if (sf != FG_OK) {
+    for (auto& e : ev) cudaEventDestroy(e);
+    return sf;
+  }
+  float fms = 0.f;
+  cudaEventElapsedTime(&fms, ev[0], ev[1]);
+  B->factor_ms = fms;
   FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_bddc_coarse_local, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kCoarseLocalSmem));
   k_bddc_coarse_local<<<ns, 128, kCoarseLocalSmem, st>>>(B->d_subs, B->dA, B->dKp, B->dG, B->dG32, B->dErr);
@@ -1257,6 +1269,7 @@ static fg_status bddc_numeric(fg_bddc* B) {
   FG_CUDA_TRY(cudaGetLastError());
   FG_TRY(check_err(B, "an edge/face constraint block"));
   const int64_t nC = B->nC;
+  FG_CUDA_TRY(cudaEventRecord(ev[2], st));
   if (nC > 0) {
     FG_CUDA_TRY(cudaMemsetAsync(B->dKc, 0, sizeof(double) * 4 * nC * nC, st));
     k_seg_sum<<<nblk(B->nKpair, 256), 256, 0, st>>>(B->nKpair, B->dKptr, B->dKsrc, B->dKdst, B->dKp, B->dKc);
@@ -1267,8 +1280,13 @@ static fg_status bddc_numeric(fg_bddc* B) {
     k_coarse_extract<<<nblk(nC * nC, 256), 256, 0, st>>>(nC, B->dKc, B->dKinv, B->dKinv32);
     ctx->launches += 1;
   }
+  FG_CUDA_TRY(cudaEventRecord(ev[3], st));
   FG_CUDA_TRY(cudaGetLastError());
   FG_CUDA_TRY(cudaStreamSynchronize(st));
+  float cms = 0.f;
+  cudaEventElapsedTime(&cms, ev[2], ev[3]);
+  B->coarse_ms = cms;
+  for (auto& e : ev) cudaEventDestroy(e);
   return FG_OK;
 }
 
@@ -1597,6 +1615,9 @@ fg_status fg_bddc_get_info(fg_bddc* B, fg_bddc_info* info) {
   info->symbolic_ms = B->symbolic_ms;
   info->numeric_ms = B->numeric_ms;
   info->device_bytes = B->bytes;
+  info->factor_flops = B->factor_flops;
+  info->factor_ms = B->factor_ms;
+  info->coarse_ms = B->coarse_ms;
   return FG_OK;
 }
 

@@ -258,6 +258,9 @@ typedef struct {
   int64_t num_coarse_dofs;
   double symbolic_ms, numeric_ms;
   uint64_t device_bytes;
+  double factor_flops;     /* FP64 flops of the batched subdomain partial Cholesky        */
+  double factor_ms;        /* its device time in the last numerical setup (CUDA events)   */
+  double coarse_ms;        /* coarse assembly + factorisation + inverse, device time      */
 } fg_bddc_info;
 void fg_bddc_params_default(fg_bddc_params* p);
 /* symbolic_setup + numerical_setup (sbm_base_mlbddc.i90:162-201,437-474) on the system's
