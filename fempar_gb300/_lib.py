@@ -38,6 +38,7 @@ EXPORTS = [
     "fg_solver_params_default", "fg_integrand_default",
     "fg_bddc_params_default", "fg_bddc_create", "fg_bddc_numerical_setup", "fg_bddc_get_info",
     "fg_bddc_apply_device", "fg_bddc_solve", "fg_bddc_solve_device", "fg_bddc_destroy",
+    "fg_batch_create", "fg_batch_run", "fg_batch_get_info", "fg_batch_destroy",
     "fg_request_footprint", "fg_server_create", "fg_server_submit", "fg_server_wait", "fg_server_take_solution",
     "fg_server_stats", "fg_server_destroy",
 ]
@@ -117,6 +118,37 @@ class BddcInfo(C.Structure):
         ("factor_flops", C.c_double),
         ("factor_ms", C.c_double),
         ("coarse_ms", C.c_double),
+    ]
+
+
+class BatchProblem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("order", C.c_int32),
+        ("coef", C.c_double),
+        ("qp_source", C.c_void_p),
+        ("x", C.c_void_p),
+    ]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("iterations", C.c_int32),
+        ("refinements", C.c_int32),
+        ("team", C.c_int32),
+        ("rel_residual", C.c_double),
+    ]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("threads", C.c_int32), ("ctas", C.c_int32), ("max_team", C.c_int32), ("teams_gt1", C.c_int32),
+        ("graph", C.c_int32),
+        ("total_dofs", C.c_int64),
+        ("predicted_balance", C.c_double),
+        ("run_ms", C.c_double),
+        ("autotune_ms", C.c_double),
     ]
 
 
@@ -221,6 +253,10 @@ def lib():
         "fg_bddc_solve": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
         "fg_bddc_solve_device": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),
         "fg_bddc_destroy": (i32, [vp]),
+        "fg_batch_create": (i32, [vp, i32, C.POINTER(BatchProblem), i32, C.POINTER(SolverParams), i32, pp]),
+        "fg_batch_run": (i32, [vp, C.POINTER(BatchResult)]),
+        "fg_batch_get_info": (i32, [vp, C.POINTER(BatchInfo)]),
+        "fg_batch_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

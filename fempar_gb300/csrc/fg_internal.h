@@ -164,6 +164,11 @@ struct fg_system {
 
 namespace fg {
 
+// fg_refe.cpp: 1D Gauss-Legendre rule (n points on [-1,1], ascending) and the Lagrange basis
+// of order p on equispaced nodes of [-1,1] (value and derivative of basis j at x)
+void gl_rule(int n, double* x, double* w);
+void lagrange_1d(int p, int j, double x, double& v, double& dv);
+
 fg_status dev_alloc(fg_ctx* ctx, void** p, size_t bytes);
 void dev_free(fg_ctx* ctx, void* p);
 fg_status upload_tables(fg_ctx* ctx, const RefTables& t, DevTables& d);

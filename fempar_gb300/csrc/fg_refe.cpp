@@ -20,8 +20,6 @@
 
 namespace fg {
 
-namespace {
-
 // Gauss-Legendre rule on [-1,1] (ascending) by Newton's method on the three-term
 // recurrence of P_n; weights 2/((1-x^2) P_n'(x)^2).
 void gl_rule(int n, double* x, double* w) {
@@ -77,8 +75,8 @@ void lagrange_1d(int p, int j, double x, double& v, double& dv) {
   dv = dnum / den;
 }
 
+namespace {
 int bitcount(int v) { return __builtin_popcount((unsigned)v); }
-
 }  // namespace
 
 void RefTables::build(int p, int nc) {

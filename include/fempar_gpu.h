@@ -284,6 +284,53 @@ fg_status fg_bddc_solve_device(fg_bddc* bddc, const fg_solver_params* params, co
 fg_status fg_bddc_destroy(fg_bddc* bddc);
 
 /* ---------------------------------------------------------------------------------------
+ * Batched independent Poisson problems in one persistent launch.  No counterpart in the
+ * reference (FEMPAR solves one problem per program); each problem is the tutorial /
+ * test_poisson path: -div(k grad u) = f on the unit cube with n^3 uniform hexahedra, Q1-Q3
+ * Lagrangian elements, (order+1)^3 Gauss points, constant k, f given at the Gauss points,
+ * u = 0 on the whole boundary, Jacobi-PCG (cg.f90:101-238, jacobi_preconditioner.f90:356-412)
+ * to ||b - A x|| <= rtol ||b|| + atol.  Assembly (the load vector; the operator is applied
+ * matrix-free from the uniform cell matrix) and the solve are fused in one cooperative
+ * kernel; FP32 CG with float-float (~2^-48) solution, right-hand side and true residuals.
+ * A plan (fg_batch_create) fixes the problems' sizes and buffers, schedules teams of CTAs,
+ * picks the block size (threads = 0: the fastest of 128/256/512 on this batch, timed once)
+ * and captures the launch in a CUDA graph; fg_batch_run re-runs it on the current source
+ * values. */
+typedef struct fg_batch fg_batch;
+typedef struct {
+  int32_t n;                 /* cells per direction                                      */
+  int32_t order;             /* 1..3                                                     */
+  double coef;               /* diffusion coefficient k > 0                              */
+  const double* qp_source;   /* n^3 (order+1)^3 values of f at the Gauss points: cells in
+                                lexicographic order, points x fastest (FG_FN_QP_VALUES)   */
+  double* x;                 /* out: (order n - 1)^3 values at the interior lattice nodes,
+                                x fastest (node (i,j,k), 1 <= i,j,k <= order n - 1)       */
+} fg_batch_problem;
+typedef struct {
+  int32_t status;            /* FG_OK, FG_ERR_NOT_CONVERGED, FG_ERR_NUMERIC, FG_ERR_TIMEOUT */
+  int32_t iterations;
+  int32_t refinements;       /* float-float true residuals computed                      */
+  int32_t team;              /* CTAs that solved the problem                             */
+  double rel_residual;       /* last ||b - A x|| / ||b||                                 */
+} fg_batch_result;
+typedef struct {
+  int32_t threads, ctas, max_team, teams_gt1, graph;
+  int64_t total_dofs;
+  double predicted_balance;  /* planner's estimate: mean CTA load / the longest            */
+  double run_ms;             /* last fg_batch_run (device events, copies included)         */
+  double autotune_ms;
+} fg_batch_info;
+/* flags: FG_INPUTS_ON_DEVICE = qp_source and x are device pointers (read / written in place
+ * at every run); otherwise host pointers, copied in and out by every run.  params: rtol,
+ * atol, max_iters, inner_rtol (reliable-update factor, 0 = 0.1); the rest is ignored. */
+fg_status fg_batch_create(fg_ctx* ctx, int32_t nprob, const fg_batch_problem* problems, int32_t flags,
+                          const fg_solver_params* params, int32_t threads, fg_batch** out);
+/* results: NULL or nprob entries.  Returns the worst status over the problems. */
+fg_status fg_batch_run(fg_batch* batch, fg_batch_result* results);
+fg_status fg_batch_get_info(fg_batch* batch, fg_batch_info* info);
+fg_status fg_batch_destroy(fg_batch* batch);
+
+/* ---------------------------------------------------------------------------------------
  * Serving: a device-resident request loop.  No counterpart in the reference (FEMPAR runs
  * one problem per program); built from the entry points above.  Worker threads each own a
  * context (its own CUDA stream) on one device; a request (mesh, FE space, integrand,
