@@ -38,7 +38,9 @@
 namespace fg {
 
 static constexpr int kBatchMaxP = 3;
-static constexpr int kMaxBox = 15 * 15 * 15;  // sum over classes of the box sizes, p = 3
+// coefficient table: per class, wy*wz rows of the x box padded to a multiple of 4 floats
+// (128-bit shared-memory loads); p = 3: (8 + 4 + 4) * 15 * 15 = 3600 floats
+static constexpr int kMaxBox = 16 * 15 * 15;
 static constexpr int kMaxCls = 27;
 
 struct BatchProb {
@@ -138,8 +140,8 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 struct BatchSmem {
-  float sh[kMaxBox], sl[kMaxBox];
-  int off[kMaxBox];
+  __align__(16) float sh[kMaxBox];
+  __align__(16) float sl[kMaxBox];
   int base[kMaxCls], cnt[kMaxCls];
   int blo[kMaxCls][3], bw[kMaxCls][3];
   float dinv[kMaxCls];
@@ -311,14 +313,29 @@ __device__ __forceinline__ void period_apply32(const BatchSmem& sm, const float*
 #pragma unroll
       for (int t = PO + 1; t <= 2 * PO; ++t) win[t] = full ? v[base + t] : 0.f;
       const int row = yy + wy * zz;
-      const float* S0 = sm.sh + sm.base[c0] + (2 * PO + 1) * row;
+      constexpr int R0 = (2 * PO + 1 + 3) & ~3, RK = (PO + 1 + 3) & ~3;
+      {
+        const float4* S0 = reinterpret_cast<const float4*>(sm.sh + sm.base[c0] + R0 * row);
 #pragma unroll
-      for (int t = 0; t <= 2 * PO; ++t) acc[0] = fmaf(S0[t], win[t], acc[0]);
+        for (int v4 = 0; v4 < R0 / 4; ++v4) {
+          const float4 c = S0[v4];
+          const float cc[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (4 * v4 + e <= 2 * PO) acc[0] = fmaf(cc[e], win[4 * v4 + e], acc[0]);
+        }
+      }
 #pragma unroll
       for (int k = 1; k < PO; ++k) {
-        const float* Sk = sm.sh + sm.base[c0 + k] + (PO + 1) * row;
+        const float4* Sk = reinterpret_cast<const float4*>(sm.sh + sm.base[c0 + k] + RK * row);
 #pragma unroll
-        for (int t = 0; t <= PO; ++t) acc[k] = fmaf(Sk[t], win[t], acc[k]);
+        for (int v4 = 0; v4 < RK / 4; ++v4) {
+          const float4 c = Sk[v4];
+          const float cc[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (4 * v4 + e <= PO) acc[k] = fmaf(cc[e], win[4 * v4 + e], acc[k]);
+        }
       }
     }
 }
@@ -351,12 +368,13 @@ __device__ __forceinline__ void period_apply_ff(const BatchSmem& sm, const float
         wl[t] = full ? vl[base + t] : 0.f;
       }
       const int row = yy + wy * zz;
-      const int b0 = sm.base[c0] + (2 * PO + 1) * row;
+      constexpr int R0 = (2 * PO + 1 + 3) & ~3, RK = (PO + 1 + 3) & ~3;
+      const int b0 = sm.base[c0] + R0 * row;
 #pragma unroll
       for (int t = 0; t <= 2 * PO; ++t) ff_fma_acc(sm.sh[b0 + t], sm.sl[b0 + t], wh[t], wl[t], ah[0], al[0]);
 #pragma unroll
       for (int k = 1; k < PO; ++k) {
-        const int bk = sm.base[c0 + k] + (PO + 1) * row;
+        const int bk = sm.base[c0 + k] + RK * row;
 #pragma unroll
         for (int t = 0; t <= PO; ++t) ff_fma_acc(sm.sh[bk + t], sm.sl[bk + t], wh[t], wl[t], ah[k], al[k]);
       }
@@ -428,11 +446,6 @@ __device__ void solve_problem(const BatchArgs& a, int prob, int rank, BatchSmem&
     sm.sh[t] = T.sh[t];
     sm.sl[t] = T.sl[t];
   }
-  for (int c = 0; c < T.ncls; ++c)
-    for (int t = threadIdx.x; t < T.cnt[c]; t += blockDim.x) {
-      int ax = t % T.w[c][0], by = (t / T.w[c][0]) % T.w[c][1], cz = t / (T.w[c][0] * T.w[c][1]);
-      sm.off[T.base[c] + t] = (ax + T.lo[c][0]) + L * (by + T.lo[c][1]) + (int)L2 * (cz + T.lo[c][2]);
-    }
   for (int t = threadIdx.x; t < NP1 * NP1; t += blockDim.x) sm.mw[t] = T.mw[t];
   __syncthreads();
   float* bh = a.vpool + P.voff;
@@ -555,7 +568,6 @@ __device__ void solve_problem(const BatchArgs& a, int prob, int rank, BatchSmem&
     if (rr <= (double)a.delta * (double)a.delta * rtrue2 || near || it >= a.max_iters) {
       // reliable update: x += xc (float-float), then r = b - A x in float-float
       for (NodeWalk w((int)u0, (int)u1, F, L); w.ok(); w.next()) {
-        const int I = w.I, J = w.J, K = w.K;
         const int64_t g = w.g;
         float h, l;
         ff_add(xh[g], xl[g], xc[g], 0.f, h, l);
@@ -612,7 +624,6 @@ __device__ void solve_problem(const BatchArgs& a, int prob, int rank, BatchSmem&
   }
   // solution: x = xh + xl at the interior nodes, x fastest
   for (NodeWalk w((int)u0, (int)u1, F, L); w.ok(); w.next()) {
-    const int I = w.I, J = w.J, K = w.K;
     const int64_t g = w.g;
     P.x[w.u] = (double)xh[g] + (double)xl[g];
   }
@@ -624,7 +635,7 @@ __device__ void solve_problem(const BatchArgs& a, int prob, int rank, BatchSmem&
   }
 }
 
-__global__ void __launch_bounds__(512) k_batch_solve(BatchArgs a) {
+__global__ void __launch_bounds__(512, 2) k_batch_solve(BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   BatchSmem& sm = *reinterpret_cast<BatchSmem*>(smraw);
   for (int j = a.job_ptr[blockIdx.x]; j < a.job_ptr[blockIdx.x + 1]; ++j) {
@@ -702,14 +713,15 @@ static void build_order_tables(int p, OrderTables& T) {
         T.w[c][0] = w1[cx];
         T.w[c][1] = w1[cy];
         T.w[c][2] = w1[cz];
-        T.cnt[c] = w1[cx] * w1[cy] * w1[cz];
+        const int rw = (w1[cx] + 3) & ~3;  // padded row
+        T.cnt[c] = rw * w1[cy] * w1[cz];
         for (int k = 0; k < w1[cz]; ++k)
           for (int j = 0; j < w1[cy]; ++j)
             for (int i = 0; i < w1[cx]; ++i) {
               double v = S1[cx][i] * M1[cy][j] * M1[cz][k] + M1[cx][i] * S1[cy][j] * M1[cz][k] +
                          M1[cx][i] * M1[cy][j] * S1[cz][k];
               float h = (float)v;
-              int t = base + i + w1[cx] * (j + w1[cy] * k);
+              int t = base + i + rw * (j + w1[cy] * k);
               T.sh[t] = h;
               T.sl[t] = (float)(v - (double)h);
               if (lo1[cx] + i == 0 && lo1[cy] + j == 0 && lo1[cz] + k == 0) T.dg[c] = h;
