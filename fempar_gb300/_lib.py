@@ -34,7 +34,7 @@ EXPORTS = [
     "fg_assemble", "fg_system_reassemble", "fg_system_destroy",
     "fg_system_export_csr", "fg_system_export_rhs", "fg_system_export_dirichlet_values",
     "fg_system_spmv_device", "fg_system_spmv_device_noalloc", "fg_system_spmv_solver_layout_device",
-    "fg_solve", "fg_solve_device",
+    "fg_solve", "fg_solve_device", "fg_system_error_norms",
     "fg_solver_params_default", "fg_integrand_default",
     "fg_bddc_params_default", "fg_bddc_create", "fg_bddc_numerical_setup", "fg_bddc_get_info",
     "fg_bddc_apply_device", "fg_bddc_solve", "fg_bddc_solve_device", "fg_bddc_destroy",
@@ -93,6 +93,11 @@ class SpaceInfo(C.Structure):
         ("nnz_full", C.c_int64), ("nnz_upper", C.c_int64), ("solver_vec_len", C.c_int64),
         ("solver_entries", C.c_int64), ("solver_layout", C.c_int32),
     ]
+
+
+class ErrorNorms(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("mean_norm", "l1_norm", "l2_norm", "linfty_norm", "h1_seminorm",
+                                          "h1_norm", "w1infty_seminorm", "w1infty_norm", "energy_norm")]
 
 
 class BddcParams(C.Structure):
@@ -245,6 +250,7 @@ def lib():
         "fg_server_stats": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
         "fg_server_destroy": (i32, [vp]),
         "fg_integrand_default": (None, [C.POINTER(Integrand)]),
+        "fg_system_error_norms": (i32, [vp, vp, i32, i32, vp, vp, C.POINTER(ErrorNorms)]),
         "fg_bddc_params_default": (None, [C.POINTER(BddcParams)]),
         "fg_bddc_create": (i32, [vp, C.POINTER(BddcParams), pp]),
         "fg_bddc_numerical_setup": (i32, [vp]),

@@ -257,6 +257,26 @@ class FEAffineOperator:
                 "fg_system_spmv_solver_layout_device")
         return y_slot
 
+    def error_norms(self, x, exact_fn=L.FG_FN_ZERO, fn_param=(), cell_sq_energy=False):
+        """Norms of u - u_h for the solution x (numpy, num_free_dofs, or a torch CUDA tensor)
+        against the analytic exact_fn (error_norms_scalar_t%compute for every scalar norm
+        type, plus the tutorial's energy norm).  Returns a dict (and the per-cell squared
+        energy errors if cell_sq_energy)."""
+        n = self.space.num_free_dofs
+        on_dev = hasattr(x, "data_ptr")
+        if not on_dev:
+            x = np.ascontiguousarray(x, dtype=np.float64)
+        if (x.numel() if on_dev else x.size) != n:
+            raise ValueError("x must have num_free_dofs entries")
+        prm = np.zeros(8)
+        prm[:len(fn_param)] = fn_param
+        cells = np.zeros(self.space.num_cells) if cell_sq_energy else None
+        out = L.ErrorNorms()
+        L.check(L.lib().fg_system_error_norms(self.h, _ptr(x), int(on_dev), int(exact_fn), _ptr(prm), _ptr(cells),
+                                              C.byref(out)), "fg_system_error_norms")
+        d = {k: getattr(out, k) for k, _ in L.ErrorNorms._fields_}
+        return (d, cells) if cell_sq_energy else d
+
     def close(self):
         if getattr(self, "h", None):
             L.lib().fg_system_destroy(self.h)

@@ -224,6 +224,21 @@ fg_status fg_solve(fg_system* sys, const fg_solver_params* params, const double*
 fg_status fg_solve_device(fg_system* sys, const fg_solver_params* params, const double* b_dev,
                           const double* x0_dev, double* x_dev, fg_solve_info* info);
 
+/* Norms of the error u - u_h of a discrete solution (free-dof values x, num_free entries;
+ * Dirichlet dofs take the system's fixed values) against an analytic u = FG_FN_* with
+ * fn_param, per cell at the Gauss points and summed over the cells.  Replaces
+ * error_norms_scalar_t%compute for the scalar norms (Sources/Lib/Integration/ErrorNorms/
+ * sbm_error_norms_scalar.i90:67-241, finalize_norm error_norms.f90:174-221) and the
+ * tutorial's energy-norm error estimator (tutorial_01 modules :542-679: cell_sq_energy,
+ * nullable host array of num_cells values sum_q k |grad e|^2 |det J| w).  Scalar fields. */
+typedef struct {
+  double mean_norm, l1_norm, l2_norm, linfty_norm;
+  double h1_seminorm, h1_norm, w1infty_seminorm, w1infty_norm;
+  double energy_norm;     /* sqrt(sum_K k_K |grad e|^2_K) (k = 1: the tutorial's estimator) */
+} fg_error_norms;
+fg_status fg_system_error_norms(fg_system* sys, const double* x, int32_t x_on_device, int32_t fn,
+                                const double* fn_param, double* cell_sq_energy, fg_error_norms* out);
+
 /* ---------------------------------------------------------------------------------------
  * BDDC preconditioner (two levels: box subdomains of cells and a coarse problem).
  * Replaces mlbddc_t (Sources/Lib/LinearAlgebra/Preconditioner/mlbddc.f90,

@@ -953,6 +953,55 @@ double orc_energy_error(const orc_problem* h, const double* x) {
   return std::sqrt(total);
 }
 
+// error_norms_scalar_compute_cell_contribution (sbm_error_norms_scalar.i90:115-241):
+// e = exact - u_h at the Gauss points; cells summed in order (update_norm, error_norms.f90:160-172).
+// out: mean, l1, l2^2, linfty, |grad e|^2, w1infty (before finalize_norm)
+void orc_error_norms(const orc_problem* h, const double* x, int fn, const double* prm, double* out) {
+  const int nd = h->nd, nq = h->nq;
+  double mean = 0.0, l1 = 0.0, l2 = 0.0, linf = 0.0, h1 = 0.0, w1 = 0.0;
+  std::vector<double> invj, det, xq;
+  for (int64_t c = 0; c < h->ncells; ++c) {
+    cell_geometry(*h, c, invj, det, xq);
+    double cm = 0.0, cl1 = 0.0, cl2 = 0.0, cli = 0.0, ch1 = 0.0, cw1 = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      double uh = 0.0, gh[3] = {0, 0, 0};
+      for (int s = 0; s < nd; ++s) {
+        int32_t g = h->gids[(size_t)c * nd + s];
+        double u = g > 0 ? x[g - 1] : h->gvals[-g - 1];
+        uh = uh + u * h->shp[(size_t)s * nq + q];
+        for (int i = 0; i < 3; ++i) {
+          double acc = 0.0;
+          for (int j = 0; j < 3; ++j) acc = acc + invj[q * 9 + j + 3 * i] * h->shg[((size_t)s * nq + q) * 3 + j];
+          gh[i] = gh[i] + u * acc;
+        }
+      }
+      double e = fn_value(fn, prm, h->dim, &xq[q * 3]) - uh;
+      double ge[3];
+      fn_gradient(fn, prm, h->dim, &xq[q * 3], ge);
+      double factor = det[q] * h->qw[q];
+      double e0 = ge[0] - gh[0], e1 = ge[1] - gh[1], e2 = ge[2] - gh[2];
+      cm = cm + e * factor;
+      cl1 = cl1 + std::fabs(e) * factor;
+      cl2 = cl2 + (e * e) * factor;
+      cli = std::max(cli, std::fabs(e));
+      ch1 = ch1 + (e0 * e0 + e1 * e1 + e2 * e2) * factor;
+      cw1 = std::max(cw1, std::max(std::fabs(e0), std::max(std::fabs(e1), std::fabs(e2))));
+    }
+    mean += cm;
+    l1 += cl1;
+    l2 += cl2;
+    linf = std::max(linf, cli);
+    h1 += ch1;
+    w1 = std::max(w1, cw1);
+  }
+  out[0] = mean;
+  out[1] = l1;
+  out[2] = l2;
+  out[3] = linf;
+  out[4] = h1;
+  out[5] = w1;
+}
+
 void orc_gauss_legendre(int n, double* x, double* w) { gauss_legendre(n, x, w); }
 
 int orc_own_dofs(int num_dims, int order, int ncomp, int iface, int32_t* out) {

@@ -112,6 +112,9 @@ void orc_spmv(const orc_problem* h, const double* x, double* y);
 /* Energy-norm true error sqrt(sum_K int_K |grad(u - u_h)|^2) for the analytic solution of
  * boundary_fn (sharp wave or linear), u_h given by free values x and the Dirichlet values. */
 double orc_energy_error(const orc_problem* h, const double* x);
+/* Scalar error norms of x against the analytic fn (sbm_error_norms_scalar.i90:115-241),
+ * before finalize_norm: out = mean, l1, l2^2, linfty, |grad e|^2, w1infty. */
+void orc_error_norms(const orc_problem* h, const double* x, int fn, const double* prm, double* out);
 
 /* Gauss-Legendre nodes/weights on [-1,1] (n points). */
 void orc_gauss_legendre(int n, double* x, double* w);

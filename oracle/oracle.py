@@ -85,6 +85,8 @@ def lib():
         L.orc_spmv.argtypes = [vp, vp, vp]
         L.orc_energy_error.restype = dbl
         L.orc_energy_error.argtypes = [vp, vp]
+        L.orc_error_norms.restype = None
+        L.orc_error_norms.argtypes = [vp, vp, C.c_int, vp, vp]
         L.orc_gauss_legendre.argtypes = [i32, vp, vp]
         L.orc_own_dofs.restype = i32
         L.orc_own_dofs.argtypes = [i32, i32, i32, i32, vp]
@@ -230,6 +232,17 @@ class Problem:
         if history:
             out["history"] = hist[: it.value]
         return out
+
+    def error_norms(self, x, fn, fn_param=()):
+        """mean, l1, l2, linfty, h1_seminorm, h1, w1infty_seminorm, w1infty (finalised)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        prm = np.zeros(8)
+        prm[:len(fn_param)] = fn_param
+        o = np.zeros(6)
+        lib().orc_error_norms(self.h, _ptr(x), int(fn), _ptr(prm), _ptr(o))
+        return {"mean_norm": o[0], "l1_norm": o[1], "l2_norm": np.sqrt(o[2]), "linfty_norm": o[3],
+                "h1_seminorm": np.sqrt(o[4]), "h1_norm": np.sqrt(o[2] + o[4]), "w1infty_seminorm": o[5],
+                "w1infty_norm": o[3] + o[5]}
 
     def energy_error(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
