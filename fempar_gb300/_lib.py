@@ -18,7 +18,7 @@ FG_ERR_NOT_CONVERGED = -4
 
 FG_POISSON, FG_ELASTICITY = 0, 1
 FG_FN_ZERO, FG_FN_CONST, FG_FN_SHARP_WAVE, FG_FN_LINEAR, FG_FN_QP_VALUES = 0, 1, 2, 3, 4
-FG_INPUTS_ON_DEVICE = 1
+FG_INPUTS_ON_DEVICE, FG_LEAN_SYSTEM = 1, 2
 FG_PREC_NONE, FG_PREC_JACOBI, FG_PREC_BDDC = 0, 1, 2
 FG_BDDC_WEIGHT_MULTIPLICITY, FG_BDDC_WEIGHT_STIFFNESS = 0, 1
 FG_FP64, FG_MIXED = 0, 1
@@ -29,7 +29,7 @@ EXPORTS = [
     "fg_status_string", "fg_last_error", "fg_version",
     "fg_ctx_create", "fg_ctx_destroy", "fg_ctx_memory", "fg_ctx_get_stream", "fg_ctx_kernel_launches",
     "fg_mesh_create_structured", "fg_mesh_destroy",
-    "fg_space_create", "fg_space_destroy", "fg_space_get_info", "fg_space_get_dof_map",
+    "fg_space_create", "fg_space_destroy", "fg_space_release_pattern", "fg_space_get_info", "fg_space_get_dof_map",
     "fg_space_get_dirichlet_coords",
     "fg_assemble", "fg_system_reassemble", "fg_system_destroy",
     "fg_system_export_csr", "fg_system_export_rhs", "fg_system_export_dirichlet_values",
@@ -227,6 +227,7 @@ def lib():
         "fg_mesh_destroy": (i32, [vp]),
         "fg_space_create": (i32, [vp, i32, i32, vp, i32, pp]),
         "fg_space_destroy": (i32, [vp]),
+        "fg_space_release_pattern": (i32, [vp]),
         "fg_space_get_info": (i32, [vp, C.POINTER(SpaceInfo)]),
         "fg_space_get_dof_map": (i32, [vp, vp]),
         "fg_space_get_dirichlet_coords": (i32, [vp, vp]),

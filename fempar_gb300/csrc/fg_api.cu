@@ -318,6 +318,18 @@ fg_status fg_space_destroy(fg_space* sp) {
   return FG_OK;
 }
 
+fg_status fg_space_release_pattern(fg_space* sp) {
+  FG_CHECK_ARG(sp, "space");
+  fg_ctx* ctx = sp->mesh->ctx;
+  FG_DEVICE_GUARD(ctx);
+  FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, sp->d_rowptr);
+  dev_free(ctx, sp->d_col);
+  sp->d_rowptr = nullptr;
+  sp->d_col = nullptr;
+  return FG_OK;
+}
+
 fg_status fg_space_get_info(fg_space* sp, fg_space_info* info) {
   FG_CHECK_ARG(sp && info, "space/info");
   info->num_dims = 3;
@@ -395,6 +407,19 @@ static fg_status numeric_phase(fg_system* sys, const fg_integrand* g) {
     FG_TRY(system_interpolate_dirichlet(sys, g->boundary_fn, g->fn_param));
   }
   FG_TRY(system_assemble(sys));
+  if (sys->lean) {
+    // element matrices are scratch of the scatter: release them before the solver layout
+    dev_free(ctx, sys->d_elmat);
+    dev_free(ctx, sys->d_elvec);
+    sys->d_elmat = sys->d_elvec = nullptr;
+    if (sp->layout == FG_LAYOUT_SELL) {
+      FG_TRY(dev_alloc(ctx, (void**)&sys->d_sval, sizeof(double) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1)));
+      FG_TRY(dev_alloc(ctx, (void**)&sys->d_sval32, sizeof(float) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1)));
+    } else {
+      FG_TRY(dev_alloc(ctx, (void**)&sys->d_tval, sizeof(double) * (sp->st_nvals > 0 ? sp->st_nvals : 1)));
+      FG_TRY(dev_alloc(ctx, (void**)&sys->d_tval32, sizeof(float) * (sp->st_nvals > 0 ? sp->st_nvals : 1)));
+    }
+  }
   if (sp->layout == FG_LAYOUT_SELL) FG_TRY(system_fill_sell(sys));
   else FG_TRY(system_fill_stencil(sys));
   FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -406,13 +431,20 @@ fg_status fg_assemble(fg_space* sp, const fg_integrand* g, fg_system** out) {
   *out = nullptr;
   fg_ctx* ctx = sp->mesh->ctx;
   FG_DEVICE_GUARD(ctx);
+  if (!sp->d_rowptr || !sp->d_col) {
+    set_error("the space's sparsity pattern was released");
+    return FG_ERR_UNSUPPORTED;
+  }
   fg_system* sys = new fg_system();
   sys->space = sp;
+  sys->lean = (g->flags & FG_LEAN_SYSTEM) != 0;
   const int64_t ncells = sp->mesh->ncells, nd = sp->tab.nd;
   fg_status s = FG_OK;
   auto A = [&](void** p, size_t b) { if (s == FG_OK) s = dev_alloc(ctx, p, b); };
   A((void**)&sys->d_val, sizeof(double) * (sp->nnz > 0 ? sp->nnz : 1));
-  if (sp->layout == FG_LAYOUT_SELL) {
+  if (sys->lean) {
+    // solver-layout arrays are allocated after the element matrices are released
+  } else if (sp->layout == FG_LAYOUT_SELL) {
     A((void**)&sys->d_sval, sizeof(double) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1));
     A((void**)&sys->d_sval32, sizeof(float) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1));
   } else {
@@ -429,6 +461,10 @@ fg_status fg_assemble(fg_space* sp, const fg_integrand* g, fg_system** out) {
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) { set_error("assemble: %s", cudaGetErrorString(e)); s = FG_ERR_CUDA; }
   }
+  if (s == FG_OK && sys->lean) {
+    dev_free(ctx, sys->d_val);
+    sys->d_val = nullptr;
+  }
   if (s != FG_OK) {
     system_free(sys);
     return s;
@@ -439,6 +475,10 @@ fg_status fg_assemble(fg_space* sp, const fg_integrand* g, fg_system** out) {
 
 fg_status fg_system_reassemble(fg_system* sys, const fg_integrand* g) {
   FG_CHECK_ARG(sys && g, "system/integrand");
+  if (sys->lean) {
+    set_error("the system was assembled lean (FG_LEAN_SYSTEM): reassembly needs a full system");
+    return FG_ERR_UNSUPPORTED;
+  }
   FG_DEVICE_GUARD(sys->space->mesh->ctx);
   FG_TRY(numeric_phase(sys, g));
   FG_TRY(system_prepare_diag(sys));
@@ -460,6 +500,10 @@ fg_status fg_system_export_csr(fg_system* sys, int symmetric_storage, int one_ba
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
   FG_DEVICE_GUARD(ctx);
+  if (!sys->d_val || !sp->d_rowptr || !sp->d_col) {
+    set_error("the CSR of this system was released (FG_LEAN_SYSTEM / fg_space_release_pattern)");
+    return FG_ERR_UNSUPPORTED;
+  }
   one_based = one_based ? 1 : 0;
   if (symmetric_storage) return space_export_upper(sp, sys->d_val, one_based, irp, ja, val);
   const int64_t n = sp->nfree;

@@ -160,6 +160,7 @@ struct fg_system {
   unsigned int* d_ticket = nullptr;
   int red_blocks = 0;
   fg_integrand integ;             // last integrand (host copy of scalars)
+  bool lean = false;              // FG_LEAN_SYSTEM: element matrices and CSR values released
 };
 
 namespace fg {

@@ -118,10 +118,13 @@ static fg_status footprint(const fg_request* q, uint64_t* bytes, int64_t* nfree_
   const double nnz = (double)nfree * box_d * box_d * box_d * ncomp;
   const double nd = (double)t.nd;
   const double nvec = std::pow((double)p * std::max({q->n[0], q->n[1], q->n[2]}) + 1.0 + 3.0 * p, 3.0) * ncomp;
-  double b = 0;
-  b += ncells * nd * nd * 8 + ncells * nd * 8;      // element matrices and vectors
-  b += nnz * (4 + 8) + nfree * 8.0;                 // CSR pattern + FP64 values + row pointers
-  b += nnz * 1.15 * (8 + 4);                        // solver layout FP64 + FP32 (padding)
+  // requests are assembled lean (FG_LEAN_SYSTEM): the element matrices are released before
+  // the solver layout is allocated, the CSR after it is filled, so the peak is the larger of
+  // (element matrices + CSR) and (CSR + solver layout), plus what lives throughout
+  const double elm = ncells * nd * nd * 8 + ncells * nd * 8;  // element matrices and vectors
+  const double csr = nnz * (4 + 8) + nfree * 8.0;             // CSR pattern + FP64 values + row pointers
+  const double lay = nnz * 1.15 * (8 + 4);                    // solver layout FP64 + FP32 (padding)
+  double b = std::max(elm, lay) + csr;
   b += nvec * (6 * 8 + 4 * 4 + 12);                 // solver vectors + Jacobi
   b += nlat * ncomp * (4 + 14) + nfree * 12.0;      // dof maps + symbolic-phase temporaries
   b += (double)(q->n[0] + 1) * (q->n[1] + 1) * (q->n[2] + 1) * 24 + ncells * 8;
@@ -149,7 +152,9 @@ static void run_request(fg_ctx* ctx, Request* R) {
     g.nu = R->r.nu;
     g.source_fn = R->r.source_fn;
     for (int i = 0; i < 8; ++i) g.fn_param[i] = R->r.fn_param[i];
+    g.flags = FG_LEAN_SYSTEM;
     s = fg_assemble(sp, &g, &sys);
+    if (s == FG_OK) s = fg_space_release_pattern(sp);
   }
   fg_solve_info info;
   std::memset(&info, 0, sizeof(info));

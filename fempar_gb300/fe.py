@@ -117,6 +117,10 @@ class SerialFESpace:
         self.qp_per_cell = info.qp_per_cell
         self.num_cells = info.num_cells
 
+    def release_pattern(self):
+        """Free the CSR pattern after lean assembly (fg_space_release_pattern)."""
+        L.check(L.lib().fg_space_release_pattern(self.h), "fg_space_release_pattern")
+
     def get_dof_map(self):
         """lst_dofs_gids, shape (ncells, dofs_per_cell), reference convention."""
         out = np.zeros(self.num_cells * self.dofs_per_cell, dtype=np.int32)
@@ -197,13 +201,17 @@ def ElasticityIntegration(**kw):
 class FEAffineOperator:
     """fe_affine_operator_t: integrate + assemble into CSR (+FP32 copy) and rhs on the device."""
 
-    def __init__(self, space: SerialFESpace, integration: DiscreteIntegration):
+    def __init__(self, space: SerialFESpace, integration: DiscreteIntegration, lean: bool = False):
+        """lean: keep only what a solve needs (FG_LEAN_SYSTEM; no export / reassembly / BDDC)."""
         self.space = space
         self.integration = integration
+        self.lean = lean
         self.h = None
 
     def compute(self):
         g, keep = self.integration.to_c()
+        if self.lean:
+            g.flags |= L.FG_LEAN_SYSTEM
         if self.h is None:
             h = C.c_void_p()
             L.check(L.lib().fg_assemble(self.space.h, C.byref(g), C.byref(h)), "fg_assemble")

@@ -56,8 +56,13 @@ enum {
   FG_FN_QP_VALUES = 4     /* source given at quadrature points: ncells*nq*ncomp     */
 };
 
-/* Input-location flag of fg_integrand.flags. */
-enum { FG_INPUTS_ON_DEVICE = 1 };
+/* Flags of fg_integrand.flags.  FG_INPUTS_ON_DEVICE: the arrays are device pointers.
+ * FG_LEAN_SYSTEM (fg_assemble only): keep only what a solve needs — the element matrices
+ * are freed right after the scatter (before the solver layout is allocated) and the CSR
+ * values after the solver layout and the Jacobi diagonal are filled; export, reassembly and
+ * BDDC on such a system return FG_ERR_UNSUPPORTED.  Peak device memory of an assembly drops
+ * from elmat + CSR + layout to max(elmat + CSR, CSR + layout). */
+enum { FG_INPUTS_ON_DEVICE = 1, FG_LEAN_SYSTEM = 2 };
 
 typedef struct {
   int kind;                        /* FG_POISSON / FG_ELASTICITY                     */
@@ -149,6 +154,10 @@ fg_status fg_mesh_destroy(fg_mesh* mesh);
 fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* dirichlet_ids, int n_ids,
                           fg_space** out);
 fg_status fg_space_destroy(fg_space* space);
+/* Free the space's CSR pattern (row pointers and column indices) once its systems are
+ * assembled lean (FG_LEAN_SYSTEM): solves keep working, further assemblies and exports
+ * return FG_ERR_UNSUPPORTED.  No counterpart in the reference (serving memory control). */
+fg_status fg_space_release_pattern(fg_space* space);
 fg_status fg_space_get_info(fg_space* space, fg_space_info* info);
 /* lst_dofs_gids: ncells*dofs_per_cell int32 in the reference's cell-local dof order
  * (fe_space.f90:636-637). */

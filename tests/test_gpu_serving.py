@@ -74,3 +74,35 @@ def test_budget_refuses_oversized_request(S):
     with pytest.raises(FGError):
         srv.submit(kind=S.POISSON, n=(40, 40, 40), order=2)
     srv.close()
+
+
+def test_lean_system_solves_identically_and_refuses_exports(S):
+    """FG_LEAN_SYSTEM (what served requests use): same solution bits as a full system,
+    smaller resident memory, export and reassembly refused."""
+    import numpy as np
+    import fempar_gb300 as fg
+    from fempar_gb300 import FGError
+    ctx = fg.Context(0)
+    n = (10, 9, 8)
+    k = np.exp(np.random.default_rng(4).normal(size=n[0] * n[1] * n[2]))
+    xs, mem = [], []
+    for lean in (False, True):
+        tri = fg.SerialTriangulation(ctx, n)
+        sp = fg.SerialFESpace(tri, order=2, dirichlet_ids=list(range(1, 27)))
+        op = fg.FEAffineOperator(sp, fg.PoissonIntegration(cell_coef=k, source_fn=fg.FG_FN_CONST, fn_param=[1.0]),
+                                 lean=lean).compute()
+        if lean:
+            sp.release_pattern()
+            with pytest.raises(FGError):
+                op.get_matrix()
+            with pytest.raises(FGError):
+                op.compute()
+        mem.append(ctx.memory()[0])
+        s = fg.IterativeLinearSolver().set_type_from_string("GPU_MPCG").set_operators(op, "jacobi")
+        s.set_parameters_from_pl({"ILS_RTOL": 1e-8, "ILS_MAX_NUM_ITERATIONS": 10000})
+        xs.append(s.solve())
+        op.close()
+        sp.close()
+        tri.close()
+    assert np.array_equal(xs[0], xs[1])
+    assert mem[1] < 0.7 * mem[0]
