@@ -18,7 +18,7 @@ FG_ERR_NOT_CONVERGED = -4
 
 FG_POISSON, FG_ELASTICITY = 0, 1
 FG_FN_ZERO, FG_FN_CONST, FG_FN_SHARP_WAVE, FG_FN_LINEAR, FG_FN_QP_VALUES = 0, 1, 2, 3, 4
-FG_INPUTS_ON_DEVICE, FG_LEAN_SYSTEM = 1, 2
+FG_INPUTS_ON_DEVICE, FG_LEAN_SYSTEM, FG_FAST_INTEGRATION = 1, 2, 4
 FG_PREC_NONE, FG_PREC_JACOBI, FG_PREC_BDDC = 0, 1, 2
 FG_BDDC_WEIGHT_MULTIPLICITY, FG_BDDC_WEIGHT_STIFFNESS = 0, 1
 FG_FP64, FG_MIXED = 0, 1

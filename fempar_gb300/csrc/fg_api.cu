@@ -234,6 +234,7 @@ fg_status fg_mesh_destroy(fg_mesh* m) {
 static void space_free(fg_space* sp) {
   fg_ctx* ctx = sp->mesh->ctx;
   dev_free(ctx, sp->dtab.base);
+  dev_free(ctx, sp->dtab.fbase);
   dev_free(ctx, sp->d_latdof);
   dev_free(ctx, sp->d_free2lat);
   dev_free(ctx, sp->d_dir2lat);

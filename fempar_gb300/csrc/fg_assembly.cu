@@ -106,7 +106,33 @@ __device__ __forceinline__ void pair_ab(int p, int nd, int& a, int& b) {
   b = row + (p - off);
 }
 
-template <int P>
+// float-float helpers: values carried as hi + lo (FP32 pair), products error-free via fmaf
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void ff_renorm(float& h, float& l) {
+  float s = h + l;
+  l = l - (s - h);
+  h = s;
+}
+// (sh, sl) += (ah, al) * (bh, bl)
+__device__ __forceinline__ void ff_fma(float ah, float al, float bh, float bl, float& sh, float& sl) {
+  float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, fmaf(al, bh, e));
+  float s, t;
+  ff_two_sum(sh, p, s, t);
+  sh = s;
+  sl += t + e;
+}
+__device__ __forceinline__ void ff_split(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
+template <int P, bool FF>
 __global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
     k_integrate_poisson(AsmGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
                         const int32_t* __restrict__ latdof, const double* __restrict__ gvals,
@@ -202,6 +228,83 @@ __global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
     sq[q] = sqrt(fac[q] * kc);  // |det J| w k > 0
   }
   __syncwarp();
+  if constexpr (FF) {
+    // float-float variant: J^-1 and sqrt(fk) as FP32 pairs (converted in place: the pairs
+    // take half the bytes of the doubles they replace), scaled gradients and the element
+    // matrix accumulated with error-free FP32 products
+    constexpr int NI = (NQ * 9 + 31) / 32, NS = (NQ + 31) / 32;
+    double tv[NI], ts[NS];
+#pragma unroll
+    for (int k = 0; k < NI; ++k) tv[k] = (lane + 32 * k < NQ * 9) ? invj[lane + 32 * k] : 0.0;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) ts[k] = (lane + 32 * k < NQ) ? sq[lane + 32 * k] : 0.0;
+    __syncwarp();
+    float* ivh = reinterpret_cast<float*>(invj);
+    float* ivl = ivh + NQ * 9;
+    float* sqh = reinterpret_cast<float*>(sq);
+    float* sql = sqh + NQ;
+#pragma unroll
+    for (int k = 0; k < NI; ++k)
+      if (lane + 32 * k < NQ * 9) ff_split(tv[k], ivh[lane + 32 * k], ivl[lane + 32 * k]);
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+      if (lane + 32 * k < NQ) ff_split(ts[k], sqh[lane + 32 * k], sql[lane + 32 * k]);
+    __syncwarp();
+    float* sgh = reinterpret_cast<float*>(sg);
+    float* sgl = sgh + NQ * NN * 3;
+    for (int idx = lane; idx < NQ * NN; idx += 32) {
+      const int q = idx / NN, a = idx % NN;
+      const int r = (a * NQ + q) * 3;
+      const float rh[3] = {tb.shgh[r], tb.shgh[r + 1], tb.shgh[r + 2]};
+      const float rl[3] = {tb.shgl[r], tb.shgl[r + 1], tb.shgl[r + 2]};
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        float th = 0.f, tl = 0.f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) ff_fma(ivh[q * 9 + j + 3 * i], ivl[q * 9 + j + 3 * i], rh[j], rl[j], th, tl);
+        ff_renorm(th, tl);
+        float gh = 0.f, gl = 0.f;
+        ff_fma(sqh[q], sql[q], th, tl, gh, gl);
+        ff_renorm(gh, gl);
+        sgh[idx * 3 + i] = gh;
+        sgl[idx * 3 + i] = gl;
+      }
+    }
+    __syncwarp();
+    for (int pbase = 0; pbase < S::NPAIR; pbase += 32 * S::CH) {
+      float ah[S::CH], al[S::CH];
+      int pa[S::CH], pb[S::CH];
+#pragma unroll
+      for (int t = 0; t < S::CH; ++t) {
+        ah[t] = 0.f;
+        al[t] = 0.f;
+        int p = pbase + lane + 32 * t;
+        if (p < S::NPAIR) pair_ab(p, ND, pa[t], pb[t]);
+        else { pa[t] = 0; pb[t] = 0; }
+      }
+      for (int q = 0; q < NQ; ++q) {
+        const float* gqh = sgh + q * NN * 3;
+        const float* gql = sgl + q * NN * 3;
+#pragma unroll
+        for (int t = 0; t < S::CH; ++t) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+            ff_fma(gqh[pb[t] * 3 + i], gql[pb[t] * 3 + i], gqh[pa[t] * 3 + i], gql[pa[t] * 3 + i], ah[t], al[t]);
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < S::CH; ++t) {
+        int p = pbase + lane + 32 * t;
+        if (p < S::NPAIR) {
+          ff_renorm(ah[t], al[t]);
+          const double v = (double)ah[t] + (double)al[t];
+          el[pa[t] * ND + pb[t]] = v;
+          el[pb[t] * ND + pa[t]] = v;
+        }
+      }
+    }
+    __syncwarp();
+  } else {
   // physical gradients scaled by sqrt(|det J| w k): s_a = sqrt(fk) J^-T grad_ref(phi_a), so an
   // element entry is sum_q s_a . s_b, 3 FP64 FMAs per Gauss point (FP64 is GB300's scarce pipe)
   for (int idx = lane; idx < NQ * NN; idx += 32) {
@@ -246,6 +349,7 @@ __global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
     }
   }
   __syncwarp();
+  }
   // element vector + Dirichlet lifting
   bool any_dir = false;
   for (int s = lane; s < ND; s += 32) any_dir |= gid[s] < 0;
@@ -380,16 +484,14 @@ static fg_status launch_poisson(fg_system* sys) {
   for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
   src.qp = sys->d_qpsrc;
   const size_t smem = S::SM_BYTES_WARP * S::WARPS;
-  static bool attr_set = false;
-  if (!attr_set) {
-    FG_CUDA_TRY(cudaFuncSetAttribute(k_integrate_poisson<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+  const bool ff = (sys->integ.flags & FG_FAST_INTEGRATION) != 0;
+  auto kern = ff ? k_integrate_poisson<P, true> : k_integrate_poisson<P, false>;
+  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const unsigned grid = nblk(ncells, S::WARPS);
   ctx->launches += sp->nfree > 0 ? 2 : 1;
-  k_integrate_poisson<P><<<grid, S::WARPS * 32, smem, ctx->stream>>>(
-      g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof, sys->d_gvals, sys->d_coef, sys->integ.coef_const, src,
-      sys->d_elmat, sys->d_elvec);
+  kern<<<grid, S::WARPS * 32, smem, ctx->stream>>>(g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof,
+                                                   sys->d_gvals, sys->d_coef, sys->integ.coef_const, src,
+                                                   sys->d_elmat, sys->d_elvec);
   FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
   if (n > 0) {

@@ -74,6 +74,10 @@ struct DevTables {
   const double* gshg;
   const double* gnod;
   size_t bytes = 0;
+  // reference gradients as float-float pairs (hi, lo), for the float-float integration
+  float* fbase = nullptr;
+  const float* shgh;
+  const float* shgl;
 };
 
 }  // namespace fg

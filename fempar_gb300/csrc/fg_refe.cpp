@@ -176,6 +176,21 @@ fg_status upload_tables(fg_ctx* ctx, const RefTables& t, DevTables& d) {
   d.gshp = d.base + ogshp;
   d.gshg = d.base + ogshg;
   d.gnod = d.base + ognod;
+  // float-float copy of the reference gradients: hi = (float)v, lo = (float)(v - hi)
+  const size_t ng = t.shg.size();
+  std::vector<float> f(2 * ng);
+  for (size_t i = 0; i < ng; ++i) {
+    float hi = (float)t.shg[i];
+    f[i] = hi;
+    f[ng + i] = (float)(t.shg[i] - (double)hi);
+  }
+  void* pf = nullptr;
+  FG_TRY(dev_alloc(ctx, &pf, f.size() * sizeof(float)));
+  d.fbase = (float*)pf;
+  FG_CUDA_TRY(cudaMemcpyAsync(d.fbase, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  d.shgh = d.fbase;
+  d.shgl = d.fbase + ng;
   return FG_OK;
 }
 

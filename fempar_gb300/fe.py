@@ -142,8 +142,11 @@ class DiscreteIntegration:
     """Description of discrete_integration_t%integrate_galerkin for the device kernels."""
 
     def __init__(self, kind=L.FG_POISSON, cell_coef=None, coef_const=1.0, nu=0.3, source_fn=L.FG_FN_ZERO,
-                 fn_param=(), qp_source=None, boundary_fn=L.FG_FN_ZERO, dirichlet_values=None):
+                 fn_param=(), qp_source=None, boundary_fn=L.FG_FN_ZERO, dirichlet_values=None,
+                 fast_integration=False):
+        """fast_integration: float-float element matrices (FG_FAST_INTEGRATION), for mixed solves."""
         self.kind = kind
+        self.fast_integration = fast_integration
         self.cell_coef = cell_coef
         self.coef_const = coef_const
         self.nu = nu
@@ -182,7 +185,7 @@ class DiscreteIntegration:
         g.qp_source = arr(self.qp_source)
         g.boundary_fn = self.boundary_fn
         g.dirichlet_values = arr(self.dirichlet_values)
-        g.flags = L.FG_INPUTS_ON_DEVICE if on_dev else 0
+        g.flags = (L.FG_INPUTS_ON_DEVICE if on_dev else 0) | (L.FG_FAST_INTEGRATION if self.fast_integration else 0)
         return g, keep
 
     @staticmethod

@@ -62,7 +62,12 @@ enum {
  * values after the solver layout and the Jacobi diagonal are filled; export, reassembly and
  * BDDC on such a system return FG_ERR_UNSUPPORTED.  Peak device memory of an assembly drops
  * from elmat + CSR + layout to max(elmat + CSR, CSR + layout). */
-enum { FG_INPUTS_ON_DEVICE = 1, FG_LEAN_SYSTEM = 2 };
+enum { FG_INPUTS_ON_DEVICE = 1, FG_LEAN_SYSTEM = 2, FG_FAST_INTEGRATION = 4 };
+/* FG_FAST_INTEGRATION (Poisson): element matrices accumulated in float-float (pairs of FP32
+ * with error-free products, ~2^-48 relative) instead of FP64 — several times faster on
+ * GB300, whose FP64 rate is ~1/70 of FP32; entries agree with the FP64 integration to
+ * ~1e-13 of the row scale.  Meant for FG_MIXED solves (the FP64 copy of the matrix then feeds
+ * the residual refinement); the default FP64 integration is the one with reference parity. */
 
 typedef struct {
   int kind;                        /* FG_POISSON / FG_ELASTICITY                     */

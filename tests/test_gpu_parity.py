@@ -318,3 +318,32 @@ def test_elasticity_q3_reported_unsupported(fg, ctx):
     sp = fg.SerialFESpace(tri, order=3, ncomp=3, dirichlet_ids=CLAMP)
     with pytest.raises(FGError):
         fg.FEAffineOperator(sp, fg.ElasticityIntegration(cell_coef=np.ones(8), nu=0.3)).compute()
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_fast_integration_matrix_and_mixed_solution(fg, ctx, order):
+    """FG_FAST_INTEGRATION (float-float element matrices): entries within 1e-12 of the
+    row scale of the FP64 integration (the reference-parity one), pattern identical, and the
+    mixed solve on it within 1e-9 of the FP64 drop-in's solution."""
+    n = (5, 4, 6)
+    xyz = perturbed_vertices(n, 0.15, seed=21)
+    k = np.exp(np.random.default_rng(2).normal(size=n[0] * n[1] * n[2]))
+    tri = fg.SerialTriangulation(ctx, n, vertex_xyz=xyz)
+    sp = fg.SerialFESpace(tri, order=order, dirichlet_ids=list(range(1, 27)))
+    sols, mats = [], []
+    for fast in (False, True):
+        op = fg.FEAffineOperator(sp, fg.PoissonIntegration(cell_coef=k, source_fn=O.FN_CONST, fn_param=[1.0],
+                                                           fast_integration=fast)).compute()
+        mats.append(op.get_matrix())
+        s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
+        s.set_parameters_from_pl({"ILS_RTOL": 1e-12, "ILS_MAX_NUM_ITERATIONS": 50000,
+                                  "PRECISION": "mixed" if fast else "fp64"})
+        sols.append(s.solve())
+        op.close()
+    (irp, ja, v64), (irp2, ja2, vff) = mats
+    assert np.array_equal(irp, irp2) and np.array_equal(ja, ja2)
+    rows = np.repeat(np.arange(len(irp) - 1), np.diff(irp))
+    scale = np.zeros(len(irp) - 1)
+    np.maximum.at(scale, rows, np.abs(v64))
+    assert (np.abs(vff - v64) / scale[rows]).max() <= 1e-12
+    assert np.linalg.norm(sols[1] - sols[0]) <= 1e-9 * np.linalg.norm(sols[0])
