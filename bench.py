@@ -175,6 +175,20 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def replica_aggregate(dist, times_ms, units, device="cpu"):
+    """Replicas (one independent problem per rank, no data-path collective): each timing
+    becomes the maximum over the ranks and the work the sum of every rank's units, so a
+    rate = units / max time.  dist = torch.distributed (initialised) or None for one rank."""
+    import torch
+    if dist is None:
+        return list(times_ms), units
+    t = torch.tensor(list(times_ms), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return [float(v) for v in t.tolist()], float(u.item())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -330,20 +344,13 @@ def main():
     fmt32 = 4 * nent + 8 * nvec + (0 if space.info.solver_layout == 0 else 4 * nent)
     fmt64 = 8 * nent + 16 * nvec + (0 if space.info.solver_layout == 0 else 4 * nent)
 
-    # ---- max over ranks ----
-    def maxr(v):
-        if not dist:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    ms_mx = maxr(statistics.mean(tmx))
-    ms_64 = maxr(statistics.mean(t64))
-    ms_e2e = maxr(statistics.mean(te2e))
-    value = world * nfree / (ms_mx * 1e-3)
-    v64 = world * nfree / (ms_64 * 1e-3)
-    ve2e = world * nfree / (ms_e2e * 1e-3)
+    # ---- replicas: slowest rank's time, every rank's dofs ----
+    dev = f"cuda:{local}"
+    (ms_mx, ms_64, ms_e2e), total = replica_aggregate(
+        dist, [statistics.mean(tmx), statistics.mean(t64), statistics.mean(te2e)], nfree, dev)
+    value = total / (ms_mx * 1e-3)
+    v64 = total / (ms_64 * 1e-3)
+    ve2e = total / (ms_e2e * 1e-3)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
