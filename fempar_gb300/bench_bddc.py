@@ -36,6 +36,37 @@ def perturbed_vertices(n, frac, rng):
     return xyz.ravel()
 
 
+def run_jacobi_only(n, rtol=1e-8, device=0, precisions=("mixed",)):
+    """The same elasticity problem with Jacobi-PCG only, assembled lean (fits 96^3 Q2, the
+    size at which dense subdomain factors do not fit)."""
+    rng = np.random.Generator(np.random.PCG64(SEED))
+    xyz = perturbed_vertices(n, 0.15, rng)
+    E = np.exp(rng.normal(0.0, 1.5, size=n ** 3))
+    ctx = Context(device)
+    t0 = time.perf_counter()
+    tri = SerialTriangulation(ctx, (n, n, n), vertex_xyz=xyz)
+    sp = SerialFESpace(tri, order=2, ncomp=3, dirichlet_ids=CLAMP_X0_IDS)
+    t_sym = (time.perf_counter() - t0) * 1e3
+    integ = ElasticityIntegration(cell_coef=E, nu=0.3, source_fn=L.FG_FN_CONST, fn_param=[0.0, 0.0, -1.0])
+    t0 = time.perf_counter()
+    op = FEAffineOperator(sp, integ, lean=True).compute()
+    t_asm = (time.perf_counter() - t0) * 1e3
+    out = {"metric": "elasticity Q2: DOF/s to 1e-8 (assembly + Jacobi-PCG)", "n": n, "dofs": sp.num_free_dofs,
+           "nnz_full": sp.info.nnz_full, "symbolic_ms": t_sym, "assembly_ms": t_asm,
+           "device_gb_after_assembly": ctx.memory()[0] / 1e9}
+    for prec in precisions:
+        s = IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
+        s.set_parameters_from_pl({"ILS_RTOL": rtol, "ILS_MAX_NUM_ITERATIONS": 400000, "PRECISION": prec})
+        s.solve()
+        inf = s.info()
+        total = t_asm + inf["solve_ms"]
+        out["jacobi_" + prec] = {"iterations": inf["iterations"], "outer_iterations": inf["outer_iterations"],
+                                 "converged": inf["converged"], "solve_ms": inf["solve_ms"], "step_ms": total,
+                                 "dof_per_s": sp.num_free_dofs / (total * 1e-3),
+                                 "ms_per_iteration": inf["solve_ms"] / max(inf["iterations"], 1)}
+    return out
+
+
 def run(n=32, nsub=8, jitter=0.0, rtol=1e-8, device=0, faces=False, weighting=L.FG_BDDC_WEIGHT_MULTIPLICITY,
         jacobi=True):
     rng = np.random.Generator(np.random.PCG64(SEED))
@@ -103,9 +134,14 @@ def main():
                     help="1/(subdomains around) weights (the reference's standard handler); "
                          "default: diag(A_i)/sum diag(A_j)")
     ap.add_argument("--no-jacobi", action="store_true")
+    ap.add_argument("--jacobi-only", action="store_true",
+                    help="no BDDC: lean assembly + mixed Jacobi-PCG (e.g. --n 96, the cfg size)")
     args = ap.parse_args()
     from . import build
     build.build()
+    if args.jacobi_only:
+        print(json.dumps(run_jacobi_only(args.n)), flush=True)
+        return
     wt = L.FG_BDDC_WEIGHT_MULTIPLICITY if args.multiplicity else L.FG_BDDC_WEIGHT_STIFFNESS
     print(json.dumps(run(args.n, args.nsub, args.jitter, faces=args.faces, weighting=wt,
                          jacobi=not args.no_jacobi)), flush=True)
