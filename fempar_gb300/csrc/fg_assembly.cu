@@ -711,11 +711,8 @@ static fg_status launch_elasticity(fg_system* sys) {
   for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
   src.qp = sys->d_qpsrc;
   const size_t smem = S::SM_BYTES_WARP * S::WARPS;
-  static bool attr_set = false;
-  if (!attr_set) {
-    FG_CUDA_TRY(cudaFuncSetAttribute(k_integrate_elasticity<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+  // per call: the attribute is per device, and server workers assemble concurrently
+  FG_CUDA_TRY(cudaFuncSetAttribute(k_integrate_elasticity<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   ctx->launches += sp->nfree > 0 ? 2 : 1;
   k_integrate_elasticity<P><<<nblk(ncells, S::WARPS), S::WARPS * 32, smem, ctx->stream>>>(
       g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof, sys->d_gvals, sys->d_coef, sys->integ.coef_const,
