@@ -1216,16 +1216,21 @@ static fg_status check_err(fg_bddc* B, const char* what) {
 }
 
 // Partial Cholesky of the first ncols columns of one N x N matrix, many CTAs per step.
-static fg_status chol_partial_grid(fg_ctx* ctx, double* A, int64_t lda, int N, int ncols, int* err) {
+// Rows from zrow on may be a unit block (row zrow + i holds a 1 in column i and zeros before
+// it, as in [[K, I], [I, 0]]): such a row's panel entries stay zero until the panel reaches
+// column i, so at panel j0 the rows from zrow + j0 + nb on are skipped by the solve and the
+// trailing update (exactly: their contributions are zero).  zrow = N: no unit block.
+static fg_status chol_partial_grid(fg_ctx* ctx, double* A, int64_t lda, int N, int ncols, int zrow, int* err) {
   cudaStream_t st = ctx->stream;
   for (int j0 = 0; j0 < ncols; j0 += 32) {
     const int nb = std::min(32, ncols - j0);
     k_chol_diag1<<<1, 32, 0, st>>>(A, lda, j0, nb, err);
-    const int rows = N - j0 - nb;
+    const int Neff = (int)std::min<int64_t>(N, (int64_t)zrow + j0 + nb);
+    const int rows = Neff - j0 - nb;
     if (rows > 0) {
-      k_chol_trsm1<<<nblk(rows, 256), 256, 0, st>>>(A, lda, N, j0, nb);
+      k_chol_trsm1<<<nblk(rows, 256), 256, 0, st>>>(A, lda, Neff, j0, nb);
       const int nt = (rows + 63) / 64;
-      k_chol_syrk1<<<(unsigned)((int64_t)nt * (nt + 1) / 2), 256, 0, st>>>(A, lda, N, j0, nb, nt);
+      k_chol_syrk1<<<(unsigned)((int64_t)nt * (nt + 1) / 2), 256, 0, st>>>(A, lda, Neff, j0, nb, nt);
       ctx->launches += 2;
     }
     ctx->launches += 1;
@@ -1275,7 +1280,7 @@ static fg_status bddc_numeric(fg_bddc* B) {
     k_seg_sum<<<nblk(B->nKpair, 256), 256, 0, st>>>(B->nKpair, B->dKptr, B->dKsrc, B->dKdst, B->dKp, B->dKc);
     k_coarse_identity<<<nblk(nC, 256), 256, 0, st>>>(nC, B->dKc);
     ctx->launches += 2;
-    FG_TRY(chol_partial_grid(ctx, B->dKc, 2 * nC, (int)(2 * nC), (int)nC, B->dErr));
+    FG_TRY(chol_partial_grid(ctx, B->dKc, 2 * nC, (int)(2 * nC), (int)nC, (int)nC, B->dErr));
     FG_TRY(check_err(B, "the coarse matrix"));
     k_coarse_extract<<<nblk(nC * nC, 256), 256, 0, st>>>(nC, B->dKc, B->dKinv, B->dKinv32);
     ctx->launches += 1;
