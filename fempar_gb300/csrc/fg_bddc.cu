@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <utility>
@@ -92,6 +93,8 @@ struct fg_bddc {
   double* dG = nullptr;
   float* dG32 = nullptr;
   int32_t* dBox = nullptr;
+  int32_t* dOrder = nullptr;  // subdomains by decreasing factorisation work
+  bool stepped = false;        // factorise panel step by panel step over all subdomains
   int64_t* dIptr = nullptr;
   int64_t* dIsrc = nullptr;
   int32_t* dIvec = nullptr;
@@ -299,12 +302,63 @@ __global__ void k_bddc_weights(int64_t nG, const int64_t* __restrict__ iptr, con
   for (int64_t t = b; t < e; ++t) w[isrc[t]] = stiffness ? diag[isrc[t]] / s : 1.0 / (double)(e - b);
 }
 
-__global__ void __launch_bounds__(256) k_bddc_potrf(const BSub* __restrict__ subs, double* __restrict__ A, int* err) {
+// Subdomains in order of decreasing size (order[]), so the largest start first and the
+// smaller ones fill the tail; two CTAs per SM share its FP64 pipe.
+__global__ void __launch_bounds__(256, 2)
+    k_bddc_potrf(const BSub* __restrict__ subs, const int32_t* __restrict__ order, double* __restrict__ A, int* err) {
+  __shared__ CholSmem sm;
+  const int sid = order[blockIdx.x];
+  const BSub S = subs[sid];
+  if (!chol_partial_cta(A + S.aoff, S.N, S.N, S.nr, sm)) {
+    if (threadIdx.x == 0) atomicCAS(err, 0, 1 + sid);
+  }
+}
+
+// The same partial Cholesky stepped by panel over all subdomains at once: per step j0 one
+// launch for the diagonal blocks, one for the row solves, one for the trailing 64 x 64 tiles of
+// every subdomain (grid.y = subdomain).  Work of uneven subdomains is then spread over all SMs
+// at every step instead of one CTA carrying the largest subdomain to the end.
+__global__ void k_bstep_diag(const BSub* __restrict__ subs, double* __restrict__ A, int j0, int* err) {
   __shared__ CholSmem sm;
   const BSub S = subs[blockIdx.x];
-  if (!chol_partial_cta(A + S.aoff, S.N, S.N, S.nr, sm)) {
+  if (j0 >= S.nr) return;
+  const int nb = min(32, S.nr - j0);
+  if (!chol_diag(A + S.aoff, S.N, j0, nb, sm)) {
     if (threadIdx.x == 0) atomicCAS(err, 0, 1 + (int)blockIdx.x);
   }
+}
+
+__global__ void __launch_bounds__(256) k_bstep_trsm(const BSub* __restrict__ subs, double* __restrict__ A, int j0) {
+  __shared__ double Dsh[32][33];
+  const BSub S = subs[blockIdx.y];
+  if (j0 >= S.nr) return;
+  const int nb = min(32, S.nr - j0);
+  const int64_t i = j0 + nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j0 + nb + (int64_t)blockIdx.x * blockDim.x >= S.N) return;  // whole block past the matrix
+  double* As = A + S.aoff;
+  for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
+    int r = t & 31, c = t >> 5;
+    Dsh[r][c] = (r < nb && c < nb && r >= c) ? As[(j0 + r) + (int64_t)(j0 + c) * S.N] : 0.0;
+  }
+  __syncthreads();
+  if (i < S.N) chol_trsm_row(As, S.N, j0, nb, i, Dsh);
+}
+
+__global__ void __launch_bounds__(256) k_bstep_syrk(const BSub* __restrict__ subs, double* __restrict__ A, int j0) {
+  __shared__ CholSmem sm;
+  const BSub S = subs[blockIdx.y];
+  if (j0 >= S.nr) return;
+  const int nb = min(32, S.nr - j0);
+  const int t0 = j0 + nb, tn = S.N - t0;
+  if (tn <= 0) return;
+  const int nt = (tn + 63) / 64;
+  const int64_t b = blockIdx.x;
+  if (b >= (int64_t)nt * (nt + 1) / 2) return;
+  int ti = (int)((sqrt(8.0 * (double)b + 1.0) - 1.0) * 0.5);
+  while ((int64_t)(ti + 1) * (ti + 2) / 2 <= b) ++ti;
+  while ((int64_t)ti * (ti + 1) / 2 > b) --ti;
+  const int tj = (int)(b - (int64_t)ti * (ti + 1) / 2);
+  chol_syrk_tile(A + S.aoff, S.N, S.N, j0, nb, t0, ti, tj, sm);
 }
 
 // Local coarse matrix K_Pi (order [V | e]), S_e^-1 and H = S_e^-1 T from the trailing block.
@@ -1146,6 +1200,22 @@ static fg_status bddc_symbolic(fg_bddc* B) {
   B->nKpair = (int64_t)kdst.size();
   // uploads
   FG_TRY(upload(B, &B->d_subs, B->subs));
+  {
+    std::vector<int32_t> ord(B->nsub);
+    for (int i = 0; i < B->nsub; ++i) ord[i] = i;
+    auto work = [&](int i) {
+      const double N = B->subs[i].N, r = N - B->subs[i].nr;
+      return N * N * N - r * r * r;
+    };
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return work(a) > work(b); });
+    FG_TRY(upload(B, &B->dOrder, ord));
+    // stepped over all subdomains by default (measured on GB300 at 32^3 Q2 elasticity, 512
+    // subdomains: 1.71 s vs 1.93 s for one CTA per subdomain with even sizes, 2.18 s vs 4.03 s
+    // with +-30 % sizes, where the largest subdomain alone sets the one-CTA finishing time);
+    // FG_BDDC_STEPPED=0 selects the single launch with one CTA per subdomain
+    const char* e = std::getenv("FG_BDDC_STEPPED");
+    B->stepped = !(e && e[0] == '0');
+  }
   FG_TRY(upload(B, &B->dLoc, h_loc));
   FG_TRY(upload(B, &B->dEc, h_ec));
   FG_TRY(upload(B, &B->dEw, h_ew));
@@ -1254,7 +1324,21 @@ static fg_status bddc_numeric(fg_bddc* B) {
   cudaEvent_t ev[4];
   for (auto& e : ev) FG_CUDA_TRY(cudaEventCreate(&e));
   FG_CUDA_TRY(cudaEventRecord(ev[0], st));
-  k_bddc_potrf<<<ns, 256, 0, st>>>(B->d_subs, B->dA, B->dErr);
+  if (B->stepped) {
+    for (int j0 = 0; j0 < B->maxnr; j0 += 32) {
+      k_bstep_diag<<<ns, 32, 0, st>>>(B->d_subs, B->dA, j0, B->dErr);
+      const int rem = B->maxN - j0 - 1;
+      if (rem > 0) {
+        k_bstep_trsm<<<dim3(nblk(rem, 256), ns), 256, 0, st>>>(B->d_subs, B->dA, j0);
+        const int nt = (rem + 63) / 64;
+        k_bstep_syrk<<<dim3((unsigned)((int64_t)nt * (nt + 1) / 2), ns), 256, 0, st>>>(B->d_subs, B->dA, j0);
+        ctx->launches += 2;
+      }
+      ctx->launches += 1;
+    }
+  } else {
+    k_bddc_potrf<<<ns, 256, 0, st>>>(B->d_subs, B->dOrder, B->dA, B->dErr);
+  }
   FG_CUDA_TRY(cudaEventRecord(ev[1], st));
   ctx->launches += 3;
   FG_CUDA_TRY(cudaGetLastError());
