@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -86,6 +87,7 @@ struct BatchArgs {
   float delta;            // reliable-update factor
   unsigned long long timeout_ns;  // a team wait gives up after this long (globaltimer)
   int* abort_all;         // set by the first wait that gives up: every CTA stops
+  int drop_arrival;       // test of the bounded wait: rank 1 of a team skips its first arrival
 };
 
 // ---- float-float helpers (error-free transformations; no reassociation in this file)
@@ -193,7 +195,7 @@ __device__ bool team_sum(const BatchArgs& a, const BatchProb& P, int prob, int r
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    atomicAdd(a.bar + prob, 1u);
+    if (!(a.drop_arrival && rank == 1 && phase == 0)) atomicAdd(a.bar + prob, 1u);
     const unsigned target = (unsigned)(phase + 1) * (unsigned)P.team;
     const unsigned long long t0 = global_ns();
     int ok = 1;
@@ -643,7 +645,13 @@ __global__ void __launch_bounds__(512, 2) k_batch_solve(BatchArgs a) {
     __syncthreads();
     const int stop = sm.abort_flag;  // one value for the whole CTA
     __syncthreads();
-    if (stop) break;
+    if (stop) {
+      // the problems this CTA leads and has not started are reported, not silently skipped
+      if (threadIdx.x == 0)
+        for (int k = j; k < a.job_ptr[blockIdx.x + 1]; ++k)
+          if (a.jobs[k].rank == 0) atomicCAS(a.status + a.jobs[k].prob, 0, (int)FG_ERR_TIMEOUT);
+      break;
+    }
     const BatchJob J = a.jobs[j];
     const int p = a.probs[J.prob].p;
     if (p == 1) solve_problem<1>(a, J.prob, J.rank, sm);
@@ -849,7 +857,17 @@ static fg_status batch_launch(fg_batch* B, cudaStream_t st) {
   a.atol = B->prm.atol;
   a.max_iters = B->prm.max_iters;
   a.delta = B->prm.inner_rtol > 0.0 ? (float)B->prm.inner_rtol : 0.1f;
+  // team waits give up after 60 s (FG_BATCH_BARRIER_TIMEOUT_MS overrides); the test switch
+  // FG_BATCH_TEST_DROP_ARRIVAL=1 makes one team member skip an arrival so that the wait runs out
   a.timeout_ns = 60ull * 1000000000ull;
+  if (const char* e = std::getenv("FG_BATCH_BARRIER_TIMEOUT_MS")) {
+    const long long ms = std::atoll(e);
+    if (ms > 0) a.timeout_ns = (unsigned long long)ms * 1000000ull;
+  }
+  {
+    const char* e = std::getenv("FG_BATCH_TEST_DROP_ARRIVAL");
+    a.drop_arrival = (e && e[0] == '1') ? 1 : 0;
+  }
   a.abort_all = B->abort_all;
   FG_CUDA_TRY(cudaMemsetAsync(B->bar, 0, sizeof(unsigned) * B->nprob, st));
   FG_CUDA_TRY(cudaMemsetAsync(B->abort_all, 0, sizeof(int), st));

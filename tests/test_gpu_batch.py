@@ -139,3 +139,39 @@ def test_batch_autotune_picks_a_block_size(fg, ctx):
     assert info["threads"] in (128, 256, 512) and info["autotune_ms"] > 0
     res = B.run()
     assert all(r["status"] == 0 for r in res)
+
+
+def test_batch_bounded_team_wait_runs_out_and_context_survives(fg, ctx, monkeypatch):
+    """Failure detection without a GPU fault: one member of every multi-CTA team skips its
+    first barrier arrival (test switch), the team waits run out after 200 ms, the run reports
+    FG_ERR_TIMEOUT, and the same context then solves normally."""
+    import time
+    from fempar_gb300 import FGError
+    from fempar_gb300.batch import BatchSolver
+    rng = np.random.default_rng(9)
+
+    def problems():
+        ps = small_set(seed=7)
+        ps.append({"n": 20, "order": 3, "coef": 2.5, "qp_source": rng.normal(size=20 ** 3 * 64),
+                   "x": np.zeros(59 ** 3)})
+        return ps
+
+    monkeypatch.setenv("FG_BATCH_BARRIER_TIMEOUT_MS", "200")
+    monkeypatch.setenv("FG_BATCH_TEST_DROP_ARRIVAL", "1")
+    B = BatchSolver(ctx, problems(), rtol=1e-10, threads=256)
+    t0 = time.perf_counter()
+    res = B.run(raise_on_error=False)
+    assert time.perf_counter() - t0 < 30.0
+    assert res[-1]["team"] > 1 and res[-1]["status"] == -6  # FG_ERR_TIMEOUT
+    with pytest.raises(FGError):
+        B.run()
+    B.close()
+    monkeypatch.delenv("FG_BATCH_TEST_DROP_ARRIVAL")
+    monkeypatch.delenv("FG_BATCH_BARRIER_TIMEOUT_MS")
+    ps = problems()
+    C = BatchSolver(ctx, ps, rtol=1e-10, threads=256)
+    res = C.run()
+    assert all(r["status"] == 0 for r in res)
+    xo = oracle_solution(ps[2])
+    assert np.linalg.norm(ps[2]["x"] - xo) <= 1e-8 * np.linalg.norm(xo)
+    C.close()
