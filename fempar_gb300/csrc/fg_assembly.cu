@@ -98,6 +98,30 @@ struct PoissonShape {
   static constexpr size_t SM_BYTES_WARP = ((size_t)SM_DOUBLES * 8 + SM_INTS * 4 + 15) / 16 * 16;
 };
 
+// Float-float variant for Q1/Q2: the scaled gradients are computed one Gauss point at a time
+// into a slice of NN x 3 (hi, lo) floats and every pair accumulates that point at once (the
+// pairs of a lane fit in registers), so a warp needs ~9 KB of shared memory instead of ~26 KB.
+template <int P>
+struct PoissonShapeFF : PoissonShape<P> {
+  using B = PoissonShape<P>;
+  static constexpr int WARPS = 8;
+  static constexpr int SM_G = B::NN * 3;  // one slice: NN x 3 hi + NN x 3 lo floats
+  static constexpr int SM_DOUBLES = B::SM_XV + B::SM_INVJ + B::SM_FAC + B::SM_XQ + B::SM_F + B::SM_SQ + SM_G + B::SM_EL;
+  static constexpr size_t SM_BYTES_WARP = ((size_t)SM_DOUBLES * 8 + B::SM_INTS * 4 + 15) / 16 * 16;
+};
+template <int P, bool FF>
+struct PoissonShapeSel {
+  using type = PoissonShape<P>;
+};
+template <>
+struct PoissonShapeSel<1, true> {
+  using type = PoissonShapeFF<1>;
+};
+template <>
+struct PoissonShapeSel<2, true> {
+  using type = PoissonShapeFF<2>;
+};
+
 // upper-triangle pair index -> (a,b), row-packed
 __device__ __forceinline__ void pair_ab(int p, int nd, int& a, int& b) {
   int row = 0, off = 0;
@@ -133,12 +157,13 @@ __device__ __forceinline__ void ff_split(double v, float& h, float& l) {
 }
 
 template <int P, bool FF>
-__global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
+__global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
     k_integrate_poisson(AsmGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
                         const int32_t* __restrict__ latdof, const double* __restrict__ gvals,
                         const double* __restrict__ coef, double coef_const, SourceSpec src,
                         double* __restrict__ E, double* __restrict__ EV) {
-  using S = PoissonShape<P>;
+  using S = typename PoissonShapeSel<P, FF>::type;
+  constexpr bool STREAM = FF && P <= 2;
   constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND, NP1 = S::NP1;
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -250,6 +275,56 @@ __global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
     for (int k = 0; k < NS; ++k)
       if (lane + 32 * k < NQ) ff_split(ts[k], sqh[lane + 32 * k], sql[lane + 32 * k]);
     __syncwarp();
+    if constexpr (STREAM) {
+      // one Gauss point at a time: slice of scaled gradients, all pairs of the lane accumulate it
+      float* qh = reinterpret_cast<float*>(sg);
+      float* ql = qh + NN * 3;
+      float ah[S::CH], al[S::CH];
+      int pa[S::CH], pb[S::CH];
+#pragma unroll
+      for (int t = 0; t < S::CH; ++t) {
+        ah[t] = 0.f;
+        al[t] = 0.f;
+        int p = lane + 32 * t;
+        if (p < S::NPAIR) pair_ab(p, ND, pa[t], pb[t]);
+        else { pa[t] = 0; pb[t] = 0; }
+      }
+      static_assert(32 * S::CH >= S::NPAIR, "one pass over the pairs");
+      for (int q = 0; q < NQ; ++q) {
+        for (int idx = lane; idx < NN * 3; idx += 32) {
+          const int a = idx / 3, i = idx - 3 * a;
+          const int r = (a * NQ + q) * 3;
+          float th = 0.f, tl = 0.f;
+#pragma unroll
+          for (int j = 0; j < 3; ++j) ff_fma(ivh[q * 9 + j + 3 * i], ivl[q * 9 + j + 3 * i], tb.shgh[r + j], tb.shgl[r + j], th, tl);
+          ff_renorm(th, tl);
+          float gh = 0.f, gl = 0.f;
+          ff_fma(sqh[q], sql[q], th, tl, gh, gl);
+          ff_renorm(gh, gl);
+          qh[idx] = gh;
+          ql[idx] = gl;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int t = 0; t < S::CH; ++t) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+            ff_fma(qh[pb[t] * 3 + i], ql[pb[t] * 3 + i], qh[pa[t] * 3 + i], ql[pa[t] * 3 + i], ah[t], al[t]);
+        }
+        __syncwarp();
+      }
+#pragma unroll
+      for (int t = 0; t < S::CH; ++t) {
+        int p = lane + 32 * t;
+        if (p < S::NPAIR) {
+          ff_renorm(ah[t], al[t]);
+          const double v = (double)ah[t] + (double)al[t];
+          el[pa[t] * ND + pb[t]] = v;
+          el[pb[t] * ND + pa[t]] = v;
+        }
+      }
+      __syncwarp();
+    } else {
     float* sgh = reinterpret_cast<float*>(sg);
     float* sgl = sgh + NQ * NN * 3;
     for (int idx = lane; idx < NQ * NN; idx += 32) {
@@ -304,6 +379,7 @@ __global__ void __launch_bounds__(PoissonShape<P>::WARPS * 32)
       }
     }
     __syncwarp();
+    }
   } else {
   // physical gradients scaled by sqrt(|det J| w k): s_a = sqrt(fk) J^-T grad_ref(phi_a), so an
   // element entry is sum_q s_a . s_b, 3 FP64 FMAs per Gauss point (FP64 is GB300's scarce pipe)
@@ -483,15 +559,17 @@ static fg_status launch_poisson(fg_system* sys) {
   src.fn = sys->integ.source_fn;
   for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
   src.qp = sys->d_qpsrc;
-  const size_t smem = S::SM_BYTES_WARP * S::WARPS;
   const bool ff = (sys->integ.flags & FG_FAST_INTEGRATION) != 0;
+  using SF = typename PoissonShapeSel<P, true>::type;
+  const int warps = ff ? SF::WARPS : S::WARPS;
+  const size_t smem = ff ? SF::SM_BYTES_WARP * SF::WARPS : S::SM_BYTES_WARP * S::WARPS;
   auto kern = ff ? k_integrate_poisson<P, true> : k_integrate_poisson<P, false>;
   FG_CUDA_TRY(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const unsigned grid = nblk(ncells, S::WARPS);
+  const unsigned grid = nblk(ncells, warps);
   ctx->launches += sp->nfree > 0 ? 2 : 1;
-  kern<<<grid, S::WARPS * 32, smem, ctx->stream>>>(g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof,
-                                                   sys->d_gvals, sys->d_coef, sys->integ.coef_const, src,
-                                                   sys->d_elmat, sys->d_elvec);
+  kern<<<grid, warps * 32, smem, ctx->stream>>>(g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof,
+                                                sys->d_gvals, sys->d_coef, sys->integ.coef_const, src,
+                                                sys->d_elmat, sys->d_elvec);
   FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
   if (n > 0) {
