@@ -28,7 +28,8 @@ FG_RES_RES, FG_RES_RHS, FG_DELTA_RHS, FG_DELTA_DELTA, FG_RES_NRMGIVEN_RHS_NRMGIV
 EXPORTS = [
     "fg_status_string", "fg_last_error", "fg_version",
     "fg_ctx_create", "fg_ctx_destroy", "fg_ctx_memory", "fg_ctx_get_stream", "fg_ctx_kernel_launches",
-    "fg_mesh_create_structured", "fg_mesh_destroy",
+    "fg_mesh_create_structured", "fg_mesh_destroy", "fg_mesh_create_unstructured", "fg_mesh_read_gid",
+    "fg_mesh_get_info", "fg_mesh_get_vefs",
     "fg_space_create", "fg_space_destroy", "fg_space_release_pattern", "fg_space_get_info", "fg_space_get_dof_map",
     "fg_space_get_dirichlet_coords",
     "fg_assemble", "fg_system_reassemble", "fg_system_destroy",
@@ -56,6 +57,14 @@ class Integrand(C.Structure):
         ("boundary_fn", C.c_int),
         ("dirichlet_values", C.c_void_p),
         ("flags", C.c_int),
+    ]
+
+
+class MeshInfo(C.Structure):
+    _fields_ = [
+        ("num_cells", C.c_int64), ("num_vertices", C.c_int64), ("num_edges", C.c_int64),
+        ("num_faces", C.c_int64), ("num_vefs", C.c_int64),
+        ("unstructured", C.c_int32), ("max_cells_around_vertex", C.c_int32),
     ]
 
 
@@ -225,6 +234,10 @@ def lib():
         "fg_ctx_kernel_launches": (i32, [vp, C.POINTER(C.c_int64)]),
         "fg_mesh_create_structured": (i32, [vp, i32, vp, vp, vp, pp]),
         "fg_mesh_destroy": (i32, [vp]),
+        "fg_mesh_create_unstructured": (i32, [vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp, vp, vp, pp]),
+        "fg_mesh_read_gid": (i32, [vp, C.c_char_p, C.c_char_p, pp]),
+        "fg_mesh_get_info": (i32, [vp, C.POINTER(MeshInfo)]),
+        "fg_mesh_get_vefs": (i32, [vp, vp, vp]),
         "fg_space_create": (i32, [vp, i32, i32, vp, i32, pp]),
         "fg_space_destroy": (i32, [vp]),
         "fg_space_release_pattern": (i32, [vp]),

@@ -223,11 +223,120 @@ fg_status fg_mesh_create_structured(fg_ctx* ctx, int num_dims, const int32_t n[3
   return FG_OK;
 }
 
+static void mesh_free(fg_mesh* m) {
+  fg_ctx* ctx = m->ctx;
+  void* ptrs[] = {m->d_coords, m->d_cellvert, m->d_cellvef, m->d_vset, m->d_vowner, m->d_vnbr, m->d_vptr, m->d_vcells};
+  for (void* p : ptrs) dev_free(ctx, p);
+  delete m;
+}
+
 fg_status fg_mesh_destroy(fg_mesh* m) {
   if (!m) return FG_OK;
   cudaSetDevice(m->ctx->device);
-  dev_free(m->ctx, m->d_coords);
-  delete m;
+  mesh_free(m);
+  return FG_OK;
+}
+
+fg_status fg_mesh_create_unstructured(fg_ctx* ctx, int64_t num_vertices, const double* vertex_xyz,
+                                      int64_t num_cells, const int32_t* cell_vertices, int64_t num_given_vefs,
+                                      const int64_t* given_vef_ptr, const int32_t* given_vef_vertices,
+                                      const int32_t* given_vef_set, fg_mesh** out) {
+  FG_CHECK_ARG(ctx && out && vertex_xyz && cell_vertices, "ctx/out/vertex_xyz/cell_vertices");
+  *out = nullptr;
+  FG_CHECK_ARG(num_vertices >= 1 && num_vertices < (int64_t)0x7fffffff, "num_vertices");
+  FG_CHECK_ARG(num_cells >= 1 && num_cells < (int64_t)0x7fffffff / 26, "num_cells");
+  FG_CHECK_ARG(num_given_vefs >= 0 && (num_given_vefs == 0 || (given_vef_ptr && given_vef_vertices && given_vef_set)),
+               "given vefs");
+  // host-side validation: every index the device kernels follow stays inside its array
+  std::vector<int32_t> cv((size_t)num_cells * 8);
+  for (size_t k = 0; k < cv.size(); ++k) {
+    const int32_t v = cell_vertices[k];
+    if (v < 1 || v > num_vertices) {
+      set_error("cell %lld: vertex id %d outside 1..%lld", (long long)(k / 8), v, (long long)num_vertices);
+      return FG_ERR_BADARG;
+    }
+    cv[k] = v - 1;
+  }
+  for (int64_t c = 0; c < num_cells; ++c)
+    for (int a = 0; a < 8; ++a)
+      for (int b = a + 1; b < 8; ++b)
+        if (cv[c * 8 + a] == cv[c * 8 + b]) {
+          set_error("cell %lld repeats vertex %d", (long long)c, cv[c * 8 + a] + 1);
+          return FG_ERR_BADARG;
+        }
+  if (num_given_vefs > 0) {
+    if (given_vef_ptr[0] != 0) { set_error("given_vef_ptr[0] must be 0"); return FG_ERR_BADARG; }
+    for (int64_t i = 0; i < num_given_vefs; ++i) {
+      const int64_t n = given_vef_ptr[i + 1] - given_vef_ptr[i];
+      if (n != 1 && n != 2 && n != 4) { set_error("given vef %lld has %lld vertices", (long long)i, (long long)n); return FG_ERR_BADARG; }
+      for (int64_t k = given_vef_ptr[i]; k < given_vef_ptr[i + 1]; ++k)
+        if (given_vef_vertices[k] < 1 || given_vef_vertices[k] > num_vertices) {
+          set_error("given vef %lld: vertex id %d outside 1..%lld", (long long)i, given_vef_vertices[k], (long long)num_vertices);
+          return FG_ERR_BADARG;
+        }
+    }
+  }
+  FG_DEVICE_GUARD(ctx);
+  fg_mesh* m = new fg_mesh();
+  m->ctx = ctx;
+  m->dim = 3;
+  m->unst = true;
+  m->n[0] = (int)num_cells;
+  m->n[1] = m->n[2] = 1;
+  for (int i = 0; i < 6; ++i) m->limits[i] = 0.0;
+  m->ncells = num_cells;
+  m->nverts = num_vertices;
+  fg_status s = dev_alloc(ctx, (void**)&m->d_coords, sizeof(double) * 3 * num_vertices);
+  if (s == FG_OK) s = dev_alloc(ctx, (void**)&m->d_cellvert, sizeof(int32_t) * cv.size());
+  if (s == FG_OK) {
+    cudaError_t e = cudaMemcpyAsync(m->d_coords, vertex_xyz, sizeof(double) * 3 * num_vertices, cudaMemcpyHostToDevice,
+                                    ctx->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(m->d_cellvert, cv.data(), sizeof(int32_t) * cv.size(), cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) { set_error("mesh upload: %s", cudaGetErrorString(e)); s = FG_ERR_CUDA; }
+  }
+  if (s == FG_OK) s = umesh_build_topology(m, num_given_vefs, given_vef_ptr, given_vef_vertices, given_vef_set);
+  if (s == FG_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { set_error("mesh: %s", cudaGetErrorString(e)); s = FG_ERR_CUDA; }
+  }
+  if (s != FG_OK) {
+    cudaStreamSynchronize(ctx->stream);
+    mesh_free(m);
+    return s;
+  }
+  *out = m;
+  return FG_OK;
+}
+
+fg_status fg_mesh_get_info(fg_mesh* m, fg_mesh_info* info) {
+  FG_CHECK_ARG(m && info, "mesh/info");
+  info->num_cells = m->ncells;
+  info->num_vertices = m->nverts;
+  if (m->unst) {
+    info->num_edges = m->nedges;
+    info->num_faces = m->nfaces;
+  } else {
+    const int64_t n0 = m->n[0], n1 = m->n[1], n2 = m->n[2];
+    info->num_edges = n0 * (n1 + 1) * (n2 + 1) + (n0 + 1) * n1 * (n2 + 1) + (n0 + 1) * (n1 + 1) * n2;
+    info->num_faces = n0 * n1 * (n2 + 1) + n0 * (n1 + 1) * n2 + (n0 + 1) * n1 * n2;
+  }
+  info->num_vefs = info->num_vertices + info->num_edges + info->num_faces;
+  info->unstructured = m->unst ? 1 : 0;
+  info->max_cells_around_vertex = m->unst ? m->max_vcells : 8;
+  return FG_OK;
+}
+
+fg_status fg_mesh_get_vefs(fg_mesh* m, int32_t* cell_vefs, int32_t* vef_set_ids) {
+  FG_CHECK_ARG(m, "mesh");
+  if (!m->unst) {
+    set_error("vef tables are exported for unstructured meshes");
+    return FG_ERR_UNSUPPORTED;
+  }
+  FG_DEVICE_GUARD(m->ctx);
+  FG_TRY(umesh_export_vefs(m, cell_vefs, vef_set_ids));
+  if (cell_vefs)
+    for (int64_t k = 0; k < m->ncells * 26; ++k) cell_vefs[k] += 1;
   return FG_OK;
 }
 
@@ -245,6 +354,9 @@ static void space_free(fg_space* sp) {
   dev_free(ctx, sp->d_sptr);
   dev_free(ctx, sp->d_scol);
   if (sp->layout == FG_LAYOUT_STENCIL) dev_free(ctx, sp->d_row2vec);
+  dev_free(ctx, sp->d_cellnode);
+  dev_free(ctx, sp->d_nptr);
+  dev_free(ctx, sp->d_ncl);
   dev_free(ctx, sp->d_st_cls);
   dev_free(ctx, sp->d_st_off);
   dev_free(ctx, sp->d_st_scls);
@@ -272,10 +384,11 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
   sp->mesh = mesh;
   sp->order = order;
   sp->ncomp = ncomp;
+  const int max_id = mesh->unst ? 31 : 27;
   for (int i = 0; i < n_ids; ++i) {
-    if (dirichlet_ids[i] < 1 || dirichlet_ids[i] > 27) {
+    if (dirichlet_ids[i] < 1 || dirichlet_ids[i] > max_id) {
       delete sp;
-      set_error("dirichlet id %d outside 1..27", dirichlet_ids[i]);
+      set_error("dirichlet id %d outside 1..%d", dirichlet_ids[i], max_id);
       return FG_ERR_BADARG;
     }
     sp->dirmask |= 1u << dirichlet_ids[i];
@@ -284,9 +397,14 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
   sp->nlat = (int64_t)sp->Ln[0] * sp->Ln[1] * sp->Ln[2];
   sp->tab.build(order, ncomp);
   fg_status s = upload_tables(ctx, sp->tab, sp->dtab);
-  if (s == FG_OK) s = space_number_dofs(sp);
-  if (s == FG_OK) s = space_build_pattern(sp);
-  {
+  if (mesh->unst) {
+    // explicit nodes and cells around them; the solver runs on the explicit-column SELL layout
+    if (s == FG_OK) s = uspace_number_dofs(sp);
+    if (s == FG_OK) s = uspace_build_pattern(sp);
+    sp->layout = FG_LAYOUT_SELL;
+  } else {
+    if (s == FG_OK) s = space_number_dofs(sp);
+    if (s == FG_OK) s = space_build_pattern(sp);
     // solver layout: lattice-implicit SELL unless FG_SOLVER_LAYOUT=sell asks for explicit columns
     const char* lay = getenv("FG_SOLVER_LAYOUT");
     sp->layout = (lay && std::strcmp(lay, "sell") == 0) ? FG_LAYOUT_SELL : FG_LAYOUT_STENCIL;

@@ -30,6 +30,10 @@ struct AsmGeom {
   int p;
   int Ln[3];
   int ncomp;
+  // unstructured meshes: cell vertices (8 per cell) and cell nodes ((p+1)^3 per cell);
+  // null on the structured lattice
+  const int32_t* cellvert;
+  const int32_t* cellnode;
 };
 
 static AsmGeom make_geom(const fg_space* sp) {
@@ -37,7 +41,23 @@ static AsmGeom make_geom(const fg_space* sp) {
   for (int d = 0; d < 3; ++d) { g.n[d] = sp->mesh->n[d]; g.Ln[d] = sp->Ln[d]; }
   g.p = sp->order;
   g.ncomp = sp->ncomp;
+  g.cellvert = sp->mesh->unst ? sp->mesh->d_cellvert : nullptr;
+  g.cellnode = sp->mesh->unst ? sp->d_cellnode : nullptr;
   return g;
+}
+
+// vertex k of cell c (lattice or explicit)
+__device__ __forceinline__ int64_t asm_vertex(const AsmGeom& g, int64_t c, int ci, int cj, int ck, int k) {
+  if (g.cellvert) return g.cellvert[c * 8 + k];
+  return (int64_t)(ci + (k & 1)) + (int64_t)(g.n[0] + 1) * ((cj + ((k >> 1) & 1)) + (int64_t)(g.n[1] + 1) * (ck + ((k >> 2) & 1)));
+}
+// node of local node a (lexicographic) of cell c
+template <int P>
+__device__ __forceinline__ int64_t asm_node(const AsmGeom& g, int64_t c, int ci, int cj, int ck, int a) {
+  constexpr int NP1 = P + 1;
+  if (g.cellnode) return g.cellnode[c * (NP1 * NP1 * NP1) + a];
+  const int ai = a % NP1, aj = (a / NP1) % NP1, ak = a / (NP1 * NP1);
+  return (int64_t)(P * ci + ai) + (int64_t)g.Ln[0] * ((P * cj + aj) + (int64_t)g.Ln[1] * (P * ck + ak));
 }
 
 struct SourceSpec {
@@ -187,14 +207,9 @@ __global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
 
   if (lane < 24) {
     int k = lane / 3, l = lane % 3;
-    int64_t v = (int64_t)(ci + (k & 1)) + (int64_t)(g.n[0] + 1) * ((cj + ((k >> 1) & 1)) + (int64_t)(g.n[1] + 1) * (ck + ((k >> 2) & 1)));
-    xv[lane] = coords[v * 3 + l];
+    xv[lane] = coords[asm_vertex(g, c, ci, cj, ck, k) * 3 + l];
   }
-  for (int s = lane; s < ND; s += 32) {
-    int ai = s % NP1, aj = (s / NP1) % NP1, ak = s / (NP1 * NP1);
-    int64_t L = (int64_t)(P * ci + ai) + (int64_t)g.Ln[0] * ((P * cj + aj) + (int64_t)g.Ln[1] * (P * ck + ak));
-    gid[s] = latdof[L];
-  }
+  for (int s = lane; s < ND; s += 32) gid[s] = latdof[asm_node<P>(g, c, ci, cj, ck, s)];
   __syncwarp();
   // Jacobian, inverse, det and physical coordinates per Gauss point
   for (int q = lane; q < NQ; q += 32) {
@@ -572,6 +587,7 @@ static fg_status launch_poisson(fg_system* sys) {
                                                 sys->d_elmat, sys->d_elvec);
   FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
+  if (sp->mesh->unst) return usystem_scatter(sys);
   if (n > 0) {
     constexpr int CAP = P == 1 ? 32 : (P == 2 ? 128 : 512);
     k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,
@@ -641,15 +657,11 @@ __global__ void __launch_bounds__(ElastShape<P>::WARPS * 32)
 
   if (lane < 24) {
     int k = lane / 3, l = lane % 3;
-    int64_t v = (int64_t)(ci + (k & 1)) +
-                (int64_t)(g.n[0] + 1) * ((cj + ((k >> 1) & 1)) + (int64_t)(g.n[1] + 1) * (ck + ((k >> 2) & 1)));
-    xv[lane] = coords[v * 3 + l];
+    xv[lane] = coords[asm_vertex(g, c, ci, cj, ck, k) * 3 + l];
   }
   for (int s = lane; s < ND; s += 32) {
     const int a = s % NN, comp = s / NN;
-    const int ai = a % NP1, aj = (a / NP1) % NP1, ak = a / (NP1 * NP1);
-    const int64_t L = (int64_t)(P * ci + ai) + (int64_t)g.Ln[0] * ((P * cj + aj) + (int64_t)g.Ln[1] * (P * ck + ak));
-    gid[s] = latdof[L * 3 + comp];
+    gid[s] = latdof[asm_node<P>(g, c, ci, cj, ck, a) * 3 + comp];
   }
   __syncwarp();
   for (int q = lane; q < NQ; q += 32) {
@@ -797,6 +809,7 @@ static fg_status launch_elasticity(fg_system* sys) {
       sys->integ.nu, src, sys->d_elmat, sys->d_elvec);
   FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
+  if (sp->mesh->unst) return usystem_scatter(sys);
   if (n > 0) {
     constexpr int CAP = P == 1 ? 128 : 512;  // (2P+1)^3 * 3 box entries
     k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,

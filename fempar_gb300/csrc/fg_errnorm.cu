@@ -19,6 +19,8 @@ namespace {
 
 struct ErrGeom {
   int n[3], p, Ln[3];
+  const int32_t* cellvert;  // unstructured meshes (null on the lattice)
+  const int32_t* cellnode;
 };
 
 __device__ double exact_value(int fn, const double* prm, const double* x) {
@@ -64,14 +66,16 @@ __global__ void __launch_bounds__(128)
   const int ci = (int)(c % g.n[0]), cj = (int)((c / g.n[0]) % g.n[1]), ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
   double xv[24];
   for (int k = 0; k < 8; ++k) {
-    int64_t v = (int64_t)(ci + (k & 1)) +
-                (int64_t)(g.n[0] + 1) * ((cj + ((k >> 1) & 1)) + (int64_t)(g.n[1] + 1) * (ck + ((k >> 2) & 1)));
+    int64_t v = g.cellvert ? (int64_t)g.cellvert[c * 8 + k]
+                           : (int64_t)(ci + (k & 1)) +
+                                 (int64_t)(g.n[0] + 1) * ((cj + ((k >> 1) & 1)) + (int64_t)(g.n[1] + 1) * (ck + ((k >> 2) & 1)));
     for (int l = 0; l < 3; ++l) xv[k * 3 + l] = coords[v * 3 + l];
   }
   double u[NN];
   for (int s = 0; s < NN; ++s) {
     int ai = s % NP1, aj = (s / NP1) % NP1, ak = s / (NP1 * NP1);
-    int64_t L = (int64_t)(P * ci + ai) + (int64_t)g.Ln[0] * ((P * cj + aj) + (int64_t)g.Ln[1] * (P * ck + ak));
+    int64_t L = g.cellnode ? (int64_t)g.cellnode[c * NN + s]
+                           : (int64_t)(P * ci + ai) + (int64_t)g.Ln[0] * ((P * cj + aj) + (int64_t)g.Ln[1] * (P * ck + ak));
     int32_t id = latdof[L];
     u[s] = id > 0 ? x[id - 1] : (id < 0 ? gvals[-id - 1] : 0.0);
   }
@@ -220,6 +224,8 @@ extern "C" fg_status fg_system_error_norms(fg_system* sys, const double* x, int3
       g.Ln[d] = sp->Ln[d];
     }
     g.p = sp->order;
+    g.cellvert = sp->mesh->unst ? sp->mesh->d_cellvert : nullptr;
+    g.cellnode = sp->mesh->unst ? sp->d_cellnode : nullptr;
     const double* xx = on_device ? x : dx;
     const unsigned blocks = (unsigned)((nc + 127) / 128);
     const double* coef = sys->d_coef;

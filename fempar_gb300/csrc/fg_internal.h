@@ -98,7 +98,18 @@ struct fg_mesh {
   int n[3] = {0, 0, 0};
   double limits[6];
   int64_t ncells = 0, nverts = 0;
-  double* d_coords = nullptr;  // 3*nverts, interleaved xyz, x-fastest lattice
+  double* d_coords = nullptr;  // 3*nverts, interleaved xyz, x-fastest lattice (structured)
+  // unstructured hexahedral mesh (fg_mesh_create_unstructured, fg_mesh_read_gid); n = {ncells,1,1}
+  bool unst = false;
+  int64_t nedges = 0, nfaces = 0, nvefs = 0;
+  int max_vcells = 0;              // most cells around one vertex
+  int32_t* d_cellvert = nullptr;   // 8*ncells vertex ids, 0-based, lexicographic local order
+  int32_t* d_cellvef = nullptr;    // 26*ncells vef ids (vertices, edges, faces), 0-based
+  int32_t* d_vset = nullptr;       // nvefs boundary set ids
+  int64_t* d_vowner = nullptr;     // nedges+nfaces: first cell * 32 + local n-face
+  int32_t* d_vnbr = nullptr;       // nedges+nfaces: cells holding the vef
+  int64_t* d_vptr = nullptr;       // nverts+1 offsets of the cells around each vertex
+  int32_t* d_vcells = nullptr;     // cells around each vertex, ascending
 };
 
 struct fg_space {
@@ -139,6 +150,12 @@ struct fg_space {
   int32_t* d_st_row = nullptr;    // 32*st_nslices: solver vector index of each row slot
   int32_t* d_row2st = nullptr;    // free row -> row slot
   std::vector<fg::StencilClass> h_st_cls;
+  // unstructured mesh: nodes (nlat of them) are vertices, edge, face and cell interior nodes
+  int32_t* d_cellnode = nullptr;  // nn*ncells node ids
+  int64_t* d_nptr = nullptr;      // nlat+1 offsets of the cells around each node
+  int64_t* d_ncl = nullptr;       // (cell << 6 | local node), ascending per node
+  int max_ncells = 0;             // most cells around one node
+  int row_cap = 0;                // power of two >= the longest row
 };
 
 struct fg_system {
@@ -189,6 +206,19 @@ fg_status space_export_upper(fg_space* sp, const double* d_val, int one_based, i
 // fg_assembly.cu
 fg_status system_interpolate_dirichlet(fg_system* sys, int boundary_fn, const double* prm);
 fg_status system_assemble(fg_system* sys);
+
+fg_status scan_i64(fg_ctx* ctx, int64_t* a, int64_t n, int64_t* total);
+fg_status space_count_upper(fg_space* sp);
+
+// fg_unstructured.cu
+fg_status umesh_build_topology(fg_mesh* m, int64_t nb, const int64_t* bptr, const int32_t* bverts,
+                               const int32_t* bset);
+fg_status umesh_export_vefs(fg_mesh* m, int32_t* cell_vefs, int32_t* vef_sets);
+fg_status uspace_number_dofs(fg_space* sp);
+fg_status uspace_build_pattern(fg_space* sp);
+fg_status uspace_export_dof_map(fg_space* sp, int32_t* out_host);
+fg_status uspace_dirichlet_coords(fg_space* sp, double* d_xyz);
+fg_status usystem_scatter(fg_system* sys);
 
 // fg_sell.cu
 fg_status space_build_sell(fg_space* sp);

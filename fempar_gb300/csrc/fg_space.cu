@@ -303,6 +303,24 @@ static fg_status exclusive_scan(fg_ctx* ctx, const int64_t* in, int64_t* out, in
   return FG_OK;
 }
 
+fg_status scan_i64(fg_ctx* ctx, int64_t* a, int64_t n, int64_t* total) { return exclusive_scan(ctx, a, a, n, total); }
+
+// entries of the upper triangle (the reference's symmetric storage), for the CSR export
+fg_status space_count_upper(fg_space* sp) {
+  fg_ctx* ctx = sp->mesh->ctx;
+  const int64_t n = sp->nfree;
+  int64_t* ulen = nullptr;
+  FG_TRY(dev_alloc(ctx, (void**)&ulen, sizeof(int64_t) * n));
+  k_upper_len<<<nblk(n, 256), 256, 0, ctx->stream>>>(n, sp->d_rowptr, sp->d_col, ulen);
+  FG_CUDA_TRY(cudaGetLastError());
+  int64_t nup = 0;
+  FG_TRY(exclusive_scan(ctx, ulen, ulen, n, &nup));
+  dev_free(ctx, ulen);
+  sp->nnz_upper = nup;
+  FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return FG_OK;
+}
+
 fg_status space_number_dofs(fg_space* sp) {
   fg_ctx* ctx = sp->mesh->ctx;
   const int64_t ncells = sp->mesh->ncells;
@@ -371,20 +389,11 @@ fg_status space_build_pattern(fg_space* sp) {
     default: set_error("neighbour box too large (%d)", box); return FG_ERR_UNSUPPORTED;
   }
   FG_CUDA_TRY(cudaGetLastError());
-  // upper-triangle count (parity export)
-  int64_t* ulen = nullptr;
-  FG_TRY(dev_alloc(ctx, (void**)&ulen, sizeof(int64_t) * n));
-  k_upper_len<<<nblk(n, 256), 256, 0, ctx->stream>>>(n, sp->d_rowptr, sp->d_col, ulen);
-  FG_CUDA_TRY(cudaGetLastError());
-  int64_t nup = 0;
-  FG_TRY(exclusive_scan(ctx, ulen, ulen, n, &nup));
-  dev_free(ctx, ulen);
-  sp->nnz_upper = nup;
-  FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  return FG_OK;
+  return space_count_upper(sp);
 }
 
 fg_status space_export_dof_map(fg_space* sp, int32_t* out_host) {
+  if (sp->mesh->unst) return uspace_export_dof_map(sp, out_host);
   fg_ctx* ctx = sp->mesh->ctx;
   Lat g = make_lat(sp);
   const int64_t total = sp->mesh->ncells * sp->tab.nd;
@@ -441,6 +450,7 @@ __global__ void k_dirichlet_coords(Lat g, int64_t ndir, const int32_t* dir2lat, 
 }
 
 fg_status space_dirichlet_coords(fg_space* sp, double* d_xyz) {
+  if (sp->mesh->unst) return uspace_dirichlet_coords(sp, d_xyz);
   if (sp->ndir == 0) return FG_OK;
   Lat g = make_lat(sp);
   k_dirichlet_coords<<<nblk(sp->ndir, 256), 256, 0, sp->mesh->ctx->stream>>>(g, sp->ndir, sp->d_dir2lat,

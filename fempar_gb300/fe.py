@@ -71,10 +71,13 @@ class Context:
 
 
 class SerialTriangulation:
-    """Structured hexahedral mesh (uniform_hex_mesh_t + serial_triangulation_t)."""
+    """Hexahedral mesh (serial_triangulation_t): structured (uniform_hex_mesh_t) from the
+    constructor, unstructured from mesh data files or arrays (``from_parameters``,
+    ``from_mesh_data_files``, ``from_arrays``)."""
 
     def __init__(self, ctx: Context, n, limits=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), vertex_xyz=None):
         self.ctx = ctx
+        self.unstructured = False
         self.n = [int(v) for v in n]
         nn = (C.c_int32 * 3)(*self.n)
         lim = (C.c_double * 6)(*[float(v) for v in limits])
@@ -89,6 +92,67 @@ class SerialTriangulation:
                 "fg_mesh_create_structured")
         self.h = h
         self.num_cells = self.n[0] * self.n[1] * self.n[2]
+
+    @classmethod
+    def _wrap(cls, ctx, h):
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.h = h
+        self.unstructured = True
+        self.n = None
+        self.num_cells = self.info()["num_cells"]
+        return self
+
+    @classmethod
+    def from_parameters(cls, ctx: Context, parameters: dict):
+        """serial_triangulation_t%create(parameters): STATIC_TRIANG_GENERATE_FROM =
+        MESH_DATA_FILES reads MESH_DIR_PATH/MESH_PREFIX.mesh; STRUCT_HEX_MESH_GENERATOR takes
+        NUM_CELLS_X_DIR (and DOMAIN_LIMITS) like the structured constructor."""
+        how = parameters.get("STATIC_TRIANG_GENERATE_FROM", "STRUCT_HEX_MESH_GENERATOR")
+        if how == "MESH_DATA_FILES":
+            return cls.from_mesh_data_files(ctx, parameters["MESH_DIR_PATH"], parameters["MESH_PREFIX"])
+        if how == "STRUCT_HEX_MESH_GENERATOR":
+            return cls(ctx, parameters["NUM_CELLS_X_DIR"],
+                       parameters.get("DOMAIN_LIMITS", (0.0, 1.0, 0.0, 1.0, 0.0, 1.0)))
+        raise ValueError(f"STATIC_TRIANG_GENERATE_FROM = {how!r}")
+
+    @classmethod
+    def from_mesh_data_files(cls, ctx: Context, dir_path: str, prefix: str):
+        """Read <dir_path>/<prefix>.mesh (GiD, fempar problem type) -- fg_mesh_read_gid."""
+        h = C.c_void_p()
+        L.check(L.lib().fg_mesh_read_gid(ctx.h, str(dir_path).encode(), str(prefix).encode(), C.byref(h)),
+                "fg_mesh_read_gid")
+        return cls._wrap(ctx, h)
+
+    @classmethod
+    def from_arrays(cls, ctx: Context, coords, cells, given_vef_ptr=None, given_vef_vertices=None,
+                    given_vef_set=None):
+        """Unstructured mesh from arrays: coords (nv, 3); cells (nc, 8) 1-based vertex ids in the
+        lexicographic local order; given boundary vefs as CSR (ptr, 1-based vertices, set ids)."""
+        xyz = np.ascontiguousarray(coords, dtype=np.float64)
+        cv = np.ascontiguousarray(cells, dtype=np.int32)
+        nb = 0 if given_vef_ptr is None else len(given_vef_ptr) - 1
+        bp = np.ascontiguousarray(given_vef_ptr if nb else [0], dtype=np.int64)
+        bv = np.ascontiguousarray(given_vef_vertices if nb else [0], dtype=np.int32)
+        bs = np.ascontiguousarray(given_vef_set if nb else [0], dtype=np.int32)
+        h = C.c_void_p()
+        L.check(L.lib().fg_mesh_create_unstructured(ctx.h, xyz.shape[0], _ptr(xyz), cv.shape[0], _ptr(cv), nb,
+                                                     _ptr(bp), _ptr(bv), _ptr(bs), C.byref(h)),
+                "fg_mesh_create_unstructured")
+        return cls._wrap(ctx, h)
+
+    def info(self):
+        i = L.MeshInfo()
+        L.check(L.lib().fg_mesh_get_info(self.h, C.byref(i)), "fg_mesh_get_info")
+        return {k: getattr(i, k) for k, _ in L.MeshInfo._fields_}
+
+    def get_vefs(self):
+        """(cell vef ids (ncells, 26), 1-based; set id of every vef) -- unstructured meshes."""
+        inf = self.info()
+        cv = np.zeros(inf["num_cells"] * 26, dtype=np.int32)
+        vs = np.zeros(inf["num_vefs"], dtype=np.int32)
+        L.check(L.lib().fg_mesh_get_vefs(self.h, _ptr(cv), _ptr(vs)), "fg_mesh_get_vefs")
+        return cv.reshape(-1, 26), vs
 
     def close(self):
         if getattr(self, "h", None):

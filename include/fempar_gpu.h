@@ -151,9 +151,42 @@ fg_status fg_mesh_create_structured(fg_ctx* ctx, int num_dims, const int32_t n[3
                                     const double* vertex_xyz, fg_mesh** out);
 fg_status fg_mesh_destroy(fg_mesh* mesh);
 
+/* Unstructured hexahedral mesh: num_vertices vertices (3 coordinates each, interleaved),
+ * num_cells cells of 8 vertex ids each (1-based, in the reference FE's lexicographic local
+ * order: bit 0 = x, bit 1 = y, bit 2 = z of the reference cell) and the given boundary vefs
+ * (vertex ids of vertex k of vef i at given_vef_vertices[given_vef_ptr[i] + k]; 1, 2 or 4
+ * vertices) with their set ids.  Edges and faces are generated on the device in the
+ * reference's first-appearance order; set ids are assigned and handed from boundary faces to
+ * their edges and vertices as the reference does.
+ * Replaces serial_triangulation_t%create from mesh data files
+ * (Sources/Lib/Geometry/Triangulation/sbm_serial_triangulation.i90:120-188,
+ *  Sources/Lib/Geometry/Triangulation/sbm_fine_triangulation.i90:115-527). */
+fg_status fg_mesh_create_unstructured(fg_ctx* ctx, int64_t num_vertices, const double* vertex_xyz,
+                                      int64_t num_cells, const int32_t* cell_vertices, int64_t num_given_vefs,
+                                      const int64_t* given_vef_ptr, const int32_t* given_vef_vertices,
+                                      const int32_t* given_vef_set, fg_mesh** out);
+/* Read <dir_path>/<prefix>.mesh (GiD, fempar problem type: header, coordinates, elements,
+ * vefs; hexahedra in GiD order are reordered to the lexicographic one when the header's order
+ * is 0) and build the unstructured mesh.  Only 3D hexahedral meshes are accepted.
+ * Replaces mesh_t%read_fempar_gid_problem_type_format
+ * (Sources/Lib/Geometry/Mesh/mesh.f90:337-504). */
+fg_status fg_mesh_read_gid(fg_ctx* ctx, const char* dir_path, const char* prefix, fg_mesh** out);
+
+typedef struct {
+  int64_t num_cells, num_vertices, num_edges, num_faces, num_vefs;
+  int32_t unstructured;             /* 1 for fg_mesh_create_unstructured / fg_mesh_read_gid */
+  int32_t max_cells_around_vertex;  /* unstructured meshes                                 */
+} fg_mesh_info;
+fg_status fg_mesh_get_info(fg_mesh* mesh, fg_mesh_info* info);
+/* Unstructured meshes: the vef ids of every cell (26 per cell, 1-based: vertices, edges,
+ * faces in the reference FE's local order) and the set id of every vef (either may be NULL).
+ * The reference's lst_vefs_gids and vefs_set (sbm_fine_triangulation.i90:115-527). */
+fg_status fg_mesh_get_vefs(fg_mesh* mesh, int32_t* cell_vefs, int32_t* vef_set_ids);
+
 /* Lagrangian FE space of order 1..3 with ncomp components (1 = scalar, 3 = vector),
  * global dof numbering and strong Dirichlet dofs on the boundary set ids listed
- * (polytope ids 1..26 of the structured generator).
+ * (polytope ids 1..26 of the structured generator; the mesh file's set ids 1..31 on an
+ * unstructured mesh).
  * Replaces serial_fe_space_t%create + set_up_strong_dirichlet_bcs + generate_global_dof_numbering
  * (Sources/Lib/Integration/FESpace/sbm_serial_fe_space.i90:28-298,525-716,2423-2884). */
 fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* dirichlet_ids, int n_ids,

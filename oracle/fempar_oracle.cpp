@@ -336,6 +336,12 @@ struct orc_problem {
   std::vector<double> rhs;
   double t_setup = 0, t_integrate = 0, t_compress = 0;
   std::vector<double> qp_source;            // copy of per-qp source if given
+  // unstructured hexahedral mesh (GiD route): explicit cells, generated vefs
+  bool unst = false;
+  int64_t nverts_u = 0, nedges = 0, nfaces = 0, nvefs = 0;
+  std::vector<int32_t> cellvert;            // ncells*8, 0-based vertex ids, lexicographic local order
+  std::vector<int64_t> cellvef;             // ncells*26, 0-based vef gids (vertices, edges, faces)
+  std::vector<int> vset;                    // nvefs boundary set ids
 
   int64_t vert_index(const int* v) const {
     return v[0] + (int64_t)(n[0] + 1) * (v[1] + (int64_t)(n[1] + 1) * (dim == 3 ? v[2] : 0));
@@ -347,6 +353,11 @@ struct orc_problem {
     ijk[2] = dim == 3 ? (int)(r / n[1]) : 0;
   }
   void cell_vertices(int64_t c, double* xv /*ngeo*3*/) const {
+    if (unst) {
+      for (int k = 0; k < 8; ++k)
+        for (int l = 0; l < 3; ++l) xv[k * 3 + l] = coords[(size_t)cellvert[(size_t)c * 8 + k] * 3 + l];
+      return;
+    }
     int ijk[3];
     cell_ijk(c, ijk);
     for (int k = 0; k < ngeo; ++k) {
@@ -374,13 +385,170 @@ int vef_set_id(const orc_problem& P, int type, const int* v, const std::vector<i
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Unstructured hexahedral meshes (the mesh-data-files route of the serial triangulation,
+// sbm_serial_triangulation.i90:120-188).
+// Local vertices of n-face f of the hex: anchor | s for every subset s of its free directions.
+std::vector<int> nface_vertices(int code) {
+  int anchor = code & 7, t = code >> 3;
+  std::vector<int> out;
+  for (int s = 0; s < 8; ++s)
+    if ((s & ~t) == 0) out.push_back(anchor | s);
+  return out;
+}
+int nface_dim(int code) { return popcount(code >> 3); }
+
+void generate_unstructured_topology(orc_problem& P, const orc_umesh* m) {
+  const int64_t nc = P.ncells, nv = P.nverts_u;
+  const std::vector<int>& codes = P.fe.codes;
+  const int NV = 26;
+  // cells around vertices, ascending (sbm_base_static_triangulation.i90:697-739)
+  std::vector<std::vector<int64_t>> around(nv);
+  for (int64_t c = 0; c < nc; ++c)
+    for (int k = 0; k < 8; ++k) around[P.cellvert[c * 8 + k]].push_back(c);
+  std::vector<std::vector<int>> fv(NV);
+  for (int f = 0; f < NV; ++f) fv[f] = nface_vertices(codes[f]);
+  auto sorted_gids = [&](int64_t c, int f) {
+    std::vector<int64_t> g;
+    for (int v : fv[f]) g.push_back(P.cellvert[c * 8 + v]);
+    std::sort(g.begin(), g.end());
+    return g;
+  };
+  // vefs: vertices keep their ids; edges, then faces, numbered on first appearance walking
+  // the cells in order, later cells around the n-face's first vertex receive the same id
+  // (sbm_fine_triangulation.i90:115-315)
+  P.cellvef.assign((size_t)nc * NV, -1);
+  for (int64_t c = 0; c < nc; ++c)
+    for (int k = 0; k < 8; ++k) P.cellvef[c * NV + k] = P.cellvert[c * 8 + k];
+  int64_t nvefs = nv;
+  for (int dim = 1; dim <= 2; ++dim) {
+    for (int64_t c = 0; c < nc; ++c)
+      for (int f = 0; f < NV; ++f) {
+        if (nface_dim(codes[f]) != dim || P.cellvef[c * NV + f] != -1) continue;
+        const int64_t id = nvefs++;
+        P.cellvef[c * NV + f] = id;
+        std::vector<int64_t> gi = sorted_gids(c, f);
+        const int64_t first = P.cellvert[c * 8 + fv[f][0]];
+        for (int64_t c2 : around[first]) {
+          if (c2 <= c) continue;
+          for (int f2 = 0; f2 < NV; ++f2) {
+            if (nface_dim(codes[f2]) != dim) continue;
+            if (sorted_gids(c2, f2) == gi) { P.cellvef[c2 * NV + f2] = id; break; }
+          }
+        }
+      }
+    if (dim == 1) P.nedges = nvefs - nv;
+    else P.nfaces = nvefs - nv - P.nedges;
+  }
+  P.nvefs = nvefs;
+  // set ids of the given boundary vefs, in the given order (sbm_fine_triangulation.i90:317-444)
+  P.vset.assign(nvefs, 0);
+  for (int64_t ib = 0; ib < m->num_given_vefs; ++ib) {
+    const int64_t b0 = m->given_vef_ptr[ib], nb = m->given_vef_ptr[ib + 1] - b0;
+    const int sid = m->given_vef_set[ib];
+    std::vector<int64_t> gv;
+    for (int64_t k = 0; k < nb; ++k) gv.push_back((int64_t)m->given_vef_vertices[b0 + k] - 1);
+    if (nb == 1) { P.vset[gv[0]] = sid; continue; }
+    const int dim = nb == 2 ? 1 : 2;
+    std::vector<int64_t> gs = gv;
+    std::sort(gs.begin(), gs.end());
+    bool done = false;
+    for (int64_t c2 : around[gv[0]]) {
+      for (int f2 = 0; f2 < NV && !done; ++f2) {
+        if (nface_dim(codes[f2]) != dim || (int64_t)fv[f2].size() != nb) continue;
+        if (sorted_gids(c2, f2) == gs) { P.vset[P.cellvef[c2 * NV + f2]] = sid; done = true; }
+      }
+      if (done) break;
+    }
+  }
+  // boundary faces (one cell around) hand their set id to the edges and vertices of their
+  // closure that have none, faces visited in gid order (sbm_fine_triangulation.i90:453-527)
+  std::vector<int> ncell_around(nvefs, 0);
+  std::vector<int64_t> first_cell(nvefs, -1);
+  std::vector<int> first_pos(nvefs, -1);
+  for (int64_t c = 0; c < nc; ++c)
+    for (int f = 0; f < NV; ++f) {
+      int64_t g = P.cellvef[c * NV + f];
+      if (ncell_around[g]++ == 0) { first_cell[g] = c; first_pos[g] = f; }
+    }
+  for (int64_t g = nv + P.nedges; g < nvefs; ++g) {
+    if (ncell_around[g] != 1) continue;
+    const int sid = P.vset[g];
+    const int64_t c = first_cell[g];
+    const int fc = codes[first_pos[g]];
+    for (int f = 0; f < NV; ++f) {
+      const int code = codes[f];
+      if (nface_dim(code) >= 2) continue;
+      // sub-n-face of the facet: its vertices are a subset of the facet's
+      bool sub = true;
+      for (int v : fv[f]) {
+        bool in = false;
+        for (int w : nface_vertices(fc)) in = in || (w == v);
+        sub = sub && in;
+      }
+      if (!sub) continue;
+      int64_t s = P.cellvef[c * NV + f];
+      if (P.vset[s] == 0) P.vset[s] = sid;
+    }
+  }
+}
+
+// Own dofs of a vef seen from cell c and from the cell that numbered them: node (i_k) of the
+// vef in c and node (j_k) in the source are the same point once the corner vertices are matched
+// (fetch_own_dofs_vef_from_source_fe, sbm_fe_cell_iterator.i90:736-856).
+void fetch_unstructured(orc_problem& P, int64_t c, int f, int64_t sc, int sf) {
+  const RefFE& fe = P.fe;
+  const int p = P.order, code = fe.codes[f], scode = fe.codes[sf];
+  int d[3], e[3], m = 0, m2 = 0;
+  for (int i = 0; i < 3; ++i) if (((code >> 3) >> i) & 1) d[m++] = i;
+  for (int i = 0; i < 3; ++i) if (((scode >> 3) >> i) & 1) e[m2++] = i;
+  const int a = code & 7, a2 = scode & 7;
+  auto corner = [&](int64_t cell, int anchor, const int* dirs, int bits) {
+    int v = anchor;
+    for (int k = 0; k < m; ++k) if ((bits >> k) & 1) v |= 1 << dirs[k];
+    return P.cellvert[cell * 8 + v];
+  };
+  int M[4] = {0, 0, 0, 0};  // source corner bits -> corner bits in c
+  for (int u = 0; u < (1 << m); ++u) {
+    int32_t g = corner(sc, a2, e, u);
+    for (int b = 0; b < (1 << m); ++b) if (corner(c, a, d, b) == g) M[u] = b;
+  }
+  int axis[2] = {0, 0}, flip[2] = {0, 0};
+  for (int k = 0; k < m; ++k) {
+    int diff = M[0] ^ M[1 << k];
+    int r = 0;
+    while (!((diff >> r) & 1)) ++r;
+    axis[k] = r;
+    flip[k] = (M[0] >> r) & 1;
+  }
+  int nn_f = 1;
+  for (int k = 0; k < m; ++k) nn_f *= (p - 1);
+  const std::vector<int>& t = fe.own[f];
+  const std::vector<int>& s = fe.own[sf];
+  if (nn_f == 0) return;
+  for (int kn = 0; kn < nn_f; ++kn) {
+    int i[2] = {0, 0}, r = kn;
+    for (int k = 0; k < m; ++k) { i[k] = r % (p - 1) + 1; r /= (p - 1); }
+    int kn2 = 0, mul = 1;
+    for (int k = 0; k < m; ++k) {
+      int j = flip[k] ? p - i[axis[k]] : i[axis[k]];
+      kn2 += (j - 1) * mul;
+      mul *= (p - 1);
+    }
+    for (int comp = 0; comp < fe.ncomp; ++comp)
+      P.gids[(size_t)c * P.nd + t[comp * nn_f + kn]] = P.gids[(size_t)sc * P.nd + s[comp * nn_f + kn2]];
+  }
+}
+
 void build_mesh_and_dofs(orc_problem& P) {
   const orc_params& p = P.p;
   P.dim = p.num_dims; P.order = p.order;
   P.ncomp = p.kind == ORC_ELASTICITY ? P.dim : 1;
-  P.n[0] = p.n[0]; P.n[1] = p.n[1]; P.n[2] = P.dim == 3 ? p.n[2] : 1;
-  P.ncells = (int64_t)P.n[0] * P.n[1] * (P.dim == 3 ? P.n[2] : 1);
-  P.nverts_lattice = (int64_t)(P.n[0] + 1) * (P.n[1] + 1) * (P.dim == 3 ? P.n[2] + 1 : 1);
+  if (!P.unst) {
+    P.n[0] = p.n[0]; P.n[1] = p.n[1]; P.n[2] = P.dim == 3 ? p.n[2] : 1;
+    P.ncells = (int64_t)P.n[0] * P.n[1] * (P.dim == 3 ? P.n[2] : 1);
+    P.nverts_lattice = (int64_t)(P.n[0] + 1) * (P.n[1] + 1) * (P.dim == 3 ? P.n[2] + 1 : 1);
+  }
   P.fe.build(P.dim, P.order, P.ncomp);
   P.geo.build(P.dim, 1, 1);
   P.nd = P.fe.nshape;
@@ -410,8 +578,8 @@ void build_mesh_and_dofs(orc_problem& P) {
     tensor_shapes(P.dim, 1, npts, P.fe.nnodes, P.gnod, g);
   }
   // vertex coordinates: ijk/n mapped to the domain limits (uniform_hex_mesh_generator.f90:608-612,632-636)
-  P.coords.assign(P.nverts_lattice * 3, 0.0);
-  for (int64_t vi = 0; vi < P.nverts_lattice; ++vi) {
+  if (!P.unst) P.coords.assign(P.nverts_lattice * 3, 0.0);
+  for (int64_t vi = 0; vi < (P.unst ? 0 : P.nverts_lattice); ++vi) {
     int64_t r = vi;
     int v[3];
     v[0] = (int)(r % (P.n[0] + 1)); r /= (P.n[0] + 1);
@@ -422,7 +590,7 @@ void build_mesh_and_dofs(orc_problem& P) {
       P.coords[vi * 3 + d] = (p.limits[2 * d + 1] - p.limits[2 * d]) * c + p.limits[2 * d];
     }
   }
-  if (p.vertex_xyz)
+  if (p.vertex_xyz && !P.unst)
     std::memcpy(P.coords.data(), p.vertex_xyz, sizeof(double) * 3 * P.nverts_lattice);
   P.coef.assign(P.ncells, 1.0);
   if (p.cell_coef) std::memcpy(P.coef.data(), p.cell_coef, sizeof(double) * P.ncells);
@@ -431,12 +599,13 @@ void build_mesh_and_dofs(orc_problem& P) {
   const RefFE& fe = P.fe;
   const int nvefs = fe.nfaces - 1;  // cell interior is the last n-face
   P.gids.assign((size_t)P.ncells * P.nd, 0);
-  std::vector<char> is_dir_id(28, 0);
+  std::vector<char> is_dir_id(64, 0);
   for (int i = 0; i < p.n_dirichlet_ids; ++i)
-    if (p.dirichlet_ids[i] >= 1 && p.dirichlet_ids[i] <= 27) is_dir_id[p.dirichlet_ids[i]] = 1;
+    if (p.dirichlet_ids[i] >= 1 && p.dirichlet_ids[i] < 64) is_dir_id[p.dirichlet_ids[i]] = 1;
   const int ntypes = 1 << P.dim;
-  const int64_t nkeys = (int64_t)ntypes * P.nverts_lattice;
-  auto vef_of = [&](int64_t c, int f, int* v, int& type) {
+  const int64_t nkeys = P.unst ? P.nvefs : (int64_t)ntypes * P.nverts_lattice;
+  auto vef_of = [&](int64_t c, int f, int* v, int& type) -> int64_t {
+    if (P.unst) { type = fe.codes[f] >> 3; return P.cellvef[(size_t)c * 26 + f]; }
     int code = fe.codes[f];
     int anchor = code & (ntypes - 1);
     type = code >> P.dim;
@@ -445,7 +614,11 @@ void build_mesh_and_dofs(orc_problem& P) {
     for (int d = 0; d < 3; ++d) v[d] = d < P.dim ? ijk[d] + ((anchor >> d) & 1) : 0;
     return (int64_t)type + ntypes * P.vert_index(v);
   };
+  auto set_of = [&](int64_t key, int type, const int* v) {
+    return P.unst ? P.vset[key] : vef_set_id(P, type, v, fe.codes);
+  };
   auto fetch = [&](int64_t c, int f, int64_t src_c, int src_f) {
+    if (P.unst) { fetch_unstructured(P, c, f, src_c, src_f); return; }
     // identity permutation: on a structured mesh all cells share one orientation,
     // so the k-th own dof of the n-face maps to the k-th own dof of the owner's n-face
     // (sbm_fe_cell_iterator.i90:736-856)
@@ -463,9 +636,9 @@ void build_mesh_and_dofs(orc_problem& P) {
       for (int f = 0; f < nvefs; ++f) {
         int v[3], type;
         int64_t key = vef_of(c, f, v, type);
-        int sid = vef_set_id(P, type, v, fe.codes);
+        int sid = set_of(key, type, v);
         if (sid == 0) continue;
-        bool code = is_dir_id[sid] != 0;  // one condition per set id, all components
+        bool code = sid > 0 && sid < 64 && is_dir_id[sid] != 0;  // one condition per set id, all components
         int64_t prev = ndir;
         if (vis_cell[key] == -1) {
           for (int s : fe.own[f]) {
@@ -794,6 +967,48 @@ orc_problem* orc_create(const orc_params* p) {
   P->t_integrate = (t2 - t1) - P->t_compress;
   P->p.vertex_xyz = nullptr; P->p.cell_coef = nullptr; P->p.qp_source = nullptr;
   return P;
+}
+
+orc_problem* orc_create_unstructured(const orc_params* p, const orc_umesh* m) {
+  if (!p || !m || p->num_dims != 3 || p->order < 1 || p->order > 8 || m->num_cells < 1) return nullptr;
+  orc_problem* P = new orc_problem();
+  P->p = *p;
+  P->unst = true;
+  P->dim = 3;
+  P->ncells = m->num_cells;
+  P->nverts_u = m->num_vertices;
+  P->coords.assign(m->coords, m->coords + 3 * m->num_vertices);
+  P->cellvert.resize((size_t)m->num_cells * 8);
+  for (size_t k = 0; k < P->cellvert.size(); ++k) {
+    int32_t v = m->cell_vertices[k] - 1;
+    if (v < 0 || v >= m->num_vertices) { delete P; return nullptr; }
+    P->cellvert[k] = v;
+  }
+  double t0 = now_s();
+  P->fe.build(3, p->order, p->kind == ORC_ELASTICITY ? 3 : 1);
+  generate_unstructured_topology(*P, m);
+  build_mesh_and_dofs(*P);
+  if (p->source_fn == ORC_FN_QP_VALUES && p->qp_source)
+    P->qp_source.assign(p->qp_source, p->qp_source + (size_t)P->ncells * P->nq * (p->kind == ORC_ELASTICITY ? 3 : 1));
+  double t1 = now_s();
+  assemble(*P);
+  double t2 = now_s();
+  P->t_setup = t1 - t0;
+  P->t_integrate = (t2 - t1) - P->t_compress;
+  P->p.vertex_xyz = nullptr; P->p.cell_coef = nullptr; P->p.qp_source = nullptr;
+  return P;
+}
+
+int64_t orc_num_vefs(const orc_problem* h, int64_t* num_edges, int64_t* num_faces) {
+  if (num_edges) *num_edges = h->nedges;
+  if (num_faces) *num_faces = h->nfaces;
+  return h->nvefs;
+}
+void orc_get_cell_vefs(const orc_problem* h, int32_t* out) {
+  for (size_t k = 0; k < h->cellvef.size(); ++k) out[k] = (int32_t)(h->cellvef[k] + 1);
+}
+void orc_get_vef_sets(const orc_problem* h, int32_t* out) {
+  for (size_t k = 0; k < h->vset.size(); ++k) out[k] = h->vset[k];
 }
 
 void orc_destroy(orc_problem* h) { delete h; }

@@ -7,6 +7,8 @@
  *
  * What it restates (reference paths are relative to the fempar source tree):
  *   structured hex/quad mesh     Sources/Lib/Geometry/Tools/uniform_hex_mesh_generator.f90:145-647
+ *   unstructured hex mesh vefs   Sources/Lib/Geometry/Triangulation/sbm_fine_triangulation.i90:115-527,
+ *                                Sources/Lib/Geometry/Triangulation/sbm_base_static_triangulation.i90:697-739
  *   polytope n-faces, nodes      Sources/Lib/Integration/ReferenceFE/sbm_polytope.i90:175-433,640-860
  *   own-dof lists, components    Sources/Lib/Integration/ReferenceFE/sbm_lagrangian_reference_fe.i90:1072-1153,1240-1285,1549-1758
  *   Dirichlet-first numbering    Sources/Lib/Integration/FESpace/sbm_serial_fe_space.i90:525-716
@@ -73,9 +75,32 @@ typedef struct {
 
 typedef struct orc_problem orc_problem;
 
+/* Unstructured hexahedral mesh, as the GiD reader hands it to the serial triangulation
+ * (sbm_serial_triangulation.i90:120-188): vertices, cells (8 vertex ids each, 1-based, in the
+ * reference FE's lexicographic local order) and the given boundary vefs with their set ids.
+ * Vefs are generated by first appearance (sbm_fine_triangulation.i90:115-315), given set ids
+ * assigned (:317-444) and handed from boundary faces to their edges/vertices (:453-527). */
+typedef struct {
+  int64_t num_vertices;
+  const double* coords;               /* 3*num_vertices                       */
+  int64_t num_cells;
+  const int32_t* cell_vertices;       /* 8*num_cells, 1-based                 */
+  int64_t num_given_vefs;
+  const int64_t* given_vef_ptr;       /* num_given_vefs+1 offsets             */
+  const int32_t* given_vef_vertices;  /* 1-based vertex ids                   */
+  const int32_t* given_vef_set;       /* set id of each given vef             */
+} orc_umesh;
+
 /* Build mesh, dof numbering, Dirichlet values, element integration, COO and CSR. */
 orc_problem* orc_create(const orc_params* p);
 void orc_destroy(orc_problem* h);
+/* Same on an unstructured hexahedral mesh (num_dims 3; n, limits, vertex_xyz unused;
+ * dirichlet_ids are the mesh's set ids, 1..63). */
+orc_problem* orc_create_unstructured(const orc_params* p, const orc_umesh* m);
+/* Vefs of the unstructured mesh: total (vertices + edges + faces), edges and faces. */
+int64_t orc_num_vefs(const orc_problem* h, int64_t* num_edges, int64_t* num_faces);
+void orc_get_cell_vefs(const orc_problem* h, int32_t* out);   /* ncells*26, 1-based vef gids */
+void orc_get_vef_sets(const orc_problem* h, int32_t* out);    /* nvefs set ids               */
 
 /* Sizes. */
 int64_t orc_num_cells(const orc_problem* h);

@@ -48,6 +48,19 @@ class _Params(C.Structure):
     ]
 
 
+class _UMesh(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_int64),
+        ("coords", C.c_void_p),
+        ("num_cells", C.c_int64),
+        ("cell_vertices", C.c_void_p),
+        ("num_given_vefs", C.c_int64),
+        ("given_vef_ptr", C.c_void_p),
+        ("given_vef_vertices", C.c_void_p),
+        ("given_vef_set", C.c_void_p),
+    ]
+
+
 def build(force: bool = False) -> str:
     """Compile liboracle.so with the committed Makefile (plain g++)."""
     src = os.path.join(HERE, "fempar_oracle.cpp")
@@ -68,6 +81,12 @@ def lib():
         L.orc_create.restype = vp
         L.orc_create.argtypes = [C.POINTER(_Params)]
         L.orc_destroy.argtypes = [vp]
+        L.orc_create_unstructured.restype = vp
+        L.orc_create_unstructured.argtypes = [C.POINTER(_Params), C.POINTER(_UMesh)]
+        L.orc_num_vefs.restype = i64
+        L.orc_num_vefs.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.orc_get_cell_vefs.argtypes = [vp, vp]
+        L.orc_get_vef_sets.argtypes = [vp, vp]
         for name in ("orc_num_cells", "orc_num_free", "orc_num_dirichlet", "orc_nnz_upper", "orc_coo_entries"):
             getattr(L, name).restype = i64
             getattr(L, name).argtypes = [vp]
@@ -160,7 +179,7 @@ class Problem:
         P.translated_jacobian = int(bool(translated_jacobian))
         P.nthreads = int(nthreads)
         self.params = P
-        self.h = lib().orc_create(C.byref(P))
+        self.h = self._create(P)
         if not self.h:
             raise ValueError("oracle rejected the parameters")
         L = lib()
@@ -171,6 +190,9 @@ class Problem:
         self.ndir = L.orc_num_dirichlet(self.h)
         self.nnz_upper = L.orc_nnz_upper(self.h)
         self.coo_entries = L.orc_coo_entries(self.h)
+
+    def _create(self, P):
+        return lib().orc_create(C.byref(P))
 
     def __del__(self):
         try:
@@ -264,3 +286,44 @@ class Problem:
         np.add.at(rp, r2 + 1, 1)
         rp = np.cumsum(rp)
         return rp, c2.astype(np.int32), v2
+
+
+class UProblem(Problem):
+    """The oracle on an unstructured hexahedral mesh (``gid.read_gid`` arrays or the same keys):
+    vefs generated by first appearance, boundary set ids from the given vefs, dirichlet_ids
+    are the mesh's set ids."""
+
+    def __init__(self, mesh, order=1, dirichlet_ids=(1,), **kw):
+        m = _UMesh()
+        coords = np.ascontiguousarray(mesh["coords"], dtype=np.float64)
+        cells = np.ascontiguousarray(mesh["cells"], dtype=np.int32)
+        bptr = np.ascontiguousarray(mesh["bvef_ptr"], dtype=np.int64)
+        bv = np.ascontiguousarray(mesh["bvef_verts"], dtype=np.int32)
+        bs = np.ascontiguousarray(mesh["bvef_set"], dtype=np.int32)
+        self._mesh_keep = [coords, cells, bptr, bv, bs]
+        m.num_vertices = coords.shape[0]
+        m.coords = _ptr(coords)
+        m.num_cells = cells.shape[0]
+        m.cell_vertices = _ptr(cells)
+        m.num_given_vefs = bptr.size - 1
+        m.given_vef_ptr = _ptr(bptr)
+        m.given_vef_vertices = _ptr(bv)
+        m.given_vef_set = _ptr(bs)
+        self._umesh = m
+        super().__init__((1, 1, 1), order=order, num_dims=3, dirichlet_ids=list(dirichlet_ids), **kw)
+        ne, nf = C.c_int64(0), C.c_int64(0)
+        self.nvefs = lib().orc_num_vefs(self.h, C.byref(ne), C.byref(nf))
+        self.nedges, self.nfaces = ne.value, nf.value
+
+    def _create(self, P):
+        return lib().orc_create_unstructured(C.byref(P), C.byref(self._umesh))
+
+    def cell_vefs(self):
+        out = np.zeros(self.ncells * 26, dtype=np.int32)
+        lib().orc_get_cell_vefs(self.h, _ptr(out))
+        return out.reshape(self.ncells, 26)
+
+    def vef_sets(self):
+        out = np.zeros(self.nvefs, dtype=np.int32)
+        lib().orc_get_vef_sets(self.h, _ptr(out))
+        return out
