@@ -30,7 +30,7 @@ EXPORTS = [
     "fg_ctx_create", "fg_ctx_destroy", "fg_ctx_memory", "fg_ctx_get_stream", "fg_ctx_kernel_launches",
     "fg_mesh_create_structured", "fg_mesh_destroy", "fg_mesh_create_unstructured", "fg_mesh_read_gid",
     "fg_mesh_get_info", "fg_mesh_get_vefs",
-    "fg_space_create", "fg_space_destroy", "fg_space_release_pattern", "fg_space_get_info", "fg_space_get_dof_map",
+    "fg_space_create", "fg_space_create_dg", "fg_space_destroy", "fg_space_release_pattern", "fg_space_get_info", "fg_space_get_dof_map",
     "fg_space_get_dirichlet_coords",
     "fg_assemble", "fg_system_reassemble", "fg_system_destroy",
     "fg_system_export_csr", "fg_system_export_rhs", "fg_system_export_dirichlet_values",
@@ -240,6 +240,7 @@ def lib():
         "fg_mesh_get_vefs": (i32, [vp, vp, vp]),
         "fg_space_create": (i32, [vp, i32, i32, vp, i32, pp]),
         "fg_space_destroy": (i32, [vp]),
+        "fg_space_create_dg": (i32, [vp, i32, pp]),
         "fg_space_release_pattern": (i32, [vp]),
         "fg_space_get_info": (i32, [vp, C.POINTER(SpaceInfo)]),
         "fg_space_get_dof_map": (i32, [vp, vp]),

@@ -357,6 +357,8 @@ static void space_free(fg_space* sp) {
   dev_free(ctx, sp->d_cellnode);
   dev_free(ctx, sp->d_nptr);
   dev_free(ctx, sp->d_ncl);
+  dev_free(ctx, sp->d_dgnbr);
+  dev_free(ctx, sp->d_dgnbrface);
   dev_free(ctx, sp->d_st_cls);
   dev_free(ctx, sp->d_st_off);
   dev_free(ctx, sp->d_st_scls);
@@ -417,6 +419,42 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
     } else {
       s = space_build_stencil(sp);
     }
+  }
+  if (s == FG_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { set_error("space: %s", cudaGetErrorString(e)); s = FG_ERR_CUDA; }
+  }
+  if (s != FG_OK) {
+    space_free(sp);
+    return s;
+  }
+  *out = sp;
+  return FG_OK;
+}
+
+fg_status fg_space_create_dg(fg_mesh* mesh, int order, fg_space** out) {
+  FG_CHECK_ARG(mesh && out, "mesh/out");
+  *out = nullptr;
+  if (order < 1 || order > FG_MAX_ORDER) {
+    set_error("order %d not built (1..%d)", order, FG_MAX_ORDER);
+    return FG_ERR_UNSUPPORTED;
+  }
+  fg_ctx* ctx = mesh->ctx;
+  FG_DEVICE_GUARD(ctx);
+  fg_space* sp = new fg_space();
+  sp->mesh = mesh;
+  sp->order = order;
+  sp->ncomp = 1;
+  sp->dg = true;
+  for (int d = 0; d < 3; ++d) sp->Ln[d] = order * mesh->n[d] + 1;
+  sp->tab.build(order, 1);
+  fg_status s = upload_tables(ctx, sp->tab, sp->dtab);
+  if (s == FG_OK) s = dg_space_build(sp);
+  sp->layout = FG_LAYOUT_SELL;
+  if (s == FG_OK) {
+    s = space_build_sell(sp);
+    sp->nvec = sp->nfree;
+    sp->d_row2vec = sp->d_iperm;
   }
   if (s == FG_OK) {
     cudaError_t e = cudaStreamSynchronize(ctx->stream);

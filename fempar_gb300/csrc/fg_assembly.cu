@@ -42,7 +42,7 @@ static AsmGeom make_geom(const fg_space* sp) {
   g.p = sp->order;
   g.ncomp = sp->ncomp;
   g.cellvert = sp->mesh->unst ? sp->mesh->d_cellvert : nullptr;
-  g.cellnode = sp->mesh->unst ? sp->d_cellnode : nullptr;
+  g.cellnode = sp->d_cellnode;  // unstructured meshes and dG spaces
   return g;
 }
 
@@ -587,6 +587,7 @@ static fg_status launch_poisson(fg_system* sys) {
                                                 sys->d_elmat, sys->d_elvec);
   FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
+  if (sp->dg) return dg_assemble_rows(sys);
   if (sp->mesh->unst) return usystem_scatter(sys);
   if (n > 0) {
     constexpr int CAP = P == 1 ? 32 : (P == 2 ? 128 : 512);
@@ -830,6 +831,10 @@ fg_status system_assemble(fg_system* sys) {
         set_error("elasticity of order %d is not built on the device (orders 1-2)", sp->order);
         return FG_ERR_UNSUPPORTED;
     }
+  }
+  if (sp->dg && (sys->integ.kind != FG_POISSON || sys->integ.cell_coef || sys->integ.coef_const != 1.0)) {
+    set_error("the dG formulation is built for the Poisson integrand with k = 1 (tutorial_01)");
+    return FG_ERR_UNSUPPORTED;
   }
   if (sys->integ.kind != FG_POISSON || sp->ncomp != 1) {
     set_error("integrand kind %d with %d components is not built", sys->integ.kind, sp->ncomp);

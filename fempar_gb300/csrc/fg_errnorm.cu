@@ -225,7 +225,7 @@ extern "C" fg_status fg_system_error_norms(fg_system* sys, const double* x, int3
     }
     g.p = sp->order;
     g.cellvert = sp->mesh->unst ? sp->mesh->d_cellvert : nullptr;
-    g.cellnode = sp->mesh->unst ? sp->d_cellnode : nullptr;
+    g.cellnode = sp->d_cellnode;
     const double* xx = on_device ? x : dx;
     const unsigned blocks = (unsigned)((nc + 127) / 128);
     const double* coef = sys->d_coef;

@@ -156,6 +156,10 @@ struct fg_space {
   int64_t* d_ncl = nullptr;       // (cell << 6 | local node), ascending per node
   int max_ncells = 0;             // most cells around one node
   int row_cap = 0;                // power of two >= the longest row
+  // discontinuous Galerkin space (fg_space_create_dg): cell-interior dofs, face neighbours
+  bool dg = false;
+  int32_t* d_dgnbr = nullptr;     // 6*ncells: neighbour across local face lf, -1 on the boundary
+  int8_t* d_dgnbrface = nullptr;  // 6*ncells: the neighbour's local face
 };
 
 struct fg_system {
@@ -219,6 +223,10 @@ fg_status uspace_build_pattern(fg_space* sp);
 fg_status uspace_export_dof_map(fg_space* sp, int32_t* out_host);
 fg_status uspace_dirichlet_coords(fg_space* sp, double* d_xyz);
 fg_status usystem_scatter(fg_system* sys);
+
+// fg_dg.cu
+fg_status dg_space_build(fg_space* sp);
+fg_status dg_assemble_rows(fg_system* sys);
 
 // fg_sell.cu
 fg_status space_build_sell(fg_space* sp);

@@ -161,14 +161,23 @@ class SerialTriangulation:
 
 
 class SerialFESpace:
-    """Lagrangian FE space with strong Dirichlet dofs (serial_fe_space_t)."""
+    """Lagrangian FE space with strong Dirichlet dofs (serial_fe_space_t); ``dg=True`` builds the
+    discontinuous space of tutorial_01's interior-penalty formulation (scalar, weak boundary
+    data, no Dirichlet ids)."""
 
-    def __init__(self, triangulation: SerialTriangulation, order: int = 1, ncomp: int = 1, dirichlet_ids=()):
+    def __init__(self, triangulation: SerialTriangulation, order: int = 1, ncomp: int = 1, dirichlet_ids=(),
+                 dg: bool = False):
         self.triangulation = triangulation
-        ids = np.ascontiguousarray(list(dirichlet_ids), dtype=np.int32)
+        self.dg = bool(dg)
         h = C.c_void_p()
-        L.check(L.lib().fg_space_create(triangulation.h, order, ncomp, _ptr(ids) if ids.size else None,
-                                        int(ids.size), C.byref(h)), "fg_space_create")
+        if self.dg:
+            if ncomp != 1 or len(list(dirichlet_ids)):
+                raise ValueError("the dG space is scalar and takes its boundary data weakly")
+            L.check(L.lib().fg_space_create_dg(triangulation.h, order, C.byref(h)), "fg_space_create_dg")
+        else:
+            ids = np.ascontiguousarray(list(dirichlet_ids), dtype=np.int32)
+            L.check(L.lib().fg_space_create(triangulation.h, order, ncomp, _ptr(ids) if ids.size else None,
+                                            int(ids.size), C.byref(h)), "fg_space_create")
         self.h = h
         info = L.SpaceInfo()
         L.check(L.lib().fg_space_get_info(h, C.byref(info)), "fg_space_get_info")

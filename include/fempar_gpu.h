@@ -192,6 +192,14 @@ fg_status fg_mesh_get_vefs(fg_mesh* mesh, int32_t* cell_vefs, int32_t* vef_set_i
 fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* dirichlet_ids, int n_ids,
                           fg_space** out);
 fg_status fg_space_destroy(fg_space* space);
+/* Discontinuous Lagrangian space of order 1..3 (scalar) for tutorial_01's symmetric interior
+ * penalty formulation: every dof belongs to one cell (ids c*nn + a + 1, cell-local order), no
+ * strong Dirichlet dofs.  fg_assemble on it takes the Poisson integrand with k = 1: volume terms,
+ * interior-facet and boundary-facet (weak Dirichlet data boundary_fn) terms with C_IP = 10 p^2.
+ * Replaces serial_fe_space_t%create with fe_space_type_dg and dg_discrete_integration_t
+ * (Tutorials/tutorial_01_poisson_sharp_circular_wave/modules/
+ *  tutorial_01_poisson_sharp_circular_wave_modules.f90:146-322). */
+fg_status fg_space_create_dg(fg_mesh* mesh, int order, fg_space** out);
 /* Free the space's CSR pattern (row pointers and column indices) once its systems are
  * assembled lean (FG_LEAN_SYSTEM): solves keep working, further assemblies and exports
  * return FG_ERR_UNSUPPORTED.  No counterpart in the reference (serving memory control). */

@@ -627,6 +627,16 @@ void build_mesh_and_dofs(orc_problem& P) {
     for (size_t k = 0; k < t.size(); ++k)
       P.gids[(size_t)c * P.nd + t[k]] = P.gids[(size_t)src_c * P.nd + s[k]];
   };
+  if (p.formulation == ORC_DG) {
+    // dG space: every dof is a cell-interior own dof, numbered cell by cell in local order;
+    // boundary data enter weakly (no strong Dirichlet dofs)
+    for (int64_t c = 0; c < P.ncells; ++c)
+      for (int s = 0; s < P.nd; ++s) P.gids[(size_t)c * P.nd + s] = (int32_t)(c * P.nd + s + 1);
+    P.ndir = 0;
+    P.nfree = P.ncells * P.nd;
+    P.gvals.clear();
+    return;
+  }
   // (1) strong Dirichlet dofs, negative, first visit order (sbm_serial_fe_space.i90:525-716)
   {
     std::vector<int64_t> vis_cell(nkeys, -1);
@@ -820,6 +830,227 @@ void integrate_cell(const orc_problem& P, int64_t c, const std::vector<double>* 
   }
 }
 
+// ---------------------------------------------------------------------------
+// dG interior-penalty facet terms (tutorial_01 modules :146-322).  Facets are visited in
+// order of first appearance (walking the cells, local faces in order); the left cell is the
+// smaller cell id (cells around a vef are ascending).  Geometry per facet quadrature point:
+//   facet map: x, dx/ds, dx/dt from the left cell's face vertices, normal = dx/ds x dx/dt,
+//     |n| = area element, n/|n| times the orientation factor that makes it the left cell's
+//     outward normal (sbm_facet_map.i90:74-128, sbm_reference_fe.i90:523-543);
+//   each cell: its reference point (the right cell's through the face's shared corners),
+//     Jacobian, inverse, shape values and physical gradients;
+//   h = min over the cells of 2 (prod_i |grad xi_i|^-1)^(1/3) (sbm_cell_map.i90:429-461,
+//     sbm_facet_integrator.i90:248-264).
+struct FacetSide { int64_t c; int f; };
+
+int64_t cell_vertex_id(const orc_problem& P, int64_t c, int k) {
+  if (P.unst) return P.cellvert[(size_t)c * 8 + k];
+  int ijk[3];
+  P.cell_ijk(c, ijk);
+  int v[3] = {ijk[0] + (k & 1), ijk[1] + ((k >> 1) & 1), ijk[2] + ((k >> 2) & 1)};
+  return P.vert_index(v);
+}
+
+void face_dirs(int code, int& d1, int& d2, int& dn, int& anchor) {
+  anchor = code & 7;
+  int t = code >> 3, m = 0, dd[2] = {0, 0};
+  for (int d = 0; d < 3; ++d) if ((t >> d) & 1) dd[m++] = d; else dn = d;
+  d1 = dd[0]; d2 = dd[1];
+}
+
+// reference point in side S of the facet point with left-face coordinates (s, t)
+void side_point(const orc_problem& P, FacetSide L, FacetSide S, double s, double t, double* xi) {
+  int d1, d2, dn, a;
+  face_dirs(P.fe.codes[S.f], d1, d2, dn, a);
+  double u[2] = {s, t};
+  if (S.c != L.c) {
+    int ld1, ld2, ldn, la;
+    face_dirs(P.fe.codes[L.f], ld1, ld2, ldn, la);
+    auto corner = [&](FacetSide F, int fd1, int fd2, int fa, int b) {
+      return cell_vertex_id(P, F.c, fa | ((b & 1) << fd1) | (((b >> 1) & 1) << fd2));
+    };
+    int M[4];
+    for (int bs = 0; bs < 4; ++bs) {
+      M[bs] = 0;
+      for (int bl = 0; bl < 4; ++bl)
+        if (corner(L, ld1, ld2, la, bl) == corner(S, d1, d2, a, bs)) M[bs] = bl;
+    }
+    for (int k = 0; k < 2; ++k) {
+      int diff = M[0] ^ M[1 << k], r = (diff & 1) ? 0 : 1;
+      u[k] = ((M[0] >> r) & 1) ? -(r == 0 ? s : t) : (r == 0 ? s : t);
+    }
+  }
+  xi[d1] = u[0];
+  xi[d2] = u[1];
+  xi[dn] = ((a >> dn) & 1) ? 1.0 : -1.0;
+}
+
+struct SideEval {
+  std::vector<double> val, grad;  // nn shape values, nn*3 physical gradients
+  double h = 0.0, det = 0.0;
+};
+
+void eval_side(const orc_problem& P, int64_t c, const double* xi, SideEval& E) {
+  std::vector<double> pt = {xi[0], xi[1], xi[2]}, gv, gg, sv, sg;
+  tensor_shapes(3, 1, pt, 1, gv, gg);
+  tensor_shapes(3, P.order, pt, 1, sv, sg);
+  double xv[24];
+  P.cell_vertices(c, xv);
+  double J[9], b[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  for (int j = 0; j < 3; ++j) {
+    for (int l = 0; l < 3; ++l) J[l + 3 * j] = 0.0;
+    for (int k = 0; k < 8; ++k) {
+      double alpha = gg[(size_t)k * 3 + j];
+      for (int l = 0; l < 3; ++l) J[l + 3 * j] = J[l + 3 * j] + alpha * xv[k * 3 + l];
+    }
+  }
+  invmtx(3, J, b, E.det);
+  const int nn = P.fe.nnodes;
+  E.val.assign(nn, 0.0);
+  E.grad.assign((size_t)nn * 3, 0.0);
+  for (int s = 0; s < nn; ++s) {
+    E.val[s] = sv[s];
+    for (int i = 0; i < 3; ++i) {
+      double acc = 0.0;
+      for (int j = 0; j < 3; ++j) acc = acc + b[j + 3 * i] * sg[(size_t)s * 3 + j];
+      E.grad[(size_t)s * 3 + i] = acc;
+    }
+  }
+  double ih[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) ih[i] = ih[i] + b[i + 3 * j] * b[i + 3 * j];
+    ih[i] = std::sqrt(ih[i]);
+  }
+  double vh = ih[0];
+  for (int i = 1; i < 3; ++i) vh = vh * ih[i];
+  vh = 1.0 / vh;
+  vh = std::pow(vh, 1.0 / 3.0);
+  E.h = 2.0 * vh;
+}
+
+double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+void dg_facets(orc_problem& P, std::vector<int32_t>& cia, std::vector<int32_t>& cja, std::vector<double>& cval) {
+  const orc_params& p = P.p;
+  const int nn = P.fe.nnodes, np1 = P.order + 1;
+  const double C_IP = 10.0 * (double)(P.order * P.order);
+  // facet key -> the (at most two) cells holding it, ascending
+  const int ntypes = 8;
+  auto key_of = [&](int64_t c, int f) -> int64_t {
+    if (P.unst) return P.cellvef[(size_t)c * 26 + f];
+    int ijk[3];
+    P.cell_ijk(c, ijk);
+    const int code = P.fe.codes[f], anchor = code & 7;
+    int v[3] = {ijk[0] + (anchor & 1), ijk[1] + ((anchor >> 1) & 1), ijk[2] + ((anchor >> 2) & 1)};
+    return (int64_t)(code >> 3) + ntypes * P.vert_index(v);
+  };
+  std::vector<std::pair<int64_t, int64_t>> occ;  // (key, c*32+f)
+  for (int64_t c = 0; c < P.ncells; ++c)
+    for (int f = 20; f < 26; ++f) occ.push_back({key_of(c, f), c * 32 + f});
+  std::sort(occ.begin(), occ.end());
+  std::vector<int64_t> other((size_t)P.ncells * 6, -1);
+  for (size_t i = 0; i + 1 < occ.size(); ++i)
+    if (occ[i].first == occ[i + 1].first) {
+      int64_t a = occ[i].second, b = occ[i + 1].second;
+      other[(a >> 5) * 6 + (a & 31) - 20] = b;
+      other[(b >> 5) * 6 + (b & 31) - 20] = a;
+    }
+  std::vector<double> x1(np1), w1(np1);
+  gauss_legendre(np1, x1.data(), w1.data());
+  const int nq = np1 * np1;
+  std::vector<double> fpts((size_t)nq * 3, 0.0), fv, fg;
+  for (int q = 0; q < nq; ++q) { fpts[q * 3] = x1[q % np1]; fpts[q * 3 + 1] = x1[q / np1]; }
+  tensor_shapes(2, 1, fpts, nq, fv, fg);  // facet geometry: 4 bilinear shapes on [-1,1]^2
+  std::vector<double> facemat((size_t)4 * nn * nn), facevec((size_t)2 * nn);
+  auto FM = [&](int i, int j, int I, int J) -> double& { return facemat[(((size_t)I * 2 + J) * nn + j) * nn + i]; };
+  for (int64_t c = 0; c < P.ncells; ++c)
+    for (int f = 20; f < 26; ++f) {
+      const int64_t o = other[c * 6 + f - 20];
+      if (o >= 0 && (o >> 5) < c) continue;  // visited from the smaller cell
+      const bool boundary = o < 0;
+      FacetSide side[2] = {{c, f}, {boundary ? -1 : (o >> 5), boundary ? -1 : (int)(o & 31)}};
+      const int nsides = boundary ? 1 : 2;
+      int d1, d2, dn, a;
+      face_dirs(P.fe.codes[f], d1, d2, dn, a);
+      double X[4][3];
+      for (int k = 0; k < 4; ++k) {
+        int64_t v = cell_vertex_id(P, c, a | ((k & 1) << d1) | (((k >> 1) & 1) << d2));
+        for (int l = 0; l < 3; ++l) X[k][l] = P.coords[(size_t)v * 3 + l];
+      }
+      const double sigma = (d1 == 0 && d2 == 2) ? -1.0 : 1.0;
+      const double outward = ((a >> dn) & 1) ? 1.0 : -1.0;
+      std::fill(facemat.begin(), facemat.end(), 0.0);
+      std::fill(facevec.begin(), facevec.end(), 0.0);
+      double orient = 0.0;
+      for (int q = 0; q < nq; ++q) {
+        const double s = fpts[q * 3], t = fpts[q * 3 + 1];
+        double xq[3] = {0, 0, 0}, js[3] = {0, 0, 0}, jt[3] = {0, 0, 0};
+        for (int k = 0; k < 4; ++k) {
+          const double ph = fv[(size_t)k * nq + q], ds = fg[((size_t)k * nq + q) * 3], dt = fg[((size_t)k * nq + q) * 3 + 1];
+          for (int l = 0; l < 3; ++l) {
+            xq[l] = xq[l] + ph * X[k][l];
+            js[l] = js[l] + ds * X[k][l];
+            jt[l] = jt[l] + dt * X[k][l];
+          }
+        }
+        double n[3] = {js[1] * jt[2] - js[2] * jt[1], js[2] * jt[0] - js[0] * jt[2], js[0] * jt[1] - js[1] * jt[0]};
+        const double det = std::sqrt(dot3(n, n));
+        SideEval E[2];
+        for (int I = 0; I < nsides; ++I) {
+          double xi[3];
+          side_point(P, side[0], side[I], s, t, xi);
+          eval_side(P, side[I].c, xi, E[I]);
+        }
+        if (q == 0) orient = sigma * outward * (E[0].det > 0.0 ? 1.0 : -1.0);
+        for (int l = 0; l < 3; ++l) n[l] = det != 0.0 ? n[l] / det * orient : 0.0;
+        double nrm[2][3];
+        for (int l = 0; l < 3; ++l) { nrm[0][l] = n[l]; nrm[1][l] = -n[l]; }
+        const double h = nsides == 2 ? std::min(E[0].h, E[1].h) : E[0].h;
+        const double factor = det * (w1[q % np1] * w1[q / np1]);
+        if (!boundary) {
+          for (int I = 0; I < 2; ++I)
+            for (int J = 0; J < 2; ++J)
+              for (int i = 0; i < nn; ++i)
+                for (int j = 0; j < nn; ++j) {
+                  const double t1 = 0.5 * dot3(&E[J].grad[(size_t)j * 3], nrm[I]) * E[I].val[i];
+                  const double t2 = 0.5 * dot3(&E[I].grad[(size_t)i * 3], nrm[J]) * E[J].val[j];
+                  const double sc = C_IP / h * E[J].val[j] * E[I].val[i];
+                  const double t3 = (sc * nrm[I][0]) * nrm[J][0] + (sc * nrm[I][1]) * nrm[J][1] + (sc * nrm[I][2]) * nrm[J][2];
+                  FM(i, j, I, J) = FM(i, j, I, J) + factor * (-t1 - t2 + t3);
+                }
+        } else {
+          const double g = fn_value(p.boundary_fn, p.fn_param, 3, xq);
+          for (int i = 0; i < nn; ++i) {
+            for (int j = 0; j < nn; ++j) {
+              const double t1 = dot3(&E[0].grad[(size_t)j * 3], n) * E[0].val[i];
+              const double t2 = dot3(&E[0].grad[(size_t)i * 3], n) * E[0].val[j];
+              const double t3 = C_IP / h * E[0].val[i] * E[0].val[j];
+              FM(i, j, 0, 0) = FM(i, j, 0, 0) + factor * (-t1 - t2 + t3);
+            }
+            double gg[3] = {g * E[0].grad[(size_t)i * 3], g * E[0].grad[(size_t)i * 3 + 1], g * E[0].grad[(size_t)i * 3 + 2]};
+            facevec[i] = facevec[i] + factor * (-dot3(gg, n) + C_IP / h * g * E[0].val[i]);
+          }
+        }
+      }
+      // COO append, upper entries (base_sparse_matrix.f90:3469-3513); facet rhs
+      for (int I = 0; I < nsides; ++I)
+        for (int J = 0; J < nsides; ++J)
+          for (int j = 0; j < nn; ++j) {
+            const int32_t jas = P.gids[(size_t)side[J].c * P.nd + j];
+            for (int i = 0; i < nn; ++i) {
+              const int32_t ias = P.gids[(size_t)side[I].c * P.nd + i];
+              if (ias > jas) continue;
+              cia.push_back(ias); cja.push_back(jas); cval.push_back(FM(i, j, I, J));
+            }
+          }
+      if (boundary)
+        for (int i = 0; i < nn; ++i) {
+          const int32_t g = P.gids[(size_t)c * P.nd + i];
+          P.rhs[g - 1] = P.rhs[g - 1] + facevec[i];
+        }
+    }
+}
+
 void assemble(orc_problem& P) {
   const int nd = P.nd;
   std::vector<double> invj0, det0, xq0;
@@ -855,6 +1086,7 @@ void assemble(orc_problem& P) {
       for (int i = 0; i < nd; ++i) if (gid[i] > 0) P.rhs[gid[i] - 1] = P.rhs[gid[i] - 1] + elvec[i];
     }
   }
+  if (P.p.formulation == ORC_DG) dg_facets(P, cia, cja, cval);
   P.coo_n = (int64_t)cia.size();
   double t0 = now_s();
   // sort_and_compress (base_sparse_matrix.f90:4121-4829): stable bucket by row, stable
@@ -952,8 +1184,13 @@ void expand_full(const orc_problem& P, FullCSR& F) {
 // ===========================================================================
 extern "C" {
 
+static bool dg_params_ok(const orc_params* p) {
+  return p->formulation != ORC_DG || (p->num_dims == 3 && p->kind == ORC_POISSON && !p->cell_coef);
+}
+
 orc_problem* orc_create(const orc_params* p) {
   if (!p || (p->num_dims != 2 && p->num_dims != 3) || p->order < 1 || p->order > 8) return nullptr;
+  if (!dg_params_ok(p)) return nullptr;
   orc_problem* P = new orc_problem();
   P->p = *p;
   double t0 = now_s();
@@ -971,6 +1208,7 @@ orc_problem* orc_create(const orc_params* p) {
 
 orc_problem* orc_create_unstructured(const orc_params* p, const orc_umesh* m) {
   if (!p || !m || p->num_dims != 3 || p->order < 1 || p->order > 8 || m->num_cells < 1) return nullptr;
+  if (!dg_params_ok(p)) return nullptr;
   orc_problem* P = new orc_problem();
   P->p = *p;
   P->unst = true;

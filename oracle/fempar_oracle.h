@@ -23,6 +23,8 @@
  *                                Sources/Lib/Integration/ReferenceFE/sbm_cell_integrator.i90:448-500
  *   physical gradients           Sources/Lib/Integration/ReferenceFE/sbm_lagrangian_reference_fe.i90:1306-1342
  *   Poisson integrand            Tutorials/tutorial_01_poisson_sharp_circular_wave/modules/...modules.f90:71-137
+ *   dG interior penalty          ...modules.f90:146-322; facet geometry: Sources/Lib/Integration/ReferenceFE/
+ *                                sbm_facet_integrator.i90:212-264, sbm_facet_map.i90:74-128, sbm_cell_map.i90:429-461
  *   elasticity integrand         Sources/Tests/Par/par_test_pb_bddc_linear_elasticity/modules/
  *                                sbm_irreducible_discrete_integration.i90:46-135
  *   Dirichlet lifting            Sources/Lib/Integration/FESpace/sbm_fe_cell_iterator.i90:1610-1637
@@ -71,7 +73,10 @@ typedef struct {
   int boundary_fn;          /* ORC_FN_* for the Dirichlet data               */
   int translated_jacobian;  /* 1 = reuse cell-1 Jacobian (reference structured-mesh shortcut) */
   int nthreads;             /* threads for the element loop (1 = reference serial order) */
+  int formulation;          /* ORC_CG, or ORC_DG: tutorial_01's interior-penalty dG (Poisson, k = 1) */
 } orc_params;
+
+enum { ORC_CG = 0, ORC_DG = 1 };
 
 typedef struct orc_problem orc_problem;
 

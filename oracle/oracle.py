@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 POISSON, ELASTICITY = 0, 1
+CG, DG = 0, 1
 FN_ZERO, FN_CONST, FN_SHARP_WAVE, FN_LINEAR, FN_QP_VALUES = 0, 1, 2, 3, 4
 RES_RES, RES_RHS, DELTA_RHS, DELTA_DELTA, RES_NRMGIVEN_RHS_NRMGIVEN, RES_NRMGIVEN_RES_NRMGIVEN = range(6)
 
@@ -45,6 +46,7 @@ class _Params(C.Structure):
         ("boundary_fn", C.c_int),
         ("translated_jacobian", C.c_int),
         ("nthreads", C.c_int),
+        ("formulation", C.c_int),
     ]
 
 
@@ -143,7 +145,7 @@ class Problem:
 
     def __init__(self, n, order=1, num_dims=3, kind=POISSON, dirichlet_ids=None, limits=None,
                  vertex_xyz=None, cell_coef=None, nu=0.3, source_fn=FN_ZERO, fn_param=(),
-                 qp_source=None, boundary_fn=FN_ZERO, translated_jacobian=False, nthreads=1):
+                 qp_source=None, boundary_fn=FN_ZERO, translated_jacobian=False, nthreads=1, formulation=CG):
         P = _Params()
         P.num_dims = num_dims
         n = list(n) + [1] * (3 - len(n))
@@ -178,6 +180,7 @@ class Problem:
         P.boundary_fn = boundary_fn
         P.translated_jacobian = int(bool(translated_jacobian))
         P.nthreads = int(nthreads)
+        P.formulation = int(formulation)
         self.params = P
         self.h = self._create(P)
         if not self.h:
