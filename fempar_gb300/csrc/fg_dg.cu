@@ -275,8 +275,8 @@ template <int P>
 struct DgShape {
   static constexpr int NP1 = P + 1, NN = NP1 * NP1 * NP1, NQF = NP1 * NP1;
   static constexpr int WARPS = P == 3 ? 1 : (P == 2 ? 4 : 8);
-  // per warp: D, O (NN*NN), rv (NN), val[2][NN], grad[2][NN][3], xv[3][24], misc[40]
-  static constexpr int DOUBLES = 2 * NN * NN + NN + 2 * NN + 6 * NN + 72 + 40;
+  // per warp: D, O (NN*NN), rv (NN), V[2][NN], A[2][NN], xv[3][24], misc[40], 1D tables[2][3][4][2]
+  static constexpr int DOUBLES = 2 * NN * NN + NN + 2 * NN + 2 * NN + 72 + 40 + 48;
   static constexpr size_t BYTES_WARP = (size_t)DOUBLES * 8;
 };
 
@@ -293,10 +293,12 @@ __global__ void __launch_bounds__(DgShape<P>::WARPS * 32)
   double* D = sm + (size_t)wib * (S::BYTES_WARP / 8);
   double* O = D + NN * NN;
   double* rv = O + NN * NN;
-  double* sval = rv + NN;        // [2][NN]
-  double* sgrad = sval + 2 * NN; // [2][NN][3]
-  double* xv = sgrad + 6 * NN;   // [3][24]: (unused), left cell, right cell
-  double* misc = xv + 72;        // n[0..2], factor[3], g[5], b[2][9] at 6, xi[2][3] at 24, h[2] at 30, det at 32
+  double* sval = rv + NN;        // [2][NN] shape values of both sides
+  double* sA = sval + 2 * NN;    // [2][NN] scaled normal derivatives of both sides
+  double* xv = sA + 2 * NN;      // [3][24]: (unused), left cell, right cell
+  double* misc = xv + 72;        // n[0..2], factor[3], g[5], b[2][9] at 6, xi[2][3] at 24, h[2] at 30, det at 32,
+                                 // B n per side at 33..38
+  double* tab = misc + 40;       // [side][dir][j][value, derivative] of the 1D basis
   const int64_t c = (int64_t)blockIdx.x * S::WARPS + wib;
   if (c >= nc) return;
   for (int t = lane; t < NN * NN; t += 32) D[t] = E[(size_t)c * NN * NN + t];
@@ -387,59 +389,61 @@ __global__ void __launch_bounds__(DgShape<P>::WARPS * 32)
       __syncwarp();
       if (qp == 0) orient = sigma * outward * (misc[32] > 0.0 ? 1.0 : -1.0);
       const double h = boundary ? misc[30] : fmin(misc[30], misc[31]);
-      // shape values and physical gradients of both sides at their points
-      for (int t = lane; t < 2 * NN; t += 32) {
-        const int side = t / NN, a = t % NN;
-        if (side == 1 && boundary) continue;
-        const double* xi = misc + 24 + 3 * side;
-        double v0[NP1], d0[NP1], v1[NP1], d1[NP1], v2[NP1], d2[NP1];
-        lag1d<P>(xi[0], v0, d0);
-        lag1d<P>(xi[1], v1, d1);
-        lag1d<P>(xi[2], v2, d2);
-        const int ai = a % NP1, aj = (a / NP1) % NP1, ak = a / (NP1 * NP1);
-        const double g0 = d0[ai] * v1[aj] * v2[ak], g1 = v0[ai] * d1[aj] * v2[ak], g2 = v0[ai] * v1[aj] * d2[ak];
-        const double* b = misc + 6 + 9 * side;
-        sval[side * NN + a] = v0[ai] * v1[aj] * v2[ak];
-        for (int i = 0; i < 3; ++i) sgrad[(side * NN + a) * 3 + i] = b[0 + 3 * i] * g0 + b[1 + 3 * i] * g1 + b[2 + 3 * i] * g2;
-      }
-      __syncwarp();
       const double n0 = misc[0] * orient, n1 = misc[1] * orient, n2 = misc[2] * orient;
       const double factor = misc[3];
       const double ch = q.cip / h;
+      // 1D basis at both sides' points; J^-1 n per side: grad(phi) . n = grad_ref(phi) . (J^-1 n)
+      if (lane < 6 && (lane < 3 || !boundary)) {
+        const int side = lane / 3, dir = lane % 3;
+        double v[NP1], dv[NP1];
+        lag1d<P>(misc[24 + 3 * side + dir], v, dv);
+        for (int jj = 0; jj < NP1; ++jj) {
+          tab[((side * 3 + dir) * 4 + jj) * 2 + 0] = v[jj];
+          tab[((side * 3 + dir) * 4 + jj) * 2 + 1] = dv[jj];
+        }
+      } else if (lane >= 8 && lane < 14 && (lane < 11 || !boundary)) {
+        const int side = (lane - 8) / 3, jr = (lane - 8) % 3;
+        const double* b = misc + 6 + 9 * side;
+        misc[33 + 3 * side + jr] = b[jr + 0] * n0 + b[jr + 3] * n1 + b[jr + 6] * n2;
+      }
+      __syncwarp();
+      // per node: value and scaled normal derivative (the sign of this cell's side folded in)
+      const double sI = I == 0 ? 1.0 : -1.0;
+      const double ascale = boundary ? factor : 0.5 * factor * sI;
+      for (int t = lane; t < 2 * NN; t += 32) {
+        const int side = t / NN, a = t % NN;
+        if (side == 1 && boundary) continue;
+        const int ai = a % NP1, aj = (a / NP1) % NP1, ak = a / (NP1 * NP1);
+        const double* T0 = tab + ((side * 3 + 0) * 4 + ai) * 2;
+        const double* T1 = tab + ((side * 3 + 1) * 4 + aj) * 2;
+        const double* T2 = tab + ((side * 3 + 2) * 4 + ak) * 2;
+        const double* w = misc + 33 + 3 * side;
+        const double dn = T0[1] * T1[0] * T2[0] * w[0] + T0[0] * T1[1] * T2[0] * w[1] + T0[0] * T1[0] * T2[1] * w[2];
+        sval[side * NN + a] = T0[0] * T1[0] * T2[0];
+        sA[side * NN + a] = ascale * dn;
+      }
+      __syncwarp();
       if (boundary) {
         const double g = misc[5];
+        const double pen = factor * ch;
         for (int t = lane; t < NN * NN; t += 32) {
           const int i = t / NN, j = t % NN;
-          const double* gi = sgrad + i * 3;
-          const double* gj = sgrad + j * 3;
-          const double t1 = (gj[0] * n0 + gj[1] * n1 + gj[2] * n2) * sval[i];
-          const double t2 = (gi[0] * n0 + gi[1] * n1 + gi[2] * n2) * sval[j];
-          const double t3 = ch * sval[i] * sval[j];
-          D[t] = D[t] + factor * (-t1 - t2 + t3);
+          D[t] = D[t] - (sA[j] * sval[i] + sA[i] * sval[j]) + pen * sval[i] * sval[j];
         }
-        for (int i = lane; i < NN; i += 32) {
-          const double* gi = sgrad + i * 3;
-          rv[i] = rv[i] + factor * (-(g * gi[0] * n0 + g * gi[1] * n1 + g * gi[2] * n2) + ch * g * sval[i]);
-        }
+        for (int i = lane; i < NN; i += 32) rv[i] = rv[i] - g * sA[i] + pen * g * sval[i];
       } else {
-        // n_I for this cell's side, n_J for both sides; n_I . n_J = +-|n|^2
-        const double sI = I == 0 ? 1.0 : -1.0;
-        const double nn2 = n0 * n0 + n1 * n1 + n2 * n2;
+        // n_I . n_J = +-|n|^2; with A = sI w|J_F| (grad phi . n)/2:
+        //   same side:  -(A_j v_i + A_i v_j) + pen v_j v_i
+        //   other side: -A^J_j v_i + A^I_i v^J_j - pen v^J_j v_i
+        const double pen = factor * ch * (n0 * n0 + n1 * n1 + n2 * n2);
+        const int Jo = 1 - I;
         for (int t = lane; t < NN * NN; t += 32) {
           const int i = t / NN, j = t % NN;
-          const double* gi = sgrad + (I * NN + i) * 3;
-          const double vi = sval[I * NN + i];
-          for (int J = 0; J < 2; ++J) {
-            const double sJ = J == 0 ? 1.0 : -1.0;
-            const double* gj = sgrad + (J * NN + j) * 3;
-            const double vj = sval[J * NN + j];
-            const double t1 = 0.5 * (sI * (gj[0] * n0 + gj[1] * n1 + gj[2] * n2)) * vi;
-            const double t2 = 0.5 * (sJ * (gi[0] * n0 + gi[1] * n1 + gi[2] * n2)) * vj;
-            const double t3 = ch * vj * vi * (sI * sJ * nn2);
-            const double add = factor * (-t1 - t2 + t3);
-            if (J == I) D[t] = D[t] + add;
-            else O[t] = O[t] + add;
-          }
+          const double vi = sval[I * NN + i], ai = sA[I * NN + i];
+          const double vj = sval[I * NN + j], aj = sA[I * NN + j];
+          const double vo = sval[Jo * NN + j], ao = sA[Jo * NN + j];
+          D[t] = D[t] - (aj * vi + ai * vj) + pen * vj * vi;
+          O[t] = O[t] - ao * vi + ai * vo - pen * vo * vi;
         }
       }
       __syncwarp();
