@@ -40,6 +40,8 @@ EXPORTS = [
     "fg_bddc_params_default", "fg_bddc_create", "fg_bddc_numerical_setup", "fg_bddc_get_info",
     "fg_bddc_apply_device", "fg_bddc_solve", "fg_bddc_solve_device", "fg_bddc_destroy",
     "fg_batch_create", "fg_batch_run", "fg_batch_get_info", "fg_batch_destroy",
+    "fg_partition_create", "fg_partition_destroy", "fg_partition_get_info", "fg_partition_get_dof_import_sizes",
+    "fg_partition_get_dof_import", "fg_partition_assemble", "fg_partition_comm_device", "fg_partition_solve",
     "fg_request_footprint", "fg_server_create", "fg_server_submit", "fg_server_wait", "fg_server_take_solution",
     "fg_server_stats", "fg_server_destroy",
 ]
@@ -66,6 +68,18 @@ class MeshInfo(C.Structure):
         ("num_faces", C.c_int64), ("num_vefs", C.c_int64),
         ("unstructured", C.c_int32), ("max_cells_around_vertex", C.c_int32),
     ]
+
+
+class PartitionInfo(C.Structure):
+    _fields_ = [("num_parts", C.c_int32), ("num_local_dofs", C.c_int64), ("max_part_dofs", C.c_int64),
+                ("num_couplings", C.c_int64), ("nnz_full", C.c_int64), ("nnz_upper", C.c_int64),
+                ("num_dirichlet", C.c_int64)]
+
+
+class DofImportSizes(C.Structure):
+    _fields_ = [("num_dofs", C.c_int32), ("num_interior_dofs", C.c_int32), ("num_interface_dofs", C.c_int32),
+                ("num_rcv", C.c_int32), ("num_snd", C.c_int32), ("num_unpack", C.c_int32), ("num_pack", C.c_int32),
+                ("num_cells", C.c_int64), ("first_local_dof", C.c_int64)]
 
 
 class SolverParams(C.Structure):
@@ -234,6 +248,14 @@ def lib():
         "fg_ctx_kernel_launches": (i32, [vp, C.POINTER(C.c_int64)]),
         "fg_mesh_create_structured": (i32, [vp, i32, vp, vp, vp, pp]),
         "fg_mesh_destroy": (i32, [vp]),
+        "fg_partition_create": (i32, [vp, vp, pp]),
+        "fg_partition_destroy": (i32, [vp]),
+        "fg_partition_get_info": (i32, [vp, C.POINTER(PartitionInfo)]),
+        "fg_partition_get_dof_import_sizes": (i32, [vp, i32, C.POINTER(DofImportSizes)]),
+        "fg_partition_get_dof_import": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "fg_partition_assemble": (i32, [vp, vp, pp]),
+        "fg_partition_comm_device": (i32, [vp, vp]),
+        "fg_partition_solve": (i32, [vp, vp, vp, vp, vp]),
         "fg_mesh_create_unstructured": (i32, [vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp, vp, vp, pp]),
         "fg_mesh_read_gid": (i32, [vp, C.c_char_p, C.c_char_p, pp]),
         "fg_mesh_get_info": (i32, [vp, C.POINTER(MeshInfo)]),

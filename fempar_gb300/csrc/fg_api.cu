@@ -401,6 +401,7 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
   fg_status s = upload_tables(ctx, sp->tab, sp->dtab);
   if (mesh->unst) {
     // explicit nodes and cells around them; the solver runs on the explicit-column SELL layout
+    sp->explicit_nodes = true;
     if (s == FG_OK) s = uspace_number_dofs(sp);
     if (s == FG_OK) s = uspace_build_pattern(sp);
     sp->layout = FG_LAYOUT_SELL;

@@ -588,7 +588,7 @@ static fg_status launch_poisson(fg_system* sys) {
   FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
   if (sp->dg) return dg_assemble_rows(sys);
-  if (sp->mesh->unst) return usystem_scatter(sys);
+  if (sp->explicit_nodes) return usystem_scatter(sys);
   if (n > 0) {
     constexpr int CAP = P == 1 ? 32 : (P == 2 ? 128 : 512);
     k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,
@@ -810,7 +810,7 @@ static fg_status launch_elasticity(fg_system* sys) {
       sys->integ.nu, src, sys->d_elmat, sys->d_elvec);
   FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
-  if (sp->mesh->unst) return usystem_scatter(sys);
+  if (sp->explicit_nodes) return usystem_scatter(sys);
   if (n > 0) {
     constexpr int CAP = P == 1 ? 128 : 512;  // (2P+1)^3 * 3 box entries
     k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,

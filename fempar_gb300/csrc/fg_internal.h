@@ -156,6 +156,9 @@ struct fg_space {
   int64_t* d_ncl = nullptr;       // (cell << 6 | local node), ascending per node
   int max_ncells = 0;             // most cells around one node
   int row_cap = 0;                // power of two >= the longest row
+  // explicit node table (unstructured meshes, partitioned spaces): row gather through the
+  // cells around each node instead of the lattice
+  bool explicit_nodes = false;
   // discontinuous Galerkin space (fg_space_create_dg): cell-interior dofs, face neighbours
   bool dg = false;
   int32_t* d_dgnbr = nullptr;     // 6*ncells: neighbour across local face lf, -1 on the boundary
@@ -219,6 +222,7 @@ fg_status umesh_build_topology(fg_mesh* m, int64_t nb, const int64_t* bptr, cons
                                const int32_t* bset);
 fg_status umesh_export_vefs(fg_mesh* m, int32_t* cell_vefs, int32_t* vef_sets);
 fg_status uspace_number_dofs(fg_space* sp);
+fg_status uspace_build_adjacency(fg_space* sp);
 fg_status uspace_build_pattern(fg_space* sp);
 fg_status uspace_export_dof_map(fg_space* sp, int32_t* out_host);
 fg_status uspace_dirichlet_coords(fg_space* sp, double* d_xyz);

@@ -604,7 +604,15 @@ fg_status uspace_number_dofs(fg_space* sp) {
   FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   dev_free(ctx, cf);
   dev_free(ctx, cd);
-  // cells around every node, ascending
+  FG_TRY(uspace_build_adjacency(sp));
+  ctx->launches += 4;
+  return FG_OK;
+}
+
+// cells around every node (nlat nodes, the cell node table d_cellnode), ascending
+fg_status uspace_build_adjacency(fg_space* sp) {
+  fg_ctx* ctx = sp->mesh->ctx;
+  const int64_t nc = sp->mesh->ncells, nn = sp->tab.nn;
   {
     const int64_t ne = nc * nn, n = sp->nlat;
     FG_TRY(dev_alloc(ctx, (void**)&sp->d_nptr, sizeof(int64_t) * (n + 1)));
@@ -624,7 +632,7 @@ fg_status uspace_number_dofs(fg_space* sp) {
     FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     dev_free(ctx, cur);
   }
-  ctx->launches += 7;
+  ctx->launches += 3;
   return FG_OK;
 }
 

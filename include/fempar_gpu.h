@@ -294,6 +294,54 @@ typedef struct {
 fg_status fg_system_error_norms(fg_system* sys, const double* x, int32_t x_on_device, int32_t fn,
                                 const double* fn_param, double* cell_sq_energy, fg_error_norms* out);
 
+/* Partitioned assembly: the structured mesh of a continuous space split into
+ * np0 x np1 x np2 box parts (cells per direction divisible by the parts) as FEMPAR's parallel
+ * FE space does for its tasks -- local cells, local dof numbering, interface couplings with the
+ * reference's owner rule, dof_import (nearest-neighbour exchange lists) and the
+ * interior-then-interface renumbering -- with all parts resident on this context's device.
+ * Replaces par_fe_space_t%generate_global_dof_numbering / compute_dof_import
+ * (Sources/Lib/Integration/FESpace/sbm_par_fe_space.i90:425-470,707-793,1877-2034,2737-2853),
+ * dof_import_t (Sources/Lib/LinearAlgebra/Vector/dof_import.f90:102-213,365-421). */
+typedef struct fg_partition fg_partition;
+typedef struct {
+  int32_t num_parts;
+  int64_t num_local_dofs;    /* all parts' local free dofs (interface dofs once per part) */
+  int64_t max_part_dofs;
+  int64_t num_couplings;     /* interface columns over all parts */
+  int64_t nnz_full;          /* entries of the subassembled matrices */
+  int64_t nnz_upper;         /* their upper-triangle entries (symmetric-storage export) */
+  int64_t num_dirichlet;     /* strong Dirichlet dofs (global ids shared by every part) */
+} fg_partition_info;
+typedef struct {
+  int32_t num_dofs, num_interior_dofs, num_interface_dofs;
+  int32_t num_rcv, num_snd, num_unpack, num_pack;
+  int64_t num_cells;
+  int64_t first_local_dof;   /* offset of the part in the concatenated local-dof vectors */
+} fg_dof_import_sizes;
+fg_status fg_partition_create(fg_space* space, const int32_t num_parts_x_dir[3], fg_partition** out);
+fg_status fg_partition_destroy(fg_partition* partition);
+fg_status fg_partition_get_info(fg_partition* partition, fg_partition_info* info);
+/* dof_import_t of part part_id (1-based): sizes, then the arrays (1-based like the reference;
+ * any pointer may be NULL): l2g = global free dof id of each local dof, weight, list_rcv,
+ * rcv_ptrs (num_rcv+1), unpack_idx, list_snd, snd_ptrs (num_snd+1), pack_idx, and the part's
+ * cells (global ids, 0-based) in local order. */
+fg_status fg_partition_get_dof_import_sizes(fg_partition* partition, int32_t part_id, fg_dof_import_sizes* sizes);
+fg_status fg_partition_get_dof_import(fg_partition* partition, int32_t part_id, int32_t* l2g, double* weight,
+                                      int32_t* list_rcv, int32_t* rcv_ptrs, int32_t* unpack_idx,
+                                      int32_t* list_snd, int32_t* snd_ptrs, int32_t* pack_idx, int64_t* cells);
+/* Subassembled local systems of every part (block-diagonal matrix over the concatenated local
+ * dofs; each part's rhs sums only its own cells): the assembler of par_fe_space_t.
+ * Export/SpMV through the usual fg_system_* calls on the concatenated local space. */
+fg_status fg_partition_assemble(fg_partition* partition, const fg_integrand* integrand, fg_system** out);
+/* x (device, concatenated local dofs) <- comm(x): subassembled -> assembled interface values
+ * (par_scalar_array_t%comm, Sources/Lib/LinearAlgebra/Vector/par_scalar_array.f90:498-533). */
+fg_status fg_partition_comm_device(fg_partition* partition, double* x);
+/* Partitioned (Jacobi-)PCG on a subassembled system: SpMV + comm, weighted dots
+ * (par_scalar_array.f90:303-345), res_res criterion; x_global (host, num_free of the global
+ * space) receives the owners' values. */
+fg_status fg_partition_solve(fg_partition* partition, fg_system* subassembled, const fg_solver_params* params,
+                             double* x_global, fg_solve_info* info);
+
 /* ---------------------------------------------------------------------------------------
  * BDDC preconditioner (two levels: box subdomains of cells and a coarse problem).
  * Replaces mlbddc_t (Sources/Lib/LinearAlgebra/Preconditioner/mlbddc.f90,

@@ -1,0 +1,112 @@
+"""Partitioned dof numbering and dof_import (oracle restatement of par_fe_space_t /
+dof_import_t), and the nearest-neighbour exchange between processes (gloo ranks on CPU).
+
+Checks: each interface dof has exactly one owner (the weights of its copies sum to 1);
+interface dofs are numbered after the interior ones; every part's pack list for a neighbour
+has the size of the neighbour's unpack list for it; comm of the parts' subassembled right-hand
+sides equals the global right-hand side (1e-15 of its max), sequentially and through
+``neighbours_exchange`` between 2 and 4 processes.
+"""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+import oracle as O
+import partition as PT
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+CASES = [((4, 4, 2), (2, 2, 1), 1), ((4, 6, 4), (2, 3, 2), 2), ((6, 4, 4), (3, 2, 2), 3), ((4, 2, 2), (2, 1, 1), 2)]
+
+
+def problem(n, order, kind=O.POISSON):
+    rng = np.random.default_rng(sum(n) + order)
+    if kind == O.ELASTICITY:
+        return O.Problem(n, order=order, kind=O.ELASTICITY, dirichlet_ids=[1, 3, 5, 7, 13, 15, 17, 19, 25],
+                         cell_coef=np.exp(rng.normal(size=int(np.prod(n)))), source_fn=O.FN_CONST,
+                         fn_param=[0.0, 0.0, -1.0])
+    return O.Problem(n, order=order, source_fn=O.FN_SHARP_WAVE, boundary_fn=O.FN_SHARP_WAVE,
+                     fn_param=[20.0, 0.3, -0.05, -0.05, -0.05], cell_coef=np.exp(rng.normal(size=int(np.prod(n)))))
+
+
+def subassembled_rhs(P, parts):
+    dm = P.dof_map()
+    out = []
+    for part in parts:
+        g2l = {int(g): i for i, g in enumerate(part["l2g"])}
+        b = np.zeros(part["num_dofs"])
+        for c in part["cells"]:
+            _, ev = P.elmat(c)
+            for a in range(P.nd):
+                if dm[c, a] > 0:
+                    b[g2l[int(dm[c, a])]] += ev[a]
+        out.append(b)
+    return out
+
+
+@pytest.mark.parametrize("n,nparts,order", CASES)
+@pytest.mark.parametrize("kind", [O.POISSON, O.ELASTICITY])
+def test_partition_invariants_and_comm(n, nparts, order, kind):
+    if kind == O.ELASTICITY and order == 3:
+        pytest.skip("elasticity is built for orders 1-2")
+    P = problem(n, order, kind)
+    parts = PT.build(P, nparts)
+    w = np.zeros(P.nfree)
+    for part in parts:
+        np.add.at(w, part["l2g"] - 1, part["weight"])
+        itf = set(part["pack_idx"]) | set(part["unpack_idx"])
+        assert all(v > part["num_interior"] for v in itf)
+        assert len(itf) == part["num_interface"]
+    assert np.all(w == 1.0)
+    for p, part in enumerate(parts, start=1):
+        for k, q in enumerate(part["list_snd"]):
+            other = parts[q - 1]
+            kk = other["list_rcv"].index(p)
+            assert part["snd_ptrs"][k + 1] - part["snd_ptrs"][k] == other["rcv_ptrs"][kk + 1] - other["rcv_ptrs"][kk]
+    full = PT.comm(parts, subassembled_rhs(P, parts))
+    ob = P.rhs()
+    for part, f in zip(parts, full):
+        assert np.max(np.abs(f - ob[part["l2g"] - 1])) <= 1e-15 * np.max(np.abs(ob)) * 10
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, n, nparts, order, out):
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (root, os.path.join(root, "oracle")):
+        sys.path.insert(0, p)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import oracle as Ol
+    import partition as PTl
+    from fempar_gb300.partition import neighbours_exchange
+    P = problem(n, order)
+    parts = PTl.build(P, nparts)
+    mine = parts[rank]
+    b = torch.from_numpy(subassembled_rhs(P, parts)[rank])
+    neighbours_exchange(dist, mine, b)
+    ob = P.rhs()
+    out[rank] = float(np.max(np.abs(b.numpy() - ob[mine["l2g"] - 1])) / np.max(np.abs(ob)))
+    dist.barrier()
+    dist.destroy_process_group()
+    del Ol
+
+
+@pytest.mark.parametrize("world,n,nparts,order", [(2, (4, 2, 2), (2, 1, 1), 2), (4, (4, 4, 2), (2, 2, 1), 2)])
+def test_neighbours_exchange_between_processes(world, n, nparts, order):
+    port = _free_port()
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_rank_main, args=(world, port, n, nparts, order, out), nprocs=world, join=True)
+    for r in range(world):
+        assert out[r] <= 1e-14, (r, out[r])
