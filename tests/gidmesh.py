@@ -131,3 +131,126 @@ def write_gid(path, mesh, c_order=True):
     lines += ["end vefs", ""]
     with open(path, "w") as f:
         f.write("\n".join(lines))
+
+
+def cube_in_cube(refine=0, inner=(0.3, 0.7), seed=None):
+    """The classic irregular hexahedral mesh: an inner cube inside the unit cube joined to it
+    by 6 frustum cells (inner corners lie in 4 cells, outer corners in 3), split `refine`
+    times into 8 by the trilinear map of each cell.  Boundary: the outer faces, edges and
+    corners with set id 1.  With `seed`, cells are shuffled and listed in random orientations."""
+    lo, hi = inner
+    verts = {}
+
+    def vid(key, x):
+        if key not in verts:
+            verts[key] = (len(verts) + 1, np.array(x, dtype=float))
+        return verts[key][0]
+
+    def outer(b):
+        return vid(("o",) + tuple(b), [float(v) for v in b])
+
+    def inn(b):
+        return vid(("i",) + tuple(b), [lo + (hi - lo) * v for v in b])
+
+    cells = [[inn([(k >> 0) & 1, (k >> 1) & 1, (k >> 2) & 1]) for k in range(8)]]
+    for d in range(3):
+        for s in (0, 1):
+            cell = []
+            for k in range(8):
+                b = [(k >> 0) & 1, (k >> 1) & 1, (k >> 2) & 1]
+                layer_outer = (b[d] == 0) if s == 0 else (b[d] == 1)
+                bb = list(b)
+                bb[d] = s
+                cell.append(outer(bb) if layer_outer else inn(bb))
+            cells.append(cell)
+    bfaces = []
+    for d in range(3):
+        a, c = [e for e in range(3) if e != d]
+        for s in (0, 1):
+            q = []
+            for (u, v) in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                b = [0, 0, 0]
+                b[d], b[a], b[c] = s, u, v
+                q.append(outer(b))
+            bfaces.append(q)
+    bedges = []
+    for d in range(3):
+        a, c = [e for e in range(3) if e != d]
+        for u in (0, 1):
+            for v in (0, 1):
+                b0, b1 = [0, 0, 0], [0, 0, 0]
+                b0[a] = b1[a] = u
+                b0[c] = b1[c] = v
+                b1[d] = 1
+                bedges.append([outer(b0), outer(b1)])
+    bverts = [[outer([(k >> 0) & 1, (k >> 1) & 1, (k >> 2) & 1])] for k in range(8)]
+    coords = {v[0]: v[1] for v in verts.values()}
+    for _ in range(refine):
+        newc = []
+        mid = {}
+
+        def key_mid(ids):
+            return tuple(sorted(ids))
+
+        def point(ids):
+            k = key_mid(ids)
+            if k not in mid:
+                nid = len(coords) + 1
+                coords[nid] = np.mean([coords[i] for i in ids], axis=0)
+                mid[k] = nid
+            return mid[k]
+
+        for cell in cells:
+            # trilinear points at parametric (0, 1/2, 1) per direction
+            X = np.array([coords[v] for v in cell])
+
+            def tri(t):
+                w = [(1 - t[0], t[0]), (1 - t[1], t[1]), (1 - t[2], t[2])]
+                return sum(w[0][k & 1] * w[1][(k >> 1) & 1] * w[2][(k >> 2) & 1] * X[k] for k in range(8))
+
+            grid = {}
+            for i in range(3):
+                for j in range(3):
+                    for k in range(3):
+                        t = (i / 2, j / 2, k / 2)
+                        # the vertices of the n-face holding the point name it, so cells that
+                        # share an edge or face share its midpoint
+                        span = [cell[b] for b in range(8)
+                                if all(t[d] == 0.5 or ((b >> d) & 1) == int(t[d]) for d in range(3))]
+                        if len(span) == 1:
+                            grid[(i, j, k)] = span[0]
+                        else:
+                            nid = point(span)
+                            coords[nid] = tri(t)
+                            grid[(i, j, k)] = nid
+            for ci in range(2):
+                for cj in range(2):
+                    for ck in range(2):
+                        newc.append([grid[(ci + (b & 1), cj + ((b >> 1) & 1), ck + ((b >> 2) & 1))] for b in range(8)])
+        nb = []
+        for q in bfaces:
+            e = [point([q[a], q[(a + 1) % 4]]) for a in range(4)]
+            c = point(list(q))
+            nb += [[q[0], e[0], c, e[3]], [e[0], q[1], e[1], c], [c, e[1], q[2], e[2]], [e[3], c, e[2], q[3]]]
+        bfaces = nb
+        ne = []
+        for e in bedges:
+            m = point(e)
+            ne += [[e[0], m], [m, e[1]]]
+        bedges = ne
+        cells = newc
+    coords_arr = np.array([coords[i] for i in range(1, len(coords) + 1)])
+    cells = np.array(cells, dtype=np.int32)
+    rng = np.random.default_rng(seed) if seed is not None else None
+    if rng is not None:
+        orients = cube_orientations()
+        cells = np.array([[c[m] for m in orients[rng.integers(len(orients))]] for c in cells], dtype=np.int32)
+        cells = cells[rng.permutation(len(cells))]
+    given = [(q, 1) for q in bfaces] + [(e, 1) for e in bedges] + [(v, 1) for v in bverts]
+    bptr = np.zeros(len(given) + 1, dtype=np.int64)
+    bptr[1:] = np.cumsum([len(g[0]) for g in given])
+    return {"dim": 3, "coords": coords_arr, "cells": cells, "cell_set": np.zeros(len(cells), np.int32),
+            "cell_geo": np.ones(len(cells), np.int32), "bvef_ptr": bptr,
+            "bvef_verts": np.array([v for g in given for v in g[0]], dtype=np.int32),
+            "bvef_set": np.array([g[1] for g in given], dtype=np.int32),
+            "bvef_geo": np.ones(len(given), np.int32)}

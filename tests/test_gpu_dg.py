@@ -114,3 +114,16 @@ def test_dg_rejects_coefficients(fg, ctx):
         fg.FEAffineOperator(sp, fg.PoissonIntegration(cell_coef=np.ones(8) * 2.0)).compute()
     with pytest.raises(FGError):
         fg.MLBDDC(fg.FEAffineOperator(sp, fg.PoissonIntegration()).compute(), nsub=(1, 1, 1))
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_dg_irregular_mesh_parity(fg, ctx, order):
+    m = gidmesh.cube_in_cube(refine=1, seed=7 + order)
+    P = O.UProblem(m, order=order, dirichlet_ids=(), formulation=O.DG, source_fn=O.FN_SHARP_WAVE,
+                   boundary_fn=O.FN_SHARP_WAVE, fn_param=SHARP)
+    tri = fg.SerialTriangulation.from_arrays(ctx, m["coords"], m["cells"], m["bvef_ptr"], m["bvef_verts"],
+                                             m["bvef_set"])
+    sp = fg.SerialFESpace(tri, order=order, dg=True)
+    op = fg.FEAffineOperator(sp, fg.PoissonIntegration(source_fn=O.FN_SHARP_WAVE, boundary_fn=O.FN_SHARP_WAVE,
+                                                        fn_param=SHARP)).compute()
+    check(fg, P, sp, op)

@@ -182,3 +182,26 @@ def test_bad_meshes_and_bddc_rejected(fg, ctx, tmp_path):
     op = fg.FEAffineOperator(sp, fg.PoissonIntegration(source_fn=O.FN_CONST, fn_param=[1.0])).compute()
     with pytest.raises(FGError):
         fg.MLBDDC(op, nsub=(1, 1, 1))
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_irregular_mesh_parity(fg, ctx, order):
+    """The cube-in-cube mesh refined twice (vertices in 3, 4, 6 and 8 cells), shuffled cells in
+    random orientations: vefs, dof map and pattern bit-exact, entries and solution as above."""
+    m = gidmesh.cube_in_cube(refine=2, seed=order)
+    P = O.UProblem(m, order=order, dirichlet_ids=(1,), source_fn=O.FN_SHARP_WAVE, boundary_fn=O.FN_SHARP_WAVE,
+                   fn_param=SHARP)
+    tri = device_mesh(fg, ctx, m)
+    cv, vs = tri.get_vefs()
+    assert np.array_equal(cv, P.cell_vefs()) and np.array_equal(vs, P.vef_sets())
+    sp = fg.SerialFESpace(tri, order=order, dirichlet_ids=[1])
+    assert np.array_equal(sp.get_dof_map(), P.dof_map())
+    op = fg.FEAffineOperator(sp, fg.PoissonIntegration(source_fn=O.FN_SHARP_WAVE, boundary_fn=O.FN_SHARP_WAVE,
+                                                        fn_param=SHARP)).compute()
+    irp, ja, val = op.get_matrix()
+    assert_matrix_close(irp, ja, val, P)
+    ref = P.cg(precond=1, rtol=1e-13, maxit=20000)
+    s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
+    s.set_parameters_from_pl({"ILS_RTOL": 1e-13, "ILS_MAX_NUM_ITERATIONS": 20000})
+    x = s.solve()
+    assert np.linalg.norm(x - ref["x"]) <= 1e-10 * np.linalg.norm(ref["x"])

@@ -138,3 +138,12 @@ def test_unstructured_matches_structured_oracle_on_a_box():
     assert valu.keys() == vals.keys()
     d = max(abs(valu[k] - vals[k]) for k in valu)
     assert d < 1e-12 * max(abs(v) for v in vals.values())
+
+
+@pytest.mark.parametrize("refine", [0, 1, 2])
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_irregular_cube_in_cube_recovers_linear_solution(refine, order):
+    """Vertices in 3, 4, 6 and 8 cells; shuffled cells in random orientations."""
+    m = gidmesh.cube_in_cube(refine=refine, seed=refine + order)
+    _, e = exact_linear_errors(m, order)
+    assert e["l2_norm"] < 1e-10 and e["h1_seminorm"] < 1e-10 and e["linfty_norm"] < 1e-10
