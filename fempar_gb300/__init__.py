@@ -18,6 +18,8 @@ FG_FP64 = _lib.FG_FP64
 FG_MIXED = _lib.FG_MIXED
 FG_BDDC_WEIGHT_MULTIPLICITY = _lib.FG_BDDC_WEIGHT_MULTIPLICITY
 FG_BDDC_WEIGHT_STIFFNESS = _lib.FG_BDDC_WEIGHT_STIFFNESS
+FG_BDDC_HANDLER_STANDARD = _lib.FG_BDDC_HANDLER_STANDARD
+FG_BDDC_HANDLER_ELASTICITY = _lib.FG_BDDC_HANDLER_ELASTICITY
 
 ALL_BOUNDARY_IDS = list(range(1, 27))
 # polytope ids of the regions with x fixed at 0: vertices 1,3,5,7; y-edges 13,15; z-edges 17,19; face 25

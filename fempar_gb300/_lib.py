@@ -21,6 +21,7 @@ FG_FN_ZERO, FG_FN_CONST, FG_FN_SHARP_WAVE, FG_FN_LINEAR, FG_FN_QP_VALUES = 0, 1,
 FG_INPUTS_ON_DEVICE, FG_LEAN_SYSTEM, FG_FAST_INTEGRATION = 1, 2, 4
 FG_PREC_NONE, FG_PREC_JACOBI, FG_PREC_BDDC = 0, 1, 2
 FG_BDDC_WEIGHT_MULTIPLICITY, FG_BDDC_WEIGHT_STIFFNESS = 0, 1
+FG_BDDC_HANDLER_STANDARD, FG_BDDC_HANDLER_ELASTICITY = 0, 1
 FG_FP64, FG_MIXED = 0, 1
 FG_RES_RES, FG_RES_RHS, FG_DELTA_RHS, FG_DELTA_DELTA, FG_RES_NRMGIVEN_RHS_NRMGIVEN, FG_RES_NRMGIVEN_RES_NRMGIVEN = range(6)
 
@@ -131,6 +132,7 @@ class BddcParams(C.Structure):
         ("use_edges", C.c_int32),
         ("use_faces", C.c_int32),
         ("weighting", C.c_int32),
+        ("coarse_handler", C.c_int32),
     ]
 
 

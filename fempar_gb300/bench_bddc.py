@@ -68,7 +68,7 @@ def run_jacobi_only(n, rtol=1e-8, device=0, precisions=("mixed",)):
 
 
 def run(n=32, nsub=8, jitter=0.0, rtol=1e-8, device=0, faces=False, weighting=L.FG_BDDC_WEIGHT_MULTIPLICITY,
-        jacobi=True):
+        jacobi=True, handler=L.FG_BDDC_HANDLER_STANDARD):
     rng = np.random.Generator(np.random.PCG64(SEED))
     xyz = perturbed_vertices(n, 0.15, rng)
     E = np.exp(rng.normal(0.0, 1.5, size=n ** 3))
@@ -82,7 +82,9 @@ def run(n=32, nsub=8, jitter=0.0, rtol=1e-8, device=0, faces=False, weighting=L.
     t_asm = (time.perf_counter() - t0) * 1e3
     cuts = bddc_cuts((n, n, n), (nsub, nsub, nsub), jitter=jitter, seed=SEED)
     t0 = time.perf_counter()
-    M = MLBDDC(op, nsub=(nsub,) * 3, cuts=cuts, use_faces=faces, weighting=weighting)
+    rigid = handler == L.FG_BDDC_HANDLER_ELASTICITY
+    M = MLBDDC(op, nsub=(nsub,) * 3, cuts=cuts, use_edges=not rigid, use_faces=faces, weighting=weighting,
+               coarse_handler=handler)
     t_create = (time.perf_counter() - t0) * 1e3
     info = M.info()
     t0 = time.perf_counter()
@@ -90,6 +92,8 @@ def run(n=32, nsub=8, jitter=0.0, rtol=1e-8, device=0, faces=False, weighting=L.
     t_num = (time.perf_counter() - t0) * 1e3
     out = {"metric": "BDDC elasticity Q2: DOF/s to 1e-8 (assembly + BDDC numerical setup + PCG)",
            "n": n, "nsub": [nsub] * 3, "jitter": jitter, "faces": faces,
+           "coarse_handler": "elasticity (vertices + rigid-body face functionals)" if rigid
+           else "standard (vertices + edge/face averages)",
            "weighting": "stiffness" if weighting == L.FG_BDDC_WEIGHT_STIFFNESS else "multiplicity",
            "dofs": sp.num_free_dofs,
            "max_local_dofs": info["max_local_dofs"], "coarse_dofs": info["num_coarse_dofs"],
@@ -106,7 +110,8 @@ def run(n=32, nsub=8, jitter=0.0, rtol=1e-8, device=0, faces=False, weighting=L.
         runs += [("jacobi_mixed", "mixed", "jacobi"), ("jacobi_fp64", "fp64", "jacobi")]
     for name, prec, M_ in runs:
         s = IterativeLinearSolver().set_type_from_string("CG").set_operators(op, M_)
-        s.set_parameters_from_pl({"ILS_RTOL": rtol, "ILS_MAX_NUM_ITERATIONS": 200000, "PRECISION": prec})
+        s.set_parameters_from_pl({"ILS_RTOL": rtol, "PRECISION": prec,
+                                  "ILS_MAX_NUM_ITERATIONS": 5000 if name.startswith("bddc") else 200000})
         t0 = time.perf_counter()
         x = s.solve()
         wall = (time.perf_counter() - t0) * 1e3
@@ -133,6 +138,9 @@ def main():
     ap.add_argument("--multiplicity", action="store_true",
                     help="1/(subdomains around) weights (the reference's standard handler); "
                          "default: diag(A_i)/sum diag(A_j)")
+    ap.add_argument("--elasticity-handler", action="store_true",
+                    help="the reference's elasticity coarse handler: vertices and six rigid-body "
+                         "functionals per face, no edge constraints (implies --faces)")
     ap.add_argument("--no-jacobi", action="store_true")
     ap.add_argument("--jacobi-only", action="store_true",
                     help="no BDDC: lean assembly + mixed Jacobi-PCG (e.g. --n 96, the cfg size)")
@@ -143,8 +151,9 @@ def main():
         print(json.dumps(run_jacobi_only(args.n)), flush=True)
         return
     wt = L.FG_BDDC_WEIGHT_MULTIPLICITY if args.multiplicity else L.FG_BDDC_WEIGHT_STIFFNESS
-    print(json.dumps(run(args.n, args.nsub, args.jitter, faces=args.faces, weighting=wt,
-                         jacobi=not args.no_jacobi)), flush=True)
+    handler = L.FG_BDDC_HANDLER_ELASTICITY if args.elasticity_handler else L.FG_BDDC_HANDLER_STANDARD
+    print(json.dumps(run(args.n, args.nsub, args.jitter, faces=args.faces or args.elasticity_handler, weighting=wt,
+                         jacobi=not args.no_jacobi, handler=handler)), flush=True)
 
 
 if __name__ == "__main__":

@@ -13,21 +13,24 @@
 // How the constrained Neumann problem is solved (our design, not the reference's
 // augmented-matrix direct solve): local dofs are ordered [I | E | V] (interior, interface
 // non-vertex, vertex).  Vertex dofs are primal variables and are eliminated outright; the
-// remaining constraints (edge / face averages, rows C_e over the E dofs) are appended as
-// extra rows.  One partial FP64 Cholesky of the first nr = nI + nE columns of
+// remaining constraints (edge / face functionals, rows [C_e C_eV] over the E and V dofs)
+// are appended as extra rows.  One partial FP64 Cholesky of the first nr = nI + nE columns of
 //        [ K_rr   .    .  ]
 //        [ K_Vr  K_VV  .  ]          (lower triangle, N = m + ne rows)
-//        [ C_e    0    0  ]
+//        [ C_e   C_eV  0  ]
 // gives the factor L of K_rr, the rows L_V = K_Vr L^-T and L_e = C_e L^-T, and in the
-// trailing block the Schur complements K_VV - K_Vr K_rr^-1 K_rV, -C_e K_rr^-1 K_rV and
-// -S_e = -C_e K_rr^-1 C_e^T.  The local coarse matrix Phi^T K Phi follows from those
+// trailing block the Schur complements K_VV - K_Vr K_rr^-1 K_rV, -T = C_eV - C_e K_rr^-1 K_rV
+// and -S_e = -C_e K_rr^-1 C_e^T.  The local coarse matrix Phi^T K Phi follows from those
 // without forming Phi, and the apply needs one forward solve before the coarse solve and
 // one backward solve after it:
 //   z = L^-1 g_r,  f_Pi = [g_V - L_V z + H^T L_e z ; S_e^-1 L_e z]     (H = S_e^-1 T)
-//   s = z - L_V^T u_V,  mu = S_e^-1 (L_e s - u_e),  w_r = L^-T (s - L_e^T mu),  w_V = u_V
+//   s = z - L_V^T u_V,  mu = S_e^-1 (L_e s - u_e + C_eV u_V),  w_r = L^-T (s - L_e^T mu),  w_V = u_V
+// (C_eV, the constraint weights on vertex dofs, is zero for the standard handler's averages
+// and nonzero for the elasticity handler's face functionals.)
 // (u = the coarse solution restricted to the subdomain).  The coarse matrix is inverted
 // by the same partial Cholesky on [[K_c, I], [I, 0]] whose trailing block is -K_c^-1.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -46,12 +49,14 @@ struct BSub {
   int64_t roff;  // rows V|e of the factor, row-major nP x nr
   int64_t loff;  // local dofs (m): solver-vector index, order I | E | V
   int64_t woff;  // interface positions (nE + nV): weights, contributions
-  int64_t eoff;  // E dofs (nE): constraint index (-1 none), constraint weight, z_E
+  int64_t eoff;  // E dofs (nE): z_E
   int64_t poff;  // local coarse dofs (nP = nV + ne): global coarse index, f_Pi
   int64_t koff;  // local coarse matrix nP x nP
   int64_t goff;  // S_e^-1 (ne x ne) then H (ne x nV)
   int64_t boff;  // box map: box lattice nodes x ncomp -> local index (-1 not free)
-  int N, m, nI, nE, nV, ne, nr, nP;
+  int64_t qoff;  // constraint entries (nq): row e, local column (E or V dof), weight
+  int64_t cvoff; // C_eV, ne x nV row-major
+  int N, m, nI, nE, nV, ne, nr, nP, nq;
   int c0[3], c1[3];
 };
 
@@ -82,8 +87,11 @@ struct fg_bddc {
   double* dDiag = nullptr;
   double* dC = nullptr;
   float* dC32 = nullptr;
-  int32_t* dEc = nullptr;
-  double* dEw = nullptr;
+  int32_t* dQrow = nullptr;  // constraint entries of all subdomains
+  int32_t* dQcol = nullptr;
+  double* dQw = nullptr;
+  double* dCv = nullptr;     // C_eV of all subdomains
+  float* dCv32 = nullptr;
   double* dZ = nullptr;
   float* dZ32 = nullptr;
   int32_t* dPc = nullptr;
@@ -253,8 +261,9 @@ __device__ bool chol_partial_cta(double* A, int64_t lda, int N, int ncols, CholS
 // sum in that order), constraint rows, and the interface diagonal.  One CTA per subdomain.
 __global__ void __launch_bounds__(256)
     k_bddc_assemble(const BSub* __restrict__ subs, const double* __restrict__ E, int nx, int ny, int p, int nn, int nd,
-                    int ncomp, const int32_t* __restrict__ box, const int32_t* __restrict__ ec,
-                    const double* __restrict__ ew, double* __restrict__ A, double* __restrict__ diag) {
+                    int ncomp, const int32_t* __restrict__ box, const int32_t* __restrict__ qrow,
+                    const int32_t* __restrict__ qcol, const double* __restrict__ qw, double* __restrict__ A,
+                    double* __restrict__ diag) {
   const BSub S = subs[blockIdx.x];
   double* As = A + S.aoff;
   const int64_t N = S.N;
@@ -280,10 +289,8 @@ __global__ void __launch_bounds__(256)
         }
         __syncthreads();
       }
-  for (int k = threadIdx.x; k < S.nE; k += blockDim.x) {
-    int ce = ec[S.eoff + k];
-    if (ce >= 0) As[(S.m + ce) + (int64_t)(S.nI + k) * N] = ew[S.eoff + k];
-  }
+  for (int t = threadIdx.x; t < S.nq; t += blockDim.x)
+    As[(S.m + qrow[S.qoff + t]) + (int64_t)qcol[S.qoff + t] * N] = qw[S.qoff + t];
   for (int k = threadIdx.x; k < S.nE + S.nV; k += blockDim.x) {
     int i = S.nI + k;
     diag[S.woff + k] = As[i + (int64_t)i * N];
@@ -714,9 +721,9 @@ __global__ void __launch_bounds__(256)
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_bddc_neumann_bwd(const BSub* __restrict__ subs, const double* __restrict__ A, const float* __restrict__ F,
-                       const T* __restrict__ R, const T* __restrict__ G, const int32_t* __restrict__ pc,
-                       const T* __restrict__ uc, const T* __restrict__ zE, const double* __restrict__ w,
-                       T* __restrict__ contrib) {
+                       const T* __restrict__ R, const T* __restrict__ G, const T* __restrict__ Cv,
+                       const int32_t* __restrict__ pc, const T* __restrict__ uc, const T* __restrict__ zE,
+                       const double* __restrict__ w, T* __restrict__ contrib) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* x = reinterpret_cast<T*>(smraw);
   __shared__ T uP[kMaxNv + kMaxNe], cm[kMaxNe], mu[kMaxNe];
@@ -739,7 +746,11 @@ __global__ void __launch_bounds__(256)
     T acc = T(0);
     for (int i = lane; i < nr; i += 32) acc += row[i] * x[i];
     acc = warp_sum(acc);
-    if (lane == 0) cm[k] = acc - uP[nV + k];
+    if (lane == 0) {
+      const T* cv = Cv + S.cvoff + (int64_t)k * nV;
+      for (int v = 0; v < nV; ++v) acc += cv[v] * uP[v];
+      cm[k] = acc - uP[nV + k];
+    }
   }
   __syncthreads();
   const T* Gi = G + S.goff;
@@ -906,8 +917,113 @@ static void pairs_to_csr(int64_t nkeys, const std::vector<std::pair<int64_t, int
 
 struct AxisInfo {
   std::vector<char> on_cut, plane;
-  std::vector<int> idx;
+  std::vector<int> idx;   // plane index on slab planes, else the slab that contains the position
+  std::vector<int> slab;  // the slab that contains the position (domain-boundary planes included)
 };
+
+// Face functionals of the elasticity coarse handler (sbm_elasticity_coarse_fe_handler.i90:
+// 180-381, strategy CI): for the face object `key` of a subdomain and rigid-body mode r_m
+// (translations e_1..e_3, rotations r4 = (y,-x,0), r5 = (-z,0,x), r6 = (0,z,-y) in the
+// coordinates themselves, :37-73), the constraint row of the local dof (node a, component c)
+// is (1/|F|) sum over the face's facets and their Gauss points of N_a r_m[c] w |J_F|, |F| the
+// face measure by the same rule.  Facets are the subdomain's own cell faces on the plane;
+// (p+1)^2 Gauss-Legendre points per facet on the bilinear map of its four vertices,
+// |J_F| = |dx/ds x dx/dt|.  Entries of dofs that are not free are dropped.
+// One change of basis: the rotations are taken about the face's centroid x_F and divided by
+// sqrt(|F|) (r4 = ((y - y_F), -(x - x_F), 0) / sqrt(|F|), ...).  Each is the reference's rotation
+// plus translations, scaled, so the six rows span the same space and the BDDC operator (which
+// depends on the constraints' span only) is the same; in the reference's coordinates the
+// rotation rows are nearly combinations of the translation rows far from the origin, and
+// S_e = C K^-1 C^T is too ill-conditioned for the FP32 factors.
+static void face_functionals(uint64_t key, int row0, const std::vector<int32_t>* cuts, const int* c0, const int* c1,
+                             const int* lo, const int* bn, const int* ncell, int p, int nc, const std::vector<double>& xyz,
+                             const int32_t* box, std::vector<int32_t>& qrow, std::vector<int32_t>& qcol,
+                             std::vector<double>& qw) {
+  const int a = (int)((key >> 60) & 3);
+  const int ia[3] = {(int)((key >> 40) & 0xFFFFF), (int)((key >> 20) & 0xFFFFF), (int)(key & 0xFFFFF)};
+  const int plane = cuts[a][ia[a]];                  // cell index of the plane along a
+  const int ca = plane == c0[a] ? c0[a] : c1[a] - 1;  // this subdomain's cells along a
+  const int side = plane == c0[a] ? 0 : 1;
+  const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;  // the face's axes, b < c
+  const int nq = p + 1;
+  std::vector<double> gx(nq), gw(nq);
+  gl_rule(nq, gx.data(), gw.data());
+  const int64_t nvx = ncell[0] + 1, nvy = ncell[1] + 1;
+  std::map<int, std::array<double, 6>> acc;  // local dof -> six integrals
+  double meas = 0.0, xF[3] = {0.0, 0.0, 0.0}, scale = 1.0;
+  // pass 0: the face measure and centroid; pass 1: the integrals
+  auto sweep = [&](int pass) {
+    for (int cc = c0[c]; cc < c1[c]; ++cc)
+      for (int cb = c0[b]; cb < c1[b]; ++cb) {
+        double V[2][2][3];
+        for (int v = 0; v < 2; ++v)
+          for (int u = 0; u < 2; ++u) {
+            int I3[3];
+            I3[a] = ca + side;
+            I3[b] = cb + u;
+            I3[c] = cc + v;
+            const int64_t vid = I3[0] + nvx * (I3[1] + nvy * I3[2]);
+            for (int d = 0; d < 3; ++d) V[u][v][d] = xyz[3 * vid + d];
+          }
+        for (int jt = 0; jt < nq; ++jt)
+          for (int is = 0; is < nq; ++is) {
+            const double s = gx[is], t = gx[jt];
+            const double fs[2] = {0.5 * (1 - s), 0.5 * (1 + s)}, ft[2] = {0.5 * (1 - t), 0.5 * (1 + t)};
+            double x[3], ds[3], dt[3];
+            for (int d = 0; d < 3; ++d) {
+              x[d] = ds[d] = dt[d] = 0.0;
+              for (int v = 0; v < 2; ++v)
+                for (int u = 0; u < 2; ++u) {
+                  x[d] += fs[u] * ft[v] * V[u][v][d];
+                  ds[d] += (u ? 0.5 : -0.5) * ft[v] * V[u][v][d];
+                  dt[d] += fs[u] * (v ? 0.5 : -0.5) * V[u][v][d];
+                }
+            }
+            const double nx = ds[1] * dt[2] - ds[2] * dt[1], ny = ds[2] * dt[0] - ds[0] * dt[2],
+                         nz = ds[0] * dt[1] - ds[1] * dt[0];
+            const double f = gw[is] * gw[jt] * std::sqrt(nx * nx + ny * ny + nz * nz);
+            if (pass == 0) {
+              meas += f;
+              for (int d = 0; d < 3; ++d) xF[d] += f * x[d];
+              continue;
+            }
+            // r_m[comp] at x (rotations about the centroid, scaled)
+            const double X = (x[0] - xF[0]) * scale, Y = (x[1] - xF[1]) * scale, Z = (x[2] - xF[2]) * scale;
+            const double r[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {Y, -X, 0}, {-Z, 0, X}, {0, Z, -Y}};
+            for (int j = 0; j <= p; ++j)
+              for (int i = 0; i <= p; ++i) {
+                double li, lj, dl;
+                lagrange_1d(p, i, s, li, dl);
+                lagrange_1d(p, j, t, lj, dl);
+                const double Nv = li * lj;
+                if (Nv == 0.0) continue;
+                int P3[3];
+                P3[a] = p * (ca + side);
+                P3[b] = p * cb + i;
+                P3[c] = p * cc + j;
+                const int64_t nb = (((int64_t)(P3[2] - lo[2]) * bn[1] + (P3[1] - lo[1])) * bn[0] + (P3[0] - lo[0])) * nc;
+                for (int comp = 0; comp < nc; ++comp) {
+                  const int ld = box[nb + comp];
+                  if (ld < 0) continue;
+                  auto& e = acc[ld];
+                  for (int m = 0; m < 6; ++m) e[m] += Nv * r[m][comp] * f;
+                }
+              }
+          }
+      }
+  };
+  sweep(0);
+  for (int d = 0; d < 3; ++d) xF[d] /= meas;
+  scale = 1.0 / std::sqrt(meas);
+  sweep(1);
+  for (int m = 0; m < 6; ++m)
+    for (auto& kv : acc)
+      if (kv.second[m] != 0.0) {
+        qrow.push_back(row0 + m);
+        qcol.push_back(kv.first);
+        qw.push_back(kv.second[m] / meas);
+      }
+}
 
 static fg_status bddc_symbolic(fg_bddc* B) {
   fg_space* sp = B->sys->space;
@@ -930,6 +1046,7 @@ static fg_status bddc_symbolic(fg_bddc* B) {
     ax[d].on_cut.assign(Ln, 0);
     ax[d].plane.assign(Ln, 0);
     ax[d].idx.assign(Ln, 0);
+    ax[d].slab.assign(Ln, 0);
     for (int k = 0; k <= ns[d]; ++k) {
       int X = p * B->cuts[d][k];
       ax[d].plane[X] = 1;
@@ -945,6 +1062,7 @@ static fg_status bddc_symbolic(fg_bddc* B) {
           if (p * B->cuts[d][q] == X) pk = q;
       }
       ax[d].idx[X] = pk;
+      ax[d].slab[X] = k;
     }
   }
   B->nsub = ns[0] * ns[1] * ns[2];
@@ -954,9 +1072,19 @@ static fg_status bddc_symbolic(fg_bddc* B) {
   std::vector<int32_t> ivec;
   std::vector<std::pair<int64_t, int64_t>> ipairs, cpairs;
   std::vector<std::pair<int32_t, int32_t>> kpairs_ij;  // (I, J) per K_Pi entry in pool order
-  std::vector<int32_t> h_loc, h_ec, h_pc, h_box;
-  std::vector<double> h_ew;
-  int64_t aoff = 0, foff = 0, roff = 0, loff = 0, woff = 0, eoff = 0, poff = 0, koff = 0, goff = 0, boff = 0;
+  std::vector<int32_t> h_loc, h_pc, h_box, h_qrow, h_qcol;
+  std::vector<double> h_qw, h_cv;
+  int64_t aoff = 0, foff = 0, roff = 0, loff = 0, woff = 0, eoff = 0, poff = 0, koff = 0, goff = 0, boff = 0,
+          cvoff = 0;
+  const bool rigid = B->prm.coarse_handler == FG_BDDC_HANDLER_ELASTICITY;
+  std::vector<double> xyz;  // vertex coordinates (elasticity handler's face integrals)
+  if (rigid) {
+    const int64_t nv = (int64_t)(me->n[0] + 1) * (me->n[1] + 1) * (me->n[2] + 1);
+    xyz.resize(3 * nv);
+    FG_CUDA_TRY(cudaMemcpyAsync(xyz.data(), me->d_coords, sizeof(double) * xyz.size(), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  }
   auto enc = [](int type, int a, int i0, int i1, int i2) -> uint64_t {
     return ((uint64_t)type << 62) | ((uint64_t)a << 60) | ((uint64_t)i0 << 40) | ((uint64_t)i1 << 20) | (uint64_t)i2;
   };
@@ -1006,11 +1134,15 @@ static fg_status bddc_symbolic(fg_bddc* B) {
                     if (!ax[d].plane[P3[d]]) a = d;
                   key = enc(1, a, ax[0].idx[X], ax[1].idx[Y], ax[2].idx[Z]);
                 } else {
+                  // a face: the cut plane and the slabs along the other two axes; points on the
+                  // domain boundary join the face (the same two subdomains share them)
                   cls = 1;
                   int a = 0;
                   for (int d = 0; d < 3; ++d)
                     if (ax[d].on_cut[P3[d]]) a = d;
-                  key = enc(2, a, ax[0].idx[X], ax[1].idx[Y], ax[2].idx[Z]);
+                  int id3[3];
+                  for (int d = 0; d < 3; ++d) id3[d] = d == a ? ax[d].idx[P3[d]] : ax[d].slab[P3[d]];
+                  key = enc(2, a, id3[0], id3[1], id3[2]);
                 }
               }
               for (int c = 0; c < nc; ++c) {
@@ -1041,11 +1173,23 @@ static fg_status bddc_symbolic(fg_bddc* B) {
         std::vector<int> lcnt;
         std::vector<std::pair<uint64_t, int>> lkeys;
         std::vector<int> econ(nE, -1);
+        std::vector<uint64_t> rfaces;  // elasticity handler: faces in order of first E dof
         for (int k = 0; k < nE; ++k) {
           const LD& d = dofs[nI + k];
           int type = (int)(d.key >> 62);
           bool use = (type == 1 && B->prm.use_edges) || (type == 2 && B->prm.use_faces);
           if (!use) continue;
+          if (rigid) {  // faces only (edges rejected at creation): six functionals, in mode order
+            if (lcon.find(std::make_pair(d.key, 0)) == lcon.end()) {
+              for (int mode = 0; mode < 6; ++mode) {
+                lcon[std::make_pair(d.key, mode)] = (int)lcnt.size();
+                lcnt.push_back(0);
+                lkeys.push_back(std::make_pair(d.key, mode));
+              }
+              rfaces.push_back(d.key);
+            }
+            continue;
+          }
           auto kc = std::make_pair(d.key, d.comp);
           auto it = lcon.find(kc);
           int ci;
@@ -1066,10 +1210,27 @@ static fg_status bddc_symbolic(fg_bddc* B) {
                     kMaxNe, kMaxNv);
           return FG_ERR_UNSUPPORTED;
         }
-        for (int k = 0; k < nE; ++k) {
-          h_ec.push_back(econ[k]);
-          h_ew.push_back(econ[k] >= 0 ? 1.0 / (double)lcnt[econ[k]] : 0.0);
+        // constraint entries (row, local column, weight) and C_eV
+        const int64_t q0 = (int64_t)h_qrow.size();
+        if (!rigid) {
+          for (int k = 0; k < nE; ++k)
+            if (econ[k] >= 0) {
+              h_qrow.push_back(econ[k]);
+              h_qcol.push_back(nI + k);
+              h_qw.push_back(1.0 / (double)lcnt[econ[k]]);
+            }
+        } else {
+          for (size_t f = 0; f < rfaces.size(); ++f)
+            face_functionals(rfaces[f], (int)(6 * f), B->cuts, S.c0, S.c1, lo, bn, me->n, p, nc, xyz,
+                             h_box.data() + b0, h_qrow, h_qcol, h_qw);
         }
+        S.qoff = q0;
+        S.nq = (int)((int64_t)h_qrow.size() - q0);
+        S.cvoff = cvoff;
+        h_cv.resize(cvoff + (int64_t)ne * nV, 0.0);
+        for (int64_t t = q0; t < (int64_t)h_qrow.size(); ++t)
+          if (h_qcol[t] >= nI + nE) h_cv[cvoff + (int64_t)h_qrow[t] * nV + (h_qcol[t] - nI - nE)] = h_qw[t];
+        cvoff += (int64_t)ne * nV;
         // local coarse dofs [V | e] -> global coarse ids
         std::vector<int32_t> cg;
         for (int k = 0; k < nV; ++k) {
@@ -1217,8 +1378,14 @@ static fg_status bddc_symbolic(fg_bddc* B) {
     B->stepped = !(e && e[0] == '0');
   }
   FG_TRY(upload(B, &B->dLoc, h_loc));
-  FG_TRY(upload(B, &B->dEc, h_ec));
-  FG_TRY(upload(B, &B->dEw, h_ew));
+  FG_TRY(upload(B, &B->dQrow, h_qrow));
+  FG_TRY(upload(B, &B->dQcol, h_qcol));
+  FG_TRY(upload(B, &B->dQw, h_qw));
+  FG_TRY(upload(B, &B->dCv, h_cv));
+  {
+    std::vector<float> cv32(h_cv.begin(), h_cv.end());
+    FG_TRY(upload(B, &B->dCv32, cv32));
+  }
   FG_TRY(upload(B, &B->dPc, h_pc));
   FG_TRY(upload(B, &B->dBox, h_box));
   FG_TRY(upload(B, &B->dIptr, iptr));
@@ -1317,7 +1484,8 @@ static fg_status bddc_numeric(fg_bddc* B) {
   const int ns = B->nsub;
   FG_CUDA_TRY(cudaMemsetAsync(B->dA, 0, sizeof(double) * (size_t)std::max<int64_t>(B->nA, 1), st));
   k_bddc_assemble<<<ns, 256, 0, st>>>(B->d_subs, sys->d_elmat, sp->mesh->n[0], sp->mesh->n[1], sp->order, sp->tab.nn,
-                                      sp->tab.nd, sp->ncomp, B->dBox, B->dEc, B->dEw, B->dA, B->dDiag);
+                                      sp->tab.nd, sp->ncomp, B->dBox, B->dQrow, B->dQcol, B->dQw, B->dA,
+                                      B->dDiag);
   if (B->nIface > 0)
     k_bddc_weights<<<nblk(B->nIface, 256), 256, 0, st>>>(B->nIface, B->dIptr, B->dIsrc, B->dDiag,
                                                          B->prm.weighting == FG_BDDC_WEIGHT_STIFFNESS, B->dW);
@@ -1425,7 +1593,8 @@ static fg_status bddc_apply_layout(fg_bddc* B, const double* r, double* z) {
     k_coarse_gemv<T><<<nblk(B->nC * 32, 256), 256, 0, st>>>(B->nC, Kinv, fc, uc);
     ctx->launches += 2;
   }
-  k_bddc_neumann_bwd<T><<<ns, 256, smR, st>>>(B->d_subs, B->dA, B->dF, R, G, B->dPc, uc, zE, B->dW, contrib);
+  const T* Cv = f32 ? (const T*)B->dCv32 : (const T*)B->dCv;
+  k_bddc_neumann_bwd<T><<<ns, 256, smR, st>>>(B->d_subs, B->dA, B->dF, R, G, Cv, B->dPc, uc, zE, B->dW, contrib);
   if (B->nIface > 0)
     k_iface_sum<T><<<nblk(B->nIface, 256), 256, 0, st>>>(B->nIface, B->dIptr, B->dIsrc, B->dIvec, contrib, v, z);
   // 5. harmonic extension
@@ -1643,6 +1812,13 @@ fg_status fg_bddc_create(fg_system* sys, const fg_bddc_params* prm, fg_bddc** ou
   }
   if (prm->weighting != FG_BDDC_WEIGHT_MULTIPLICITY && prm->weighting != FG_BDDC_WEIGHT_STIFFNESS)
     return bddc_bad("weighting");
+  if (prm->coarse_handler != FG_BDDC_HANDLER_STANDARD && prm->coarse_handler != FG_BDDC_HANDLER_ELASTICITY)
+    return bddc_bad("coarse_handler");
+  if (prm->coarse_handler == FG_BDDC_HANDLER_ELASTICITY && (sp->ncomp != 3 || prm->use_edges)) {
+    // the reference's elasticity handler asserts .not.use_edges (sbm_elasticity_coarse_fe_handler.i90:110-111)
+    set_error("BDDC: the elasticity coarse handler needs a 3-component space and use_edges = 0");
+    return FG_ERR_UNSUPPORTED;
+  }
   if (!sys->d_elmat) return bddc_bad("system without element matrices");
   fg_bddc* B = new fg_bddc();
   B->sys = sys;

@@ -401,10 +401,13 @@ class MLBDDC:
     symbolic and numerical setup from the operator's element matrices;
     ``numerical_setup()`` refreshes it after ``FEAffineOperator.compute()`` on new data.
     Parameters follow the reference's coarse-space switches (coarse_space_use_vertices /
-    edges / faces) and the standard handler's multiplicity weighting."""
+    edges / faces), the standard handler's multiplicity weighting and the choice of coarse
+    FE handler: ``coarse_handler=FG_BDDC_HANDLER_ELASTICITY`` selects the elasticity handler
+    (rigid-body face functionals, no edge constraints: pass ``use_edges=False``)."""
 
     def __init__(self, A: FEAffineOperator, nsub=(2, 2, 2), cuts=None, use_vertices=True, use_edges=True,
-                 use_faces=False, weighting=L.FG_BDDC_WEIGHT_MULTIPLICITY):
+                 use_faces=False, weighting=L.FG_BDDC_WEIGHT_MULTIPLICITY,
+                 coarse_handler=L.FG_BDDC_HANDLER_STANDARD):
         p = L.BddcParams()
         L.lib().fg_bddc_params_default(C.byref(p))
         for d in range(3):
@@ -415,6 +418,7 @@ class MLBDDC:
             p.cuts = self._cuts.ctypes.data
         p.use_vertices, p.use_edges, p.use_faces = int(use_vertices), int(use_edges), int(use_faces)
         p.weighting = int(weighting)
+        p.coarse_handler = int(coarse_handler)
         self.A = A
         h = C.c_void_p()
         L.check(L.lib().fg_bddc_create(A.h, C.byref(p), C.byref(h)), "fg_bddc_create")

@@ -359,6 +359,17 @@ fg_status fg_partition_solve(fg_partition* partition, fg_system* subassembled, c
 typedef struct fg_bddc fg_bddc;
 enum { FG_PREC_BDDC = 2 };
 enum { FG_BDDC_WEIGHT_MULTIPLICITY = 0, FG_BDDC_WEIGHT_STIFFNESS = 1 };
+/* Coarse FE handler.  STANDARD: sbm_standard_coarse_fe_handler.i90 (one coarse dof per
+ * object and component, algebraic averages).  ELASTICITY: elasticity_pb_bddc_l1_coarse_fe_handler_t
+ * (sbm_elasticity_coarse_fe_handler.i90:75-381): 3 coarse dofs per vertex, no edge
+ * constraints (use_edges must be 0), and per face 6 functionals -- the 3 translations and 3
+ * rotations r4 = (y,-x,0), r5 = (-z,0,x), r6 = (0,z,-y) -- each the face integral of the
+ * shape functions times the mode over the face measure (strategy "CI", :180-381); a face's
+ * rows reach its edge and vertex dofs.  The rotations are taken about the face's centroid and
+ * scaled by its size: the same span of functionals, hence the same preconditioner, with a
+ * constraint Schur complement that stays well-conditioned for the FP32 factors.
+ * Vector-valued (3-component) spaces only. */
+enum { FG_BDDC_HANDLER_STANDARD = 0, FG_BDDC_HANDLER_ELASTICITY = 1 };
 typedef struct {
   int32_t nsub[3];         /* subdomains per direction                                     */
   const int32_t* cuts;     /* NULL: even split; else nsub[0]+1, nsub[1]+1, nsub[2]+1 increasing
@@ -368,6 +379,7 @@ typedef struct {
   int32_t use_faces;       /* coarse_space_use_faces                                       */
   int32_t weighting;       /* FG_BDDC_WEIGHT_MULTIPLICITY (reference standard handler) or
                               FG_BDDC_WEIGHT_STIFFNESS (diag(A_i) / sum_j diag(A_j))        */
+  int32_t coarse_handler;  /* FG_BDDC_HANDLER_STANDARD (default) or FG_BDDC_HANDLER_ELASTICITY */
 } fg_bddc_params;
 typedef struct {
   int32_t num_subdomains;

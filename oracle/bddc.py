@@ -17,19 +17,45 @@ problem, on the element matrices and dof map of the oracle (``oracle.Problem``):
   that component over the object's free dofs
   (``Sources/Lib/Integration/FESpace/sbm_standard_coarse_fe_handler.i90:28-219``);
 * weights W = 1 / (number of subdomains around the dof) (``:221-295``), or, as an option,
-  the diagonal-stiffness weights diag(A_i) / sum_j diag(A_j).
+  the diagonal-stiffness weights diag(A_i) / sum_j diag(A_j);
+* or, with ``coarse_handler=HANDLER_ELASTICITY``, the elasticity coarse handler
+  (``Sources/Lib/Integration/FESpace/sbm_elasticity_coarse_fe_handler.i90``): one coarse dof
+  per vertex and component, no edge constraints (``:110-111``), and six per face whose
+  constraint rows are the face integrals of the shape functions times the rigid-body modes
+  (translations, then r4 = (y,-x,0), r5 = (-z,0,x), r6 = (0,z,-y), ``:37-73``) divided by
+  the face measure (strategy CI, ``:180-381``), over the subdomain's own cells.
 
 Subdomains are boxes of cells given by cut positions per axis.  Objects are classified
 from the box grid: an interface node that lies on a slab plane in all three directions is
 a vertex, a node on two interior cut planes (and inside a slab along the third axis) an
 edge point, a node on one interior cut plane a face point.  Edges and faces are grouped
-by the planes and slabs they lie in.
+by the planes and slabs they lie in (a face point on the domain boundary belongs to the
+slab next to it: the same two subdomains share it).
 """
 from __future__ import annotations
 
 import numpy as np
 
 WEIGHT_MULTIPLICITY, WEIGHT_STIFFNESS = 0, 1
+HANDLER_STANDARD, HANDLER_ELASTICITY = 0, 1
+
+_MODES = 6  # rigid-body modes in 3D: 3 translations + 3 rotations
+
+
+def _lagrange(p, i, x):
+    """Lagrange basis i of order p on the equispaced nodes of [-1, 1] at x."""
+    nodes = -1.0 + 2.0 * np.arange(p + 1) / p
+    v = 1.0
+    for j in range(p + 1):
+        if j != i:
+            v *= (x - nodes[j]) / (nodes[i] - nodes[j])
+    return v
+
+
+def _rigid_modes(x):
+    """Values r_m[comp] of the six rigid-body modes at point x (rows m)."""
+    return np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0],
+                     [x[1], -x[0], 0.0], [-x[2], 0.0, x[0]], [0.0, x[2], -x[1]]])
 
 
 def _slab_index(X, pos):
@@ -40,7 +66,7 @@ def _slab_index(X, pos):
 
 class BDDCOracle:
     def __init__(self, problem, n, order, ncomp, cuts, use_vertices=True, use_edges=True, use_faces=False,
-                 weighting=WEIGHT_MULTIPLICITY):
+                 weighting=WEIGHT_MULTIPLICITY, coarse_handler=HANDLER_STANDARD, vertex_xyz=None):
         P = problem
         p = order
         self.n = [int(v) for v in n]
@@ -93,11 +119,22 @@ class BDDCOracle:
                 a = [d for d in range(3) if not plane[d]][0]
                 key = (1, a) + tuple(idx)
             else:
+                # a face: the cut plane and the slabs along the other axes (points on the
+                # domain boundary join the face: the same two subdomains share them)
                 d = on_cut.index(True)
-                key = (2, d) + tuple(idx)
+                slab = [min(int(np.searchsorted(pos[e], X[e], side="right")) - 1, len(pos[e]) - 2) for e in range(3)]
+                key = (2, d) + tuple(idx[e] if e == d else slab[e] for e in range(3))
             keys[g] = key
         use = {0: use_vertices, 1: use_edges, 2: use_faces}
-        objs = sorted({(k, int(comp_of[g])) for g, k in keys.items() if use[k[0]]})
+        rigid = coarse_handler == HANDLER_ELASTICITY
+        if rigid and (ncomp != 3 or use_edges):
+            raise ValueError("the elasticity coarse handler needs 3 components and no edge constraints")
+        if rigid:
+            # faces: six functionals per face object; vertices: one per component
+            objs = sorted({(k, int(comp_of[g])) for g, k in keys.items() if k[0] == 0 and use[0]} |
+                          {(k, mode) for k in keys.values() if k[0] == 2 and use[2] for mode in range(_MODES)})
+        else:
+            objs = sorted({(k, int(comp_of[g])) for g, k in keys.items() if use[k[0]]})
         self.coarse_index = {kc: i for i, kc in enumerate(objs)}
         self.ncoarse = len(objs)
         obj_dofs = {kc: [] for kc in objs}
@@ -105,6 +142,52 @@ class BDDCOracle:
             kc = (k, int(comp_of[g]))
             if kc in obj_dofs:
                 obj_dofs[kc].append(g)
+        if vertex_xyz is None:
+            K3, J3, I3 = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+            vertex_xyz = np.stack([I3.ravel() / nx, J3.ravel() / ny, K3.ravel() / nz], axis=1)
+        xyz = np.asarray(vertex_xyz, dtype=np.float64).reshape(-1, 3)
+        lat_dof = {(int(lat[g, 0]), int(lat[g, 1]), int(lat[g, 2]), int(comp_of[g])): g for g in range(self.nfree)}
+        gx, gw = np.polynomial.legendre.leggauss(p + 1)
+
+        def face_rows(key, s, loc, m):
+            """The six constraint rows of face object `key` seen from subdomain s."""
+            d = key[1]
+            b, c = [e for e in range(3) if e != d]
+            sidx = [s % nsub[0], (s // nsub[0]) % nsub[1], s // (nsub[0] * nsub[1])]
+            lo_c = [int(self.cuts[e][sidx[e]]) for e in range(3)]
+            hi_c = [int(self.cuts[e][sidx[e] + 1]) for e in range(3)]
+            plane = int(self.cuts[d][key[2 + d]])
+            ca, side = (plane, 0) if plane == lo_c[d] else (plane - 1, 1)
+            rows = np.zeros((_MODES, m))
+            meas = 0.0
+            for cc in range(lo_c[c], hi_c[c]):
+                for cb in range(lo_c[b], hi_c[b]):
+                    V = np.zeros((2, 2, 3))
+                    for u in range(2):
+                        for v in range(2):
+                            I3 = [0, 0, 0]
+                            I3[d], I3[b], I3[c] = ca + side, cb + u, cc + v
+                            V[u, v] = xyz[I3[0] + (nx + 1) * (I3[1] + (ny + 1) * I3[2])]
+                    for t, wt in zip(gx, gw):
+                        for s_, ws in zip(gx, gw):
+                            fs, ft = [(1 - s_) / 2, (1 + s_) / 2], [(1 - t) / 2, (1 + t) / 2]
+                            x = sum(fs[u] * ft[v] * V[u, v] for u in range(2) for v in range(2))
+                            dxs = sum((u - 0.5) * ft[v] * V[u, v] for u in range(2) for v in range(2))
+                            dxt = sum(fs[u] * (v - 0.5) * V[u, v] for u in range(2) for v in range(2))
+                            f = ws * wt * np.linalg.norm(np.cross(dxs, dxt))
+                            meas += f
+                            R = _rigid_modes(x)
+                            for j in range(p + 1):
+                                for i in range(p + 1):
+                                    Nv = _lagrange(p, i, s_) * _lagrange(p, j, t)
+                                    P3 = [0, 0, 0]
+                                    P3[d], P3[b], P3[c] = p * (ca + side), p * cb + i, p * cc + j
+                                    for comp in range(3):
+                                        g = lat_dof.get((P3[0], P3[1], P3[2], comp))
+                                        if g is not None and g in loc:
+                                            rows[:, loc[g]] += Nv * R[:, comp] * f
+            return rows / meas
+
         # per-subdomain local problems
         self.subs = []
         for s, cells in enumerate(sub_cells):
@@ -123,9 +206,20 @@ class BDDCOracle:
                             K[ids[a], ids[b]] += em[a, b]
             gl = np.array(gl, dtype=np.int64)
             iface = np.array([len(parts[g]) > 1 for g in gl])
-            my_objs = sorted({(keys[g], int(comp_of[g])) for g in gl if g in keys} & set(obj_dofs))
+            if rigid:
+                my_objs = sorted(({(keys[g], int(comp_of[g])) for g in gl if g in keys} |
+                                  {(keys[g], mode) for g in gl if g in keys for mode in range(_MODES)})
+                                 & set(self.coarse_index))
+            else:
+                my_objs = sorted({(keys[g], int(comp_of[g])) for g in gl if g in keys} & set(obj_dofs))
             C = np.zeros((len(my_objs), m))
+            frows = {}
             for r, kc in enumerate(my_objs):
+                if rigid and kc[0][0] == 2:
+                    if kc[0] not in frows:
+                        frows[kc[0]] = face_rows(kc[0], s, loc, m)
+                    C[r] = frows[kc[0]][kc[1]]
+                    continue
                 ds = obj_dofs[kc]
                 for g in ds:
                     C[r, loc[g]] = 1.0 / len(ds)

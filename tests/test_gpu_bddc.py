@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from bddc import WEIGHT_MULTIPLICITY, WEIGHT_STIFFNESS, BDDCOracle
+from bddc import HANDLER_ELASTICITY, WEIGHT_MULTIPLICITY, WEIGHT_STIFFNESS, BDDCOracle
 
 pytestmark = pytest.mark.gpu
 
@@ -132,6 +132,71 @@ def test_bddc_pcg_matches_oracle(fg, ctx, case):
     assert sm.info()["iterations"] <= inf["iterations"] + 2
     assert np.linalg.norm(xm - ref["x"]) <= 1e-7 * np.linalg.norm(ref["x"])
     M.close()
+
+
+RIGID_CASES = [
+    # n, order, nsub, jitter, weighting (elasticity, clamped at x = 0)
+    ((6, 4, 4), 1, (3, 2, 2), 0.2, WEIGHT_MULTIPLICITY),
+    ((4, 4, 4), 2, (2, 2, 2), 0.0, WEIGHT_STIFFNESS),
+    ((6, 5, 4), 2, (3, 2, 2), 0.3, WEIGHT_STIFFNESS),
+]
+
+
+@pytest.mark.parametrize("case", RIGID_CASES)
+def test_bddc_elasticity_handler_matches_oracle(fg, ctx, case):
+    """The elasticity coarse handler: rigid-body face functionals whose rows reach the
+    faces' edge and vertex dofs (C_eV != 0 in the device's elimination)."""
+    import torch
+    n, order, nsub, jitter, wt = case
+    P, keep, op, ncomp = pair(fg, ctx, n, order, O.ELASTICITY, CLAMP)
+    cuts = fg.bddc_cuts(n, nsub, jitter=jitter, seed=7)
+    Bo = BDDCOracle(P, n, order, 3, cuts, use_edges=False, use_faces=True, weighting=wt,
+                    coarse_handler=HANDLER_ELASTICITY, vertex_xyz=perturbed(n, 0.15, 3))
+    M = fg.MLBDDC(op, nsub=nsub, cuts=cuts, use_edges=False, use_faces=True, weighting=wt,
+                  coarse_handler=fg.FG_BDDC_HANDLER_ELASTICITY)
+    assert M.info()["num_coarse_dofs"] == Bo.ncoarse
+    rng = np.random.default_rng(11)
+    dev = f"cuda:{ctx.device}"
+    for k in range(2):
+        r = rng.normal(size=P.nfree)
+        zo = Bo.apply(r)
+        rt = torch.tensor(r, device=dev)
+        z = torch.zeros_like(rt)
+        M.apply_device(rt, z)
+        assert np.linalg.norm(z.cpu().numpy() - zo) <= 1e-10 * np.linalg.norm(zo)
+        # FP32 factors (the device takes the rotations about each face's centroid, scaled by
+        # the face size: the same span as the oracle's rows in the raw coordinates, and a
+        # well-conditioned S_e in FP32)
+        z32 = torch.zeros_like(rt)
+        M.apply_device(rt, z32, precision=fg.FG_MIXED)
+        assert np.linalg.norm(z32.cpu().numpy() - zo) <= 1e-4 * np.linalg.norm(zo)
+    # iteration counts: within 2 at 1e-10 (the two sides' applies differ by rounding, ~1e-12,
+    # which moves the count of these 30-60 iteration solves by one or two)
+    xo, ito, oko = Bo.pcg(P, P.rhs(), rtol=1e-10, maxit=1000)
+    ref = P.cg(precond=1, rtol=1e-13, maxit=100000)
+    s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, M)
+    s.set_parameters_from_pl({"ILS_RTOL": 1e-10, "ILS_MAX_NUM_ITERATIONS": 1000})
+    x = s.solve()
+    assert s.info()["converged"] and oko
+    assert abs(s.info()["iterations"] - ito) <= 2, (s.info()["iterations"], ito)
+    assert np.linalg.norm(x - ref["x"]) <= 1e-7 * np.linalg.norm(ref["x"])
+    # mixed: FP32 preconditioner, FP64 Krylov vectors, to 1e-8
+    sm = fg.IterativeLinearSolver().set_type_from_string("GPU_MPCG").set_operators(op, M)
+    sm.set_parameters_from_pl({"ILS_RTOL": 1e-8, "ILS_MAX_NUM_ITERATIONS": 1000})
+    xm = sm.solve()
+    assert sm.info()["converged"]
+    assert np.linalg.norm(xm - ref["x"]) <= 1e-6 * np.linalg.norm(ref["x"])
+    M.close()
+
+
+def test_bddc_elasticity_handler_rejects(fg, ctx):
+    from fempar_gb300 import FGError
+    P, keep, op, ncomp = pair(fg, ctx, (4, 4, 4), 1, O.ELASTICITY, CLAMP)
+    with pytest.raises(FGError):  # the reference's handler asserts no edge constraints
+        fg.MLBDDC(op, nsub=(2, 2, 2), use_edges=True, use_faces=True, coarse_handler=fg.FG_BDDC_HANDLER_ELASTICITY)
+    P, keep, op, ncomp = pair(fg, ctx, (4, 4, 4), 1, O.POISSON, CLAMP)
+    with pytest.raises(FGError):  # rigid-body modes need three components
+        fg.MLBDDC(op, nsub=(2, 2, 2), use_edges=False, use_faces=True, coarse_handler=fg.FG_BDDC_HANDLER_ELASTICITY)
 
 
 def test_bddc_criteria_follow_cg(fg, ctx):
