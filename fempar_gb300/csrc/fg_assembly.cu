@@ -460,17 +460,17 @@ __global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
 }
 
 // warp per free row; CAP = power-of-two box capacity
-template <int P, int CAP>
-__global__ void __launch_bounds__(256)
+template <int P, int CAP, int W = 8>
+__global__ void __launch_bounds__(W * 32)
     k_scatter_rows(AsmGeom g, int64_t nfree, const int32_t* __restrict__ free2lat, const int32_t* __restrict__ latdof,
                    const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                    const double* __restrict__ E, const double* __restrict__ EV, double* __restrict__ val,
                    float* __restrict__ val32, double* __restrict__ rhs) {
   constexpr int NP1 = P + 1, NN = NP1 * NP1 * NP1;
-  __shared__ int32_t s_col[8][CAP];
-  __shared__ double s_acc[8][CAP];
+  __shared__ int32_t s_col[W][CAP];
+  __shared__ double s_acc[W][CAP];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int64_t r = (int64_t)blockIdx.x * 8 + wib;
+  const int64_t r = (int64_t)blockIdx.x * W + wib;
   if (r >= nfree) return;
   const int ncomp = g.ncomp, ND = NN * ncomp;
   const int32_t slot = free2lat[r];
@@ -618,9 +618,12 @@ struct ElastShape {
   static constexpr int ND = 3 * NN;
   static constexpr int NPAIR = NN * (NN + 1) / 2;
   static constexpr int CH = P == 1 ? 2 : 4;  // node pairs per lane per pass
-  static constexpr int WARPS = P == 1 ? 8 : 3;
+  static constexpr int WARPS = P == 1 ? 8 : P == 2 ? 3 : 2;
+  // Q3: the 192 x 192 element matrix (288 KB) does not fit in shared memory; it is written
+  // straight to its slot in HBM and read back from there for the Dirichlet lifting
+  static constexpr bool EL_GLOBAL = P >= 3;
   static constexpr int SM_XV = 24, SM_INVJ = NQ * 9, SM_FAC = NQ, SM_XQ = NQ * 3, SM_F = NQ * 3, SM_SQ = NQ,
-                       SM_G = NQ * NN * 3, SM_EL = ND * ND;
+                       SM_G = NQ * NN * 3, SM_EL = EL_GLOBAL ? 0 : ND * ND;
   static constexpr int SM_DOUBLES = SM_XV + SM_INVJ + SM_FAC + SM_XQ + SM_F + SM_SQ + SM_G + SM_EL;
   static constexpr int SM_INTS = ND;
   static constexpr size_t SM_BYTES_WARP = ((size_t)SM_DOUBLES * 8 + SM_INTS * 4 + 15) / 16 * 16;
@@ -644,11 +647,12 @@ __global__ void __launch_bounds__(ElastShape<P>::WARPS * 32)
   double* fsrc = xq + S::SM_XQ;
   double* sq = fsrc + S::SM_F;
   double* sg = sq + S::SM_SQ;
-  double* el = sg + S::SM_G;
-  int32_t* gid = (int32_t*)(el + S::SM_EL);
+  int32_t* gid = (int32_t*)(sg + S::SM_G + S::SM_EL);
 
   const int64_t c = (int64_t)blockIdx.x * S::WARPS + wib;
   if (c >= ncells) return;
+  double* const Ec = E + (size_t)c * ND * ND;
+  double* const el = S::EL_GLOBAL ? Ec : sg + S::SM_G;
   const int ci = (int)(c % g.n[0]);
   const int cj = (int)((c / g.n[0]) % g.n[1]);
   const int ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
@@ -786,8 +790,8 @@ __global__ void __launch_bounds__(ElastShape<P>::WARPS * 32)
       }
     EV[c * ND + i] = ev;
   }
-  double* Ec = E + (size_t)c * ND * ND;
-  for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = el[idx];
+  if (!S::EL_GLOBAL)
+    for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = el[idx];
 }
 
 template <int P>
@@ -812,10 +816,11 @@ static fg_status launch_elasticity(fg_system* sys) {
   const int64_t n = sp->nfree;
   if (sp->explicit_nodes) return usystem_scatter(sys);
   if (n > 0) {
-    constexpr int CAP = P == 1 ? 128 : 512;  // (2P+1)^3 * 3 box entries
-    k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,
-                                                                 sp->d_col, sys->d_elmat, sys->d_elvec, sys->d_val,
-                                                                 sys->d_val32, sys->d_rhs);
+    constexpr int CAP = P == 1 ? 128 : P == 2 ? 512 : 1056;  // (2P+1)^3 * 3 box entries, rounded up to 32
+    constexpr int W = P == 3 ? 2 : 8;                         // warps (rows) per block: static smem <= 48 KB
+    k_scatter_rows<P, CAP, W><<<nblk(n, W), W * 32, 0, ctx->stream>>>(
+        g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr, sp->d_col, sys->d_elmat, sys->d_elvec, sys->d_val,
+        sys->d_val32, sys->d_rhs);
     FG_CUDA_TRY(cudaGetLastError());
   }
   return FG_OK;
@@ -827,8 +832,9 @@ fg_status system_assemble(fg_system* sys) {
     switch (sp->order) {
       case 1: return launch_elasticity<1>(sys);
       case 2: return launch_elasticity<2>(sys);
+      case 3: return launch_elasticity<3>(sys);
       default:
-        set_error("elasticity of order %d is not built on the device (orders 1-2)", sp->order);
+        set_error("elasticity of order %d is not built on the device (orders 1-3)", sp->order);
         return FG_ERR_UNSUPPORTED;
     }
   }

@@ -475,7 +475,7 @@ typedef struct fg_server fg_server;
 typedef struct {
   int kind;                     /* FG_POISSON / FG_ELASTICITY                          */
   int32_t n[3];                 /* cells per direction (unit cube)                     */
-  int order;                    /* 1..3 (elasticity 1..2)                              */
+  int order;                    /* 1..3                                                */
   const double* cell_coef;      /* host, ncells (copied at submit); NULL = coef_const  */
   double coef_const, nu;
   int source_fn;                /* FG_FN_ZERO / FG_FN_CONST                            */

@@ -289,7 +289,7 @@ def build_elasticity_pair(fg, ctx, n, order, seed=3, perturb=True):
     return P, tri, sp, op
 
 
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("order", [1, 2, 3])
 def test_elasticity_assembly(fg, ctx, order):
     P, tri, sp, op = build_elasticity_pair(fg, ctx, (4, 3, 3), order)
     irp, ja, val = op.get_matrix()
@@ -298,13 +298,16 @@ def test_elasticity_assembly(fg, ctx, order):
     assert np.max(np.abs(b - ob)) <= RHS_TOL * np.max(np.abs(ob))
 
 
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("order", [1, 2, 3])
 def test_elasticity_solution(fg, ctx, order):
     P, tri, sp, op = build_elasticity_pair(fg, ctx, (5, 3, 4), order, seed=8)
     ref = P.cg(precond=1, rtol=1e-13, maxit=50000)
-    for prec, tol in (("fp64", SOL_TOL), ("mixed", 1e-9)):
+    # mixed: Q3 elasticity with E ~ lognormal(sigma 1.5) is too ill-conditioned for FP32 inner
+    # solves to reach 1e-12; it is held to the mixed solver's target, 1e-8
+    mixed_rtol, mixed_tol = (1e-12, 1e-9) if order < 3 else (1e-8, 1e-6)
+    for prec, tol in (("fp64", SOL_TOL), ("mixed", mixed_tol)):
         s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
-        s.set_parameters_from_pl({"ILS_RTOL": 1e-13 if prec == "fp64" else 1e-12, "ILS_MAX_NUM_ITERATIONS": 50000,
+        s.set_parameters_from_pl({"ILS_RTOL": 1e-13 if prec == "fp64" else mixed_rtol, "ILS_MAX_NUM_ITERATIONS": 50000,
                                   "PRECISION": prec})
         x = s.solve()
         assert s.info()["converged"], prec
@@ -312,11 +315,11 @@ def test_elasticity_solution(fg, ctx, order):
         assert err <= tol, (prec, err)
 
 
-def test_elasticity_q3_reported_unsupported(fg, ctx):
+def test_order_4_reported_unsupported(fg, ctx):
     from fempar_gb300 import FGError
     tri = fg.SerialTriangulation(ctx, (2, 2, 2))
-    sp = fg.SerialFESpace(tri, order=3, ncomp=3, dirichlet_ids=CLAMP)
     with pytest.raises(FGError):
+        sp = fg.SerialFESpace(tri, order=4, ncomp=3, dirichlet_ids=CLAMP)
         fg.FEAffineOperator(sp, fg.ElasticityIntegration(cell_coef=np.ones(8), nu=0.3)).compute()
 
 

@@ -106,7 +106,7 @@ def test_poisson_parity(fg, ctx, order, dirichlet):
         assert err <= tol, (prec, err)
 
 
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("order", [1, 2, 3])
 def test_elasticity_parity(fg, ctx, order):
     m = gidmesh.box_mesh((4, 3, 3), seed=21 + order, perturb=0.2)
     E = np.exp(np.random.default_rng(order).normal(0.0, 1.0, size=len(m["cells"])))
