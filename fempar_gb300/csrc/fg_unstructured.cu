@@ -701,8 +701,9 @@ fg_status uspace_build_pattern(fg_space* sp) {
   const int64_t n = sp->nfree;
   const int nn = sp->tab.nn, ncomp = sp->ncomp;
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_rowptr, sizeof(int64_t) * (n + 1)));
-  if (n == 0) {
+  if (n == 0) {  // no free dofs: an empty pattern (row pointer 0, a one-slot column array)
     FG_CUDA_TRY(cudaMemsetAsync(sp->d_rowptr, 0, sizeof(int64_t), ctx->stream));
+    FG_TRY(dev_alloc(ctx, (void**)&sp->d_col, sizeof(int32_t)));
     sp->nnz = 0;
     return FG_OK;
   }
