@@ -55,7 +55,9 @@ def build_pair(fg, ctx, n, order, kind):
                                                  ((4, 6, 4), (2, 3, 2), 2, O.POISSON),
                                                  ((6, 4, 4), (3, 2, 2), 3, O.POISSON),
                                                  ((4, 4, 4), (2, 2, 2), 1, O.ELASTICITY),
-                                                 ((4, 2, 4), (2, 1, 2), 2, O.ELASTICITY)])
+                                                 ((4, 2, 4), (2, 1, 2), 2, O.ELASTICITY),
+                                                 ((3, 2, 2), (3, 2, 2), 1, O.POISSON),
+                                                 ((3, 2, 1), (3, 2, 1), 2, O.POISSON)])
 def test_partition_parity(fg, ctx, n, nparts, order, kind):
     import torch
     from fempar_gb300.partition import PartitionedFESpace
