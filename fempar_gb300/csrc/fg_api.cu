@@ -179,19 +179,20 @@ fg_status fg_mesh_create_structured(fg_ctx* ctx, int num_dims, const int32_t n[3
                                     const double* vertex_xyz, fg_mesh** out) {
   FG_CHECK_ARG(ctx && n && out, "ctx/n/out");
   *out = nullptr;
-  if (num_dims != 3) {
-    set_error("only 3D hexahedral meshes are built on the device");
+  if (num_dims != 2 && num_dims != 3) {
+    set_error("num_dims must be 2 (quadrilaterals) or 3 (hexahedra)");
     return FG_ERR_UNSUPPORTED;
   }
-  FG_CHECK_ARG(n[0] >= 1 && n[1] >= 1 && n[2] >= 1, "n");
+  FG_CHECK_ARG(n[0] >= 1 && n[1] >= 1 && (num_dims == 2 || n[2] >= 1), "n");
   FG_DEVICE_GUARD(ctx);
   fg_mesh* m = new fg_mesh();
   m->ctx = ctx;
-  m->dim = 3;
-  for (int d = 0; d < 3; ++d) m->n[d] = n[d];
+  m->dim = num_dims;
+  // 2D: one layer of cells in the lattice bookkeeping (n[2] = 1), vertices at z = 0
+  for (int d = 0; d < 3; ++d) m->n[d] = (num_dims == 2 && d == 2) ? 1 : n[d];
   for (int i = 0; i < 6; ++i) m->limits[i] = limits ? limits[i] : (i % 2 ? 1.0 : 0.0);
-  m->ncells = (int64_t)n[0] * n[1] * n[2];
-  m->nverts = (int64_t)(n[0] + 1) * (n[1] + 1) * (n[2] + 1);
+  m->ncells = (int64_t)m->n[0] * m->n[1] * (num_dims == 2 ? 1 : m->n[2]);
+  m->nverts = (int64_t)(m->n[0] + 1) * (m->n[1] + 1) * (num_dims == 2 ? 1 : m->n[2] + 1);
   std::vector<double> h(3 * m->nverts);
   if (vertex_xyz) {
     std::memcpy(h.data(), vertex_xyz, sizeof(double) * h.size());
@@ -200,13 +201,14 @@ fg_status fg_mesh_create_structured(fg_ctx* ctx, int num_dims, const int32_t n[3
     for (int64_t v = 0; v < m->nverts; ++v) {
       int64_t r = v;
       int ijk[3];
-      ijk[0] = (int)(r % (n[0] + 1)); r /= (n[0] + 1);
-      ijk[1] = (int)(r % (n[1] + 1)); r /= (n[1] + 1);
+      ijk[0] = (int)(r % (m->n[0] + 1)); r /= (m->n[0] + 1);
+      ijk[1] = (int)(r % (m->n[1] + 1)); r /= (m->n[1] + 1);
       ijk[2] = (int)r;
-      for (int d = 0; d < 3; ++d) {
-        double c = (double)ijk[d] / (double)n[d];
+      for (int d = 0; d < num_dims; ++d) {
+        double c = (double)ijk[d] / (double)m->n[d];
         h[v * 3 + d] = (m->limits[2 * d + 1] - m->limits[2 * d]) * c + m->limits[2 * d];
       }
+      if (num_dims == 2) h[v * 3 + 2] = 0.0;
     }
   }
   fg_status s = dev_alloc(ctx, (void**)&m->d_coords, sizeof(double) * h.size());
@@ -316,6 +318,10 @@ fg_status fg_mesh_get_info(fg_mesh* m, fg_mesh_info* info) {
   if (m->unst) {
     info->num_edges = m->nedges;
     info->num_faces = m->nfaces;
+  } else if (m->dim == 2) {
+    const int64_t n0 = m->n[0], n1 = m->n[1];
+    info->num_edges = n0 * (n1 + 1) + (n0 + 1) * n1;
+    info->num_faces = 0;
   } else {
     const int64_t n0 = m->n[0], n1 = m->n[1], n2 = m->n[2];
     info->num_edges = n0 * (n1 + 1) * (n2 + 1) + (n0 + 1) * n1 * (n2 + 1) + (n0 + 1) * (n1 + 1) * n2;
@@ -323,7 +329,7 @@ fg_status fg_mesh_get_info(fg_mesh* m, fg_mesh_info* info) {
   }
   info->num_vefs = info->num_vertices + info->num_edges + info->num_faces;
   info->unstructured = m->unst ? 1 : 0;
-  info->max_cells_around_vertex = m->unst ? m->max_vcells : 8;
+  info->max_cells_around_vertex = m->unst ? m->max_vcells : (m->dim == 2 ? 4 : 8);
   return FG_OK;
 }
 
@@ -375,8 +381,8 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
     set_error("order %d not built (1..%d)", order, FG_MAX_ORDER);
     return FG_ERR_UNSUPPORTED;
   }
-  if (ncomp != 1 && ncomp != 3) {
-    set_error("ncomp must be 1 or 3");
+  if (ncomp != 1 && ncomp != mesh->dim) {
+    set_error("ncomp must be 1 or the number of dimensions (%d)", mesh->dim);
     return FG_ERR_UNSUPPORTED;
   }
   FG_CHECK_ARG(n_ids >= 0 && (n_ids == 0 || dirichlet_ids), "dirichlet ids");
@@ -386,7 +392,7 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
   sp->mesh = mesh;
   sp->order = order;
   sp->ncomp = ncomp;
-  const int max_id = mesh->unst ? 31 : 27;
+  const int max_id = mesh->unst ? 31 : (mesh->dim == 2 ? 9 : 27);
   for (int i = 0; i < n_ids; ++i) {
     if (dirichlet_ids[i] < 1 || dirichlet_ids[i] > max_id) {
       delete sp;
@@ -395,11 +401,17 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
     }
     sp->dirmask |= 1u << dirichlet_ids[i];
   }
-  for (int d = 0; d < 3; ++d) sp->Ln[d] = order * mesh->n[d] + 1;
+  for (int d = 0; d < 3; ++d) sp->Ln[d] = (mesh->dim == 2 && d == 2) ? 1 : order * mesh->n[d] + 1;
   sp->nlat = (int64_t)sp->Ln[0] * sp->Ln[1] * sp->Ln[2];
-  sp->tab.build(order, ncomp);
+  if (mesh->dim == 2) sp->tab.build2d(order, ncomp);
+  else sp->tab.build(order, ncomp);
   fg_status s = upload_tables(ctx, sp->tab, sp->dtab);
-  if (mesh->unst) {
+  if (mesh->dim == 2) {
+    // quadrilaterals: the solver runs on the explicit-column SELL layout
+    if (s == FG_OK) s = q2_number_dofs(sp);
+    if (s == FG_OK) s = q2_build_pattern(sp);
+    sp->layout = FG_LAYOUT_SELL;
+  } else if (mesh->unst) {
     // explicit nodes and cells around them; the solver runs on the explicit-column SELL layout
     sp->explicit_nodes = true;
     if (s == FG_OK) s = uspace_number_dofs(sp);
@@ -436,6 +448,10 @@ fg_status fg_space_create(fg_mesh* mesh, int order, int ncomp, const int32_t* di
 fg_status fg_space_create_dg(fg_mesh* mesh, int order, fg_space** out) {
   FG_CHECK_ARG(mesh && out, "mesh/out");
   *out = nullptr;
+  if (mesh->dim != 3) {
+    set_error("the dG space is built on 3D meshes");
+    return FG_ERR_UNSUPPORTED;
+  }
   if (order < 1 || order > FG_MAX_ORDER) {
     set_error("order %d not built (1..%d)", order, FG_MAX_ORDER);
     return FG_ERR_UNSUPPORTED;
@@ -490,7 +506,7 @@ fg_status fg_space_release_pattern(fg_space* sp) {
 
 fg_status fg_space_get_info(fg_space* sp, fg_space_info* info) {
   FG_CHECK_ARG(sp && info, "space/info");
-  info->num_dims = 3;
+  info->num_dims = sp->mesh->dim;
   info->order = sp->order;
   info->ncomp = sp->ncomp;
   info->dofs_per_cell = sp->tab.nd;
@@ -551,7 +567,10 @@ static fg_status numeric_phase(fg_system* sys, const fg_integrand* g) {
   fg_ctx* ctx = sp->mesh->ctx;
   const bool dev = (g->flags & FG_INPUTS_ON_DEVICE) != 0;
   sys->integ = *g;
-  if (g->kind == FG_ELASTICITY && sp->ncomp != 3) { set_error("elasticity needs ncomp=3"); return FG_ERR_BADARG; }
+  if (g->kind == FG_ELASTICITY && sp->ncomp != sp->mesh->dim) {
+    set_error("elasticity needs ncomp = %d", sp->mesh->dim);
+    return FG_ERR_BADARG;
+  }
   if (g->kind == FG_POISSON && sp->ncomp != 1) { set_error("Poisson needs ncomp=1"); return FG_ERR_BADARG; }
   if (g->cell_coef) FG_TRY(stage_input(ctx, g->cell_coef, sp->mesh->ncells, dev, &sys->d_coef));
   else if (sys->d_coef) { dev_free(ctx, sys->d_coef); sys->d_coef = nullptr; }

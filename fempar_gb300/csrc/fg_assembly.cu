@@ -543,6 +543,7 @@ static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / 
 
 fg_status system_interpolate_dirichlet(fg_system* sys, int boundary_fn, const double* prm) {
   fg_space* sp = sys->space;
+  if (sp->mesh->dim == 2) return q2_interpolate_dirichlet(sys, boundary_fn, prm);
   fg_ctx* ctx = sp->mesh->ctx;
   if (sp->ndir == 0) return FG_OK;
   double* xyz = nullptr;
@@ -828,6 +829,7 @@ static fg_status launch_elasticity(fg_system* sys) {
 
 fg_status system_assemble(fg_system* sys) {
   fg_space* sp = sys->space;
+  if (sp->mesh->dim == 2) return q2_assemble(sys);
   if (sys->integ.kind == FG_ELASTICITY && sp->ncomp == 3) {
     switch (sp->order) {
       case 1: return launch_elasticity<1>(sys);

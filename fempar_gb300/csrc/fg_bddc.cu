@@ -1802,7 +1802,7 @@ fg_status fg_bddc_create(fg_system* sys, const fg_bddc_params* prm, fg_bddc** ou
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
   FG_CUDA_TRY(cudaSetDevice(ctx->device));
-  if (sp->mesh->unst || sp->dg) {
+  if (sp->mesh->unst || sp->dg || sp->mesh->dim != 3) {
     set_error("BDDC: box subdomains are built for continuous spaces on structured meshes only");
     return FG_ERR_UNSUPPORTED;
   }

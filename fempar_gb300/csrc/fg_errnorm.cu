@@ -191,8 +191,8 @@ extern "C" fg_status fg_system_error_norms(fg_system* sys, const double* x, int3
   }
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
-  if (sp->ncomp != 1) {
-    set_error("error norms are built for scalar fields");
+  if (sp->ncomp != 1 || sp->mesh->dim != 3) {
+    set_error("error norms are built for scalar fields on 3D meshes");
     return FG_ERR_UNSUPPORTED;
   }
   if (fn != FG_FN_ZERO && fn != FG_FN_CONST && fn != FG_FN_LINEAR && fn != FG_FN_SHARP_WAVE) {

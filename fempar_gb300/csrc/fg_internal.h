@@ -49,6 +49,9 @@ struct RefTables {
   std::vector<double> gshg;   // 8*nq*3    Q1 geometry gradients
   std::vector<double> gnod;   // 8*nn      Q1 geometry shapes at the FE nodes
   void build(int order, int ncomp);
+  // quadrilateral (dim 2): (p+1)^2 nodes and points, 9 n-faces (anchor | free << 2), 4
+  // geometry nodes; gradients keep 3 slots with the third zero
+  void build2d(int order, int ncomp);
 };
 
 // One row class of the lattice-implicit SELL layout (fg_stencil.cu).
@@ -216,6 +219,13 @@ fg_status system_assemble(fg_system* sys);
 
 fg_status scan_i64(fg_ctx* ctx, int64_t* a, int64_t n, int64_t* total);
 fg_status space_count_upper(fg_space* sp);
+// fg_quad.cu: 2D structured quadrilateral meshes
+fg_status q2_number_dofs(fg_space* sp);
+fg_status q2_build_pattern(fg_space* sp);
+fg_status q2_export_dof_map(fg_space* sp, int32_t* out_host);
+fg_status q2_dirichlet_coords(fg_space* sp, double* d_xyz);
+fg_status q2_interpolate_dirichlet(fg_system* sys, int boundary_fn, const double* prm);
+fg_status q2_assemble(fg_system* sys);
 
 // fg_unstructured.cu
 fg_status umesh_build_topology(fg_mesh* m, int64_t nb, const int64_t* bptr, const int32_t* bverts,

@@ -490,8 +490,8 @@ extern "C" {
 fg_status fg_partition_create(fg_space* space, const int32_t num_parts_x_dir[3], fg_partition** out) {
   if (!space || !num_parts_x_dir || !out) { set_error("bad argument: space/num_parts_x_dir/out"); return FG_ERR_BADARG; }
   *out = nullptr;
-  if (space->mesh->unst || space->dg || space->explicit_nodes) {
-    set_error("partitioned spaces are built from continuous spaces on structured meshes");
+  if (space->mesh->unst || space->dg || space->explicit_nodes || space->mesh->dim != 3) {
+    set_error("partitioned spaces are built from continuous spaces on structured 3D meshes");
     return FG_ERR_UNSUPPORTED;
   }
   fg_ctx* ctx = space->mesh->ctx;

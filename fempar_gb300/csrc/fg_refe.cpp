@@ -1,4 +1,4 @@
-// fg_refe.cpp -- host-side reference-element tables of the Lagrangian hex FE.
+// fg_refe.cpp -- host-side reference-element tables of the Lagrangian hex (and quad) FE.
 //
 // Node order, quadrature order and the polytope n-face order reproduce the reference
 // element of FEMPAR (Sources/Lib/Integration/ReferenceFE):
@@ -148,6 +148,69 @@ void RefTables::build(int p, int nc) {
       double fy = by ? 0.5 * (1 + ys) : 0.5 * (1 - ys);
       double fz = bz ? 0.5 * (1 + zs) : 0.5 * (1 - zs);
       gnod[k * nn + a] = fx * fy * fz;
+    }
+  }
+}
+
+void RefTables::build2d(int p, int nc) {
+  dim = 2;
+  order = p;
+  ncomp = nc;
+  const int np1 = p + 1;
+  nn = np1 * np1;
+  nd = nn * nc;
+  nq = np1 * np1;
+  // n-face codes of the quadrilateral: anchor | (free directions << 2), sorted by (dim, code)
+  int cnt = 0;
+  for (int t = 0; t < 4; ++t)
+    for (int a = 0; a < 4; ++a)
+      if ((a & t) == 0) codes[cnt++] = a | (t << 2);
+  std::sort(codes, codes + 9, [](int u, int v) {
+    int du = bitcount(u >> 2), dv = bitcount(v >> 2);
+    return du != dv ? du < dv : u < v;
+  });
+  for (int i = 9; i < 27; ++i) codes[i] = -1;
+  for (int i = 0; i < 64; ++i) code2idx[i] = -1;
+  for (int i = 0; i < 9; ++i) code2idx[codes[i]] = i;
+
+  double x1[FG_MAX_ORDER + 1], w1[FG_MAX_ORDER + 1];
+  gl_rule(np1, x1, w1);
+  qw.assign(nq, 0.0);
+  for (int j = 0; j < np1; ++j)
+    for (int i = 0; i < np1; ++i) qw[i + np1 * j] = w1[i] * w1[j];
+  double L[FG_MAX_ORDER + 1][FG_MAX_ORDER + 1], dL[FG_MAX_ORDER + 1][FG_MAX_ORDER + 1];
+  for (int j = 0; j < np1; ++j)
+    for (int q = 0; q < np1; ++q) lagrange_1d(p, j, x1[q], L[j][q], dL[j][q]);
+  shp.assign((size_t)nn * nq, 0.0);
+  shg.assign((size_t)nn * nq * 3, 0.0);
+  for (int a = 0; a < nn; ++a) {
+    int ai = a % np1, aj = a / np1;
+    for (int q = 0; q < nq; ++q) {
+      int qi = q % np1, qj = q / np1;
+      shp[(size_t)a * nq + q] = L[ai][qi] * L[aj][qj];
+      shg[((size_t)a * nq + q) * 3 + 0] = dL[ai][qi] * L[aj][qj];
+      shg[((size_t)a * nq + q) * 3 + 1] = dL[aj][qj] * L[ai][qi];
+    }
+  }
+  gshp.assign(4 * nq, 0.0);
+  gshg.assign(4 * nq * 3, 0.0);
+  for (int k = 0; k < 4; ++k) {
+    int bx = k & 1, by = (k >> 1) & 1;
+    for (int q = 0; q < nq; ++q) {
+      double xs = x1[q % np1], ys = x1[q / np1];
+      double fx = bx ? 0.5 * (1 + xs) : 0.5 * (1 - xs), gx = bx ? 0.5 : -0.5;
+      double fy = by ? 0.5 * (1 + ys) : 0.5 * (1 - ys), gy = by ? 0.5 : -0.5;
+      gshp[k * nq + q] = fx * fy;
+      gshg[(k * nq + q) * 3 + 0] = gx * fy;
+      gshg[(k * nq + q) * 3 + 1] = gy * fx;
+    }
+  }
+  gnod.assign(4 * nn, 0.0);
+  for (int k = 0; k < 4; ++k) {
+    int bx = k & 1, by = (k >> 1) & 1;
+    for (int a = 0; a < nn; ++a) {
+      double xs = (2.0 / p) * (a % np1) - 1.0, ys = (2.0 / p) * (a / np1) - 1.0;
+      gnod[k * nn + a] = (bx ? 0.5 * (1 + xs) : 0.5 * (1 - xs)) * (by ? 0.5 * (1 + ys) : 0.5 * (1 - ys));
     }
   }
 }

@@ -40,7 +40,9 @@ static constexpr int RB = 256;  // threads per block of the vector / SpMV kernel
 enum { S_RZ = 0, S_ALPHA, S_BETA, S_ERR, S_TOL, S_APP, S_RNRMM, S_BNRM, S_R0NRM, S_SIGMA, S_RMAX, S_DELTA, S_RNSCALED,
        S_COUNT = 16 };
 enum { I_ITER = 0, I_DONE, I_CONV, I_MAXIT, I_FLAG, I_COUNT = 8 };
-enum { FLAG_NONE = 0, FLAG_UPDATE = 1, FLAG_CHECK = 2, FLAG_MAXIT = 3 };
+// FLAG_BREAK: the FP32 recurrence broke down (non-finite or non-positive r_z, residual grown
+// 1e4-fold): the segment's correction is dropped and the solve finishes in FP64
+enum { FLAG_NONE = 0, FLAG_UPDATE = 1, FLAG_CHECK = 2, FLAG_MAXIT = 3, FLAG_BREAK = 4 };
 
 struct RedBuf {
   double* part;  // [4][nblocks]
@@ -319,7 +321,8 @@ __global__ void __launch_bounds__(RB)
     S[S_RNSCALED] = rn;
     const double est = rn * S[S_SIGMA];
     int flag = FLAG_NONE;
-    if (est <= S[S_TOL]) flag = FLAG_CHECK;
+    if (!(rn <= 1e4 * S[S_RMAX]) || !(tot[1] > 0.0 && tot[1] <= 1e300)) flag = FLAG_BREAK;  // NaN fails both
+    else if (est <= S[S_TOL]) flag = FLAG_CHECK;
     else if (rn < S[S_DELTA] * S[S_RMAX]) flag = FLAG_UPDATE;
     else if (it >= I[I_MAXIT]) flag = FLAG_MAXIT;
     if (rn > S[S_RMAX]) S[S_RMAX] = rn;
@@ -769,7 +772,9 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
     } else {
       tol = prm->rtol * rn + prm->atol;
     }
-    int outer = 0;
+    int outer = 0, stalls = 0, polish_its = 0;
+    bool polish = false;
+    double rn_prev = rn;
     int64_t graph_launches = 0;
     if (!std::isfinite(rn)) {
       status = FG_ERR_NUMERIC;
@@ -815,10 +820,12 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
         if (e != cudaSuccess) { set_error("mixed loop: %s", cudaGetErrorString(e)); status = FG_ERR_CUDA; break; }
         if (!h_I[I_DONE]) continue;
         // reliable update: fold the FP32 correction into x64 and recompute the true residual
+        // (after a breakdown the segment's correction is dropped instead)
         FG_CUDA_TRY(cudaMemcpyAsync(h_S, w.S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
         FG_CUDA_TRY(cudaStreamSynchronize(st));
-        const double sigma = h_S[S_SIGMA];
-        launch_k(k_fold, w, st, nv, sigma, w.x32, w.x);
+        const bool broke = h_I[I_FLAG] == FLAG_BREAK;
+        if (broke) k_fill<float><<<nblk(nv, RB), RB, 0, st>>>(nv, w.x32, 0.0f);
+        else launch_k(k_fold, w, st, nv, h_S[S_SIGMA], w.x32, w.x);
         ctx->launches += 1;
         spmv_k<double, 2>(sys, w, w.x, w.r, w.b, st);
         ++outer;
@@ -828,6 +835,12 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
         if (!std::isfinite(rn)) { status = FG_ERR_NUMERIC; set_error("non-finite residual"); break; }
         if (rn <= tol) { out.converged = 1; break; }
         if (h_I[I_ITER] >= prm->max_iters) break;
+        // FP32 segments aim at a 10x reduction of the true residual; a breakdown, or two
+        // segments in a row that gain less than 2x (FP32 rounding of an ill-conditioned
+        // matrix near a tight tolerance), hand the rest of the solve to the FP64 PCG
+        stalls = rn > 0.5 * rn_prev ? stalls + 1 : 0;
+        rn_prev = rn;
+        if (broke || stalls >= 2) { polish = true; break; }
         refresh(0);
         FG_CUDA_TRY(cudaGetLastError());
       }
@@ -836,8 +849,24 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
       FG_CUDA_TRY(cudaMemcpyAsync(h_I, w.I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, st));
       FG_CUDA_TRY(cudaStreamSynchronize(st));
       ctx->launches += graph_launches * 3 * chunk;
+      if (polish && status == FG_OK) {
+        // FP64 PCG from x64 to the same absolute tolerance, with the iterations left
+        const int mixed_its = h_I[I_ITER];
+        spmv_k<double, 0>(sys, w, w.x, w.r, nullptr, st);
+        launch_k(k_init64, w, st, nv, (const double*)w.b, 1, w.r, w.p, (const double*)sys->d_idiag, precond,
+                 (int)FG_RES_RES, 0.0, tol, std::max(prm->max_iters - mixed_its, 1), w.rb, w.S, w.I);
+        ctx->launches += 1;
+        FG_CUDA_TRY(cudaGetLastError());
+        status = run_chunks(ctx, w, chunk,
+                            [&]() { iter64(sys, w, precond, false, (int)FG_RES_RES, 0.0, tol, st); }, h_I, h_S);
+        ctx->launches += (int64_t)3 * chunk * (((int64_t)h_I[I_ITER] + chunk - 1) / chunk);
+        polish_its = h_I[I_ITER];
+        out.converged = h_I[I_CONV];
+        rn = h_S[S_ERR];
+        h_I[I_ITER] = mixed_its;
+      }
     }
-    out.iterations = h_I[I_ITER];
+    out.iterations = h_I[I_ITER] + polish_its;
     out.outer_iterations = outer;
     out.error_estimate = rn;
     out.tolerance = tol;

@@ -395,6 +395,7 @@ fg_status space_build_pattern(fg_space* sp) {
 
 fg_status space_export_dof_map(fg_space* sp, int32_t* out_host) {
   if (sp->mesh->unst || sp->dg) return uspace_export_dof_map(sp, out_host);
+  if (sp->mesh->dim == 2) return q2_export_dof_map(sp, out_host);
   fg_ctx* ctx = sp->mesh->ctx;
   Lat g = make_lat(sp);
   const int64_t total = sp->mesh->ncells * sp->tab.nd;
@@ -453,6 +454,7 @@ __global__ void k_dirichlet_coords(Lat g, int64_t ndir, const int32_t* dir2lat, 
 fg_status space_dirichlet_coords(fg_space* sp, double* d_xyz) {
   if (sp->ndir == 0) return FG_OK;
   if (sp->mesh->unst) return uspace_dirichlet_coords(sp, d_xyz);
+  if (sp->mesh->dim == 2) return q2_dirichlet_coords(sp, d_xyz);
   Lat g = make_lat(sp);
   k_dirichlet_coords<<<nblk(sp->ndir, 256), 256, 0, sp->mesh->ctx->stream>>>(g, sp->ndir, sp->d_dir2lat,
                                                                               sp->mesh->d_coords, d_xyz);

@@ -76,22 +76,28 @@ class SerialTriangulation:
     ``from_mesh_data_files``, ``from_arrays``)."""
 
     def __init__(self, ctx: Context, n, limits=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), vertex_xyz=None):
+        """``n`` of length 3 gives hexahedra, of length 2 quadrilaterals (num_dims = 2); vertex
+        coordinates are 3 per vertex in both cases (z ignored in 2D)."""
         self.ctx = ctx
         self.unstructured = False
-        self.n = [int(v) for v in n]
+        self.num_dims = len(n)
+        if self.num_dims not in (2, 3):
+            raise ValueError("n must have 2 or 3 entries")
+        self.n = [int(v) for v in n] + ([1] if self.num_dims == 2 else [])
         nn = (C.c_int32 * 3)(*self.n)
-        lim = (C.c_double * 6)(*[float(v) for v in limits])
+        lim = list(limits) + [0.0, 0.0] * (3 - len(limits) // 2)
+        lim = (C.c_double * 6)(*[float(v) for v in lim[:6]])
         vx = None
+        nverts = (self.n[0] + 1) * (self.n[1] + 1) * (self.n[2] + 1 if self.num_dims == 3 else 1)
         if vertex_xyz is not None:
             vx = np.ascontiguousarray(vertex_xyz, dtype=np.float64)
-            expected = 3 * (self.n[0] + 1) * (self.n[1] + 1) * (self.n[2] + 1)
-            if vx.size != expected:
-                raise ValueError(f"vertex_xyz must hold {expected} values")
+            if vx.size != 3 * nverts:
+                raise ValueError(f"vertex_xyz must hold {3 * nverts} values")
         h = C.c_void_p()
-        L.check(L.lib().fg_mesh_create_structured(ctx.h, 3, nn, lim, _ptr(vx), C.byref(h)),
+        L.check(L.lib().fg_mesh_create_structured(ctx.h, self.num_dims, nn, lim, _ptr(vx), C.byref(h)),
                 "fg_mesh_create_structured")
         self.h = h
-        self.num_cells = self.n[0] * self.n[1] * self.n[2]
+        self.num_cells = self.n[0] * self.n[1] * (self.n[2] if self.num_dims == 3 else 1)
 
     @classmethod
     def _wrap(cls, ctx, h):
@@ -99,6 +105,7 @@ class SerialTriangulation:
         self.ctx = ctx
         self.h = h
         self.unstructured = True
+        self.num_dims = 3
         self.n = None
         self.num_cells = self.info()["num_cells"]
         return self
