@@ -151,6 +151,110 @@ __global__ void __launch_bounds__(128)
   o[7] = 0.0;
 }
 
+// Quadrilaterals (2D): the same norms with the bilinear map (n = 2 branch of invmtx) and the
+// 2D analytic functions.
+__device__ double exact_value_2d(int fn, const double* prm, const double* x) {
+  switch (fn) {
+    case FG_FN_CONST: return prm[0];
+    case FG_FN_LINEAR: return x[0] + x[1];
+    case FG_FN_SHARP_WAVE: {
+      const double dx = x[0] - prm[2], dy = x[1] - prm[3];
+      return atan(prm[0] * (sqrt(dx * dx + dy * dy) - prm[1]));
+    }
+    default: return 0.0;
+  }
+}
+
+__device__ void exact_gradient_2d(int fn, const double* prm, const double* x, double* g) {
+  g[0] = g[1] = 0.0;
+  if (fn == FG_FN_LINEAR) {
+    g[0] = g[1] = 1.0;
+  } else if (fn == FG_FN_SHARP_WAVE) {
+    const double a = prm[0];
+    const double d[2] = {x[0] - prm[2], x[1] - prm[3]};
+    const double r = sqrt(d[0] * d[0] + d[1] * d[1]);
+    const double t = r - prm[1];
+    const double s = a / (r * (a * a * t * t + 1.0));
+    g[0] = s * d[0];
+    g[1] = s * d[1];
+  }
+}
+
+template <int P>
+__global__ void __launch_bounds__(128)
+    k_cell_errors_2d(ErrGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
+                     const int32_t* __restrict__ latdof, const double* __restrict__ x,
+                     const double* __restrict__ gvals, const double* __restrict__ coef, double coef_const, int fn,
+                     const double* __restrict__ prm_g, double* __restrict__ C) {
+  constexpr int NP1 = P + 1, NN = NP1 * NP1, NQ = NN;
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  double prm[8];
+  for (int i = 0; i < 8; ++i) prm[i] = prm_g[i];
+  const int ci = (int)(c % g.n[0]), cj = (int)(c / g.n[0]);
+  double xv[8];
+  for (int k = 0; k < 4; ++k) {
+    const int64_t v = (int64_t)(ci + (k & 1)) + (int64_t)(g.n[0] + 1) * (cj + (k >> 1));
+    xv[k * 2 + 0] = coords[v * 3 + 0];
+    xv[k * 2 + 1] = coords[v * 3 + 1];
+  }
+  double u[NN];
+  for (int s = 0; s < NN; ++s) {
+    const int64_t L = (int64_t)(P * ci + s % NP1) + (int64_t)g.Ln[0] * (P * cj + s / NP1);
+    const int32_t id = latdof[L];
+    u[s] = id > 0 ? x[id - 1] : (id < 0 ? gvals[-id - 1] : 0.0);
+  }
+  const double kc = coef ? coef[c] : coef_const;
+  double mean = 0.0, l1 = 0.0, l2 = 0.0, linf = 0.0, h1 = 0.0, w1inf = 0.0;
+  bool neg = false;
+  for (int q = 0; q < NQ; ++q) {
+    double J[2][2];  // J[l][j] = sum_k dN_k/dxi_j x_k(l)
+    for (int j = 0; j < 2; ++j)
+      for (int l = 0; l < 2; ++l) {
+        double acc = 0.0;
+        for (int k = 0; k < 4; ++k) acc = acc + tb.gshg[(k * NQ + q) * 3 + j] * xv[k * 2 + l];
+        J[l][j] = acc;
+      }
+    const double det = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+    const double dn = 1.0 / det;
+    const double b11 = J[1][1] * dn, b21 = -J[1][0] * dn, b12 = -J[0][1] * dn, b22 = J[0][0] * dn;
+    if (q == 0) neg = det < 0.0;
+    const double factor = (neg ? fabs(det) : det) * tb.qw[q];
+    double xq[2] = {0.0, 0.0};
+    for (int k = 0; k < 4; ++k) {
+      const double a = tb.gshp[k * NQ + q];
+      xq[0] = xq[0] + a * xv[k * 2 + 0];
+      xq[1] = xq[1] + a * xv[k * 2 + 1];
+    }
+    double uh = 0.0, gh[2] = {0.0, 0.0};
+    for (int s = 0; s < NN; ++s) {
+      uh = uh + u[s] * tb.shp[s * NQ + q];
+      const double r0 = tb.shg[(s * NQ + q) * 3 + 0], r1 = tb.shg[(s * NQ + q) * 3 + 1];
+      gh[0] = gh[0] + u[s] * (b11 * r0 + b21 * r1);
+      gh[1] = gh[1] + u[s] * (b12 * r0 + b22 * r1);
+    }
+    const double e = exact_value_2d(fn, prm, xq) - uh;
+    double ge[2];
+    exact_gradient_2d(fn, prm, xq, ge);
+    const double e0 = ge[0] - gh[0], e1 = ge[1] - gh[1];
+    mean = mean + e * factor;
+    l1 = l1 + fabs(e) * factor;
+    l2 = l2 + (e * e) * factor;
+    linf = fmax(linf, fabs(e));
+    h1 = h1 + (e0 * e0 + e1 * e1) * factor;
+    w1inf = fmax(w1inf, fmax(fabs(e0), fabs(e1)));
+  }
+  double* o = C + c * kNC;
+  o[0] = mean;
+  o[1] = l1;
+  o[2] = l2;
+  o[3] = linf;
+  o[4] = h1;
+  o[5] = w1inf;
+  o[6] = kc * h1;
+  o[7] = 0.0;
+}
+
 // One block: column sums (max for linf / w1inf) over the cells, fixed order.
 __global__ void __launch_bounds__(512) k_reduce_errors(int64_t ncells, const double* __restrict__ C, double* out) {
   __shared__ double sh[kNC][512];
@@ -191,8 +295,8 @@ extern "C" fg_status fg_system_error_norms(fg_system* sys, const double* x, int3
   }
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
-  if (sp->ncomp != 1 || sp->mesh->dim != 3) {
-    set_error("error norms are built for scalar fields on 3D meshes");
+  if (sp->ncomp != 1) {
+    set_error("error norms are built for scalar fields");
     return FG_ERR_UNSUPPORTED;
   }
   if (fn != FG_FN_ZERO && fn != FG_FN_CONST && fn != FG_FN_LINEAR && fn != FG_FN_SHARP_WAVE) {
@@ -230,7 +334,17 @@ extern "C" fg_status fg_system_error_norms(fg_system* sys, const double* x, int3
     const unsigned blocks = (unsigned)((nc + 127) / 128);
     const double* coef = sys->d_coef;
     const double cc = sys->integ.coef_const;
-    if (nc > 0) {
+    if (nc > 0 && sp->mesh->dim == 2) {
+      if (sp->order == 1)
+        k_cell_errors_2d<1><<<blocks, 128, 0, st>>>(g, nc, sp->mesh->d_coords, sp->dtab, sp->d_latdof, xx,
+                                                    sys->d_gvals, coef, cc, fn, dprm, dC);
+      else if (sp->order == 2)
+        k_cell_errors_2d<2><<<blocks, 128, 0, st>>>(g, nc, sp->mesh->d_coords, sp->dtab, sp->d_latdof, xx,
+                                                    sys->d_gvals, coef, cc, fn, dprm, dC);
+      else
+        k_cell_errors_2d<3><<<blocks, 128, 0, st>>>(g, nc, sp->mesh->d_coords, sp->dtab, sp->d_latdof, xx,
+                                                    sys->d_gvals, coef, cc, fn, dprm, dC);
+    } else if (nc > 0) {
       if (sp->order == 1)
         k_cell_errors<1><<<blocks, 128, 0, st>>>(g, nc, sp->mesh->d_coords, sp->dtab, sp->d_latdof, xx, sys->d_gvals,
                                                  coef, cc, fn, dprm, dC);
@@ -240,6 +354,8 @@ extern "C" fg_status fg_system_error_norms(fg_system* sys, const double* x, int3
       else
         k_cell_errors<3><<<blocks, 128, 0, st>>>(g, nc, sp->mesh->d_coords, sp->dtab, sp->d_latdof, xx, sys->d_gvals,
                                                  coef, cc, fn, dprm, dC);
+    }
+    if (nc > 0) {
       k_reduce_errors<<<1, 512, 0, st>>>(nc, dC, dout);
       ctx->launches += 2;
       if (cell_sq_energy) {

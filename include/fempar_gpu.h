@@ -147,8 +147,8 @@ fg_status fg_ctx_kernel_launches(fg_ctx* ctx, int64_t* count);
  * num_dims = 2: quadrilaterals of [lim0,lim1]x[lim2,lim3] with n[0]*n[1] cells (n[2] ignored),
  * vertex_xyz of 3*(n0+1)(n1+1) values (z ignored), bilinear map, boundary set ids 1..8 (the
  * generator's 2D polytope order; 9 interior).  On 2D meshes: continuous spaces (Poisson, ncomp
- * 1; plane-strain elasticity, ncomp 2) of orders 1-3, assembly, CSR export and the solvers;
- * the dG space, BDDC, partitions and error norms return FG_ERR_UNSUPPORTED.
+ * 1; plane-strain elasticity, ncomp 2) of orders 1-3, assembly, CSR export, the solvers and
+ * error norms; the dG space, BDDC and partitions return FG_ERR_UNSUPPORTED.
  * Replaces uniform_hex_mesh_t%generate_part_local_mesh + serial_triangulation_t%create
  * (Sources/Lib/Geometry/Tools/uniform_hex_mesh_generator.f90:145-647,
  *  Sources/Lib/Geometry/Triangulation/sbm_serial_triangulation.i90:29-201). */

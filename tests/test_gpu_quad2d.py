@@ -122,6 +122,36 @@ def test_elasticity_2d(fg, ctx, order):
     check_solution(fg, op, P)
 
 
+@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("fn", ["sharp", "linear"])
+def test_error_norms_2d_match_oracle(fg, ctx, order, fn):
+    """Device error norms on quadrilaterals against the oracle's 2D evaluation of the same
+    solution vector (error_norms_scalar_t, sbm_error_norms_scalar.i90:67-241)."""
+    n = (6, 5)
+    xyz = perturbed2(n, 0.2, seed=40 + order)
+    f = fg.FG_FN_SHARP_WAVE if fn == "sharp" else fg.FG_FN_LINEAR
+    prm = SHARP if fn == "sharp" else []
+    tri = fg.SerialTriangulation(ctx, n, vertex_xyz=xyz)
+    sp = fg.SerialFESpace(tri, order=order, dirichlet_ids=ALL2)
+    src = fg.FG_FN_SHARP_WAVE if fn == "sharp" else fg.FG_FN_ZERO
+    op = fg.FEAffineOperator(sp, fg.PoissonIntegration(source_fn=src, boundary_fn=f, fn_param=prm)).compute()
+    s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
+    s.set_parameters_from_pl({"ILS_RTOL": 1e-12, "ILS_MAX_NUM_ITERATIONS": 100000})
+    x = s.solve()
+    d, cells = op.error_norms(x, f, prm, cell_sq_energy=True)
+    P = O.Problem(n, order=order, num_dims=2, dirichlet_ids=ALL2, vertex_xyz=xyz,
+                  source_fn=O.FN_SHARP_WAVE if fn == "sharp" else O.FN_ZERO,
+                  boundary_fn=O.FN_SHARP_WAVE if fn == "sharp" else O.FN_LINEAR, fn_param=prm)
+    o = P.error_norms(x, O.FN_SHARP_WAVE if fn == "sharp" else O.FN_LINEAR, prm)
+    scale = max(o["h1_norm"], 1e-300)
+    for k, v in o.items():
+        ref = scale if k == "mean_norm" else max(abs(v), 1e-14 * scale)
+        assert abs(d[k] - v) <= 1e-12 * max(abs(ref), 1e-30) + 1e-14, (k, d[k], v)
+    assert abs(np.sqrt(cells.sum()) - d["energy_norm"]) <= 1e-12 * max(d["energy_norm"], 1e-30)
+    if fn == "linear":  # u = x + y lies in the space: the error is the solver's
+        assert d["h1_norm"] <= 1e-9
+
+
 def test_2d_unsupported_parts_report_errors(fg, ctx):
     from fempar_gb300 import FGError
     tri = fg.SerialTriangulation(ctx, (3, 3))
