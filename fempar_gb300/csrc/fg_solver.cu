@@ -284,14 +284,35 @@ __global__ void __launch_bounds__(RB)
   }
 }
 
-// p = z + beta p
+// p = z + beta p (FP32: four entries per thread and load; the vectors are 16-byte aligned)
 template <typename T, bool PRECOND>
 __global__ void __launch_bounds__(RB)
     k_pupdate(int64_t n, T* __restrict__ p, const T* __restrict__ r, const T* __restrict__ idiag, const double* S,
               const int* I) {
   if (I[I_DONE]) return;
   const T beta = (T)S[S_BETA];
-  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+  const int64_t t0 = blockIdx.x * (int64_t)RB + threadIdx.x, stride = (int64_t)gridDim.x * RB;
+  int64_t head = 0;
+  if (sizeof(T) == 4) {
+    const int64_t n4 = n >> 2;
+    head = n4 << 2;
+    float4* p4 = reinterpret_cast<float4*>(p);
+    const float4* r4 = reinterpret_cast<const float4*>(r);
+    const float4* d4 = reinterpret_cast<const float4*>(idiag);
+    const float b = (float)beta;
+    for (int64_t i = t0; i < n4; i += stride) {
+      const float4 ri = r4[i];
+      float4 pi = p4[i];
+      float4 di = make_float4(1.f, 1.f, 1.f, 1.f);
+      if (PRECOND) di = d4[i];
+      pi.x = fmaf(b, pi.x, PRECOND ? di.x * ri.x : ri.x);
+      pi.y = fmaf(b, pi.y, PRECOND ? di.y * ri.y : ri.y);
+      pi.z = fmaf(b, pi.z, PRECOND ? di.z * ri.z : ri.z);
+      pi.w = fmaf(b, pi.w, PRECOND ? di.w * ri.w : ri.w);
+      p4[i] = pi;
+    }
+  }
+  for (int64_t i = head + t0; i < n; i += stride) {
     const T ri = r[i];
     const T zi = PRECOND ? idiag[i] * ri : ri;
     p[i] = fmaT(beta, p[i], zi);
@@ -306,7 +327,43 @@ __global__ void __launch_bounds__(RB)
   if (I[I_DONE]) return;
   const float a = (float)S[S_ALPHA];
   Acc<float> rr, rz;
-  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+  // four entries per thread and load (the vectors are 16-byte aligned), then the tail
+  const int64_t t0 = blockIdx.x * (int64_t)RB + threadIdx.x, stride = (int64_t)gridDim.x * RB;
+  const int64_t n4 = n >> 2;
+  {
+    float4* x4 = reinterpret_cast<float4*>(x);
+    float4* r4 = reinterpret_cast<float4*>(r);
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+    const float4* a4 = reinterpret_cast<const float4*>(Ap);
+    const float4* d4 = reinterpret_cast<const float4*>(idiag);
+    for (int64_t i = t0; i < n4; i += stride) {
+      float4 xi = x4[i], ri = r4[i];
+      const float4 pi = p4[i], api = a4[i];
+      float4 di = make_float4(1.f, 1.f, 1.f, 1.f);
+      if (PRECOND) di = d4[i];
+      xi.x = fmaf(a, pi.x, xi.x);
+      xi.y = fmaf(a, pi.y, xi.y);
+      xi.z = fmaf(a, pi.z, xi.z);
+      xi.w = fmaf(a, pi.w, xi.w);
+      ri.x = fmaf(-a, api.x, ri.x);
+      ri.y = fmaf(-a, api.y, ri.y);
+      ri.z = fmaf(-a, api.z, ri.z);
+      ri.w = fmaf(-a, api.w, ri.w);
+      x4[i] = xi;
+      r4[i] = ri;
+      rr.add(ri.x, ri.x);
+      rr.add(ri.y, ri.y);
+      rr.add(ri.z, ri.z);
+      rr.add(ri.w, ri.w);
+      if (PRECOND) {
+        rz.add(ri.x, di.x * ri.x);
+        rz.add(ri.y, di.y * ri.y);
+        rz.add(ri.z, di.z * ri.z);
+        rz.add(ri.w, di.w * ri.w);
+      }
+    }
+  }
+  for (int64_t i = (n4 << 2) + t0; i < n; i += stride) {
     x[i] = fmaf(a, p[i], x[i]);
     const float ri = fmaf(-a, Ap[i], r[i]);
     r[i] = ri;
@@ -524,7 +581,9 @@ static inline void launch_k(void (*k)(KA...), const Work& w, cudaStream_t st, A.
 static fg_status ensure_work(fg_system* sys, Work& w) {
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
-  const int64_t n = sp->nvec > 0 ? sp->nvec : 1;
+  // vector stride a multiple of 4 entries: every FP32 vector starts on a 16-byte boundary
+  // (the FP32 update kernels load float4)
+  const int64_t n = ((sp->nvec > 0 ? sp->nvec : 1) + 3) & ~(int64_t)3;
   if (!sys->d_work) {
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_work, sizeof(double) * 6 * n));
     FG_TRY(dev_alloc(ctx, (void**)&sys->d_work32, sizeof(float) * 4 * n));
