@@ -349,3 +349,26 @@ def test_fast_integration_matrix_and_mixed_solution(fg, ctx, order):
     np.maximum.at(scale, rows, np.abs(v64))
     assert (np.abs(vff - v64) / scale[rows]).max() <= 1e-12
     assert np.linalg.norm(sols[1] - sols[0]) <= 1e-9 * np.linalg.norm(sols[0])
+
+
+def test_plain_method_32_q1_sharp_wave(fg, ctx):
+    """The reference's CPU-runnable case at its size: Poisson on the unit cube, 32^3 Q1, the
+    sharp circular wave u = atan(50(|x - c| - 0.7)), c = (-0.05, -0.05, -0.05), as Dirichlet
+    data and source, unpreconditioned CG to 1e-8 from x0 = 0.  Numbering, pattern, entries,
+    iteration count (+-1) and solution against the oracle."""
+    n = (32, 32, 32)
+    P, tri, sp, op = build_pair(fg, ctx, n, 1, source_fn=O.FN_SHARP_WAVE, boundary_fn=O.FN_SHARP_WAVE,
+                                fn_param=SHARP)
+    assert sp.num_free_dofs == P.nfree == 29791
+    assert np.array_equal(sp.get_dof_map(), P.dof_map())
+    irp, ja, val = op.get_matrix()
+    assert_matrix_close(irp, ja, val, P)
+    b, ob = op.get_translation(), P.rhs()
+    assert np.max(np.abs(b - ob)) <= RHS_TOL * np.max(np.abs(ob))
+    ref = P.cg(precond=0, rtol=1e-8, maxit=100000)
+    s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "identity")
+    s.set_parameters_from_pl({"ILS_RTOL": 1e-8, "ILS_MAX_NUM_ITERATIONS": 100000})
+    x = s.solve()
+    assert s.info()["converged"]
+    assert abs(s.info()["iterations"] - ref["iters"]) <= 1, (s.info()["iterations"], ref["iters"])
+    assert np.linalg.norm(x - ref["x"]) <= 1e-9 * np.linalg.norm(ref["x"])
