@@ -437,7 +437,17 @@ __global__ void __launch_bounds__(RB)
 // ---------------------------------------------------------------------------
 // Lattice-implicit SELL SpMV: warp per slice, lane per row, 4 values per lane per load;
 // the column of box position k is the row's node plus the class offset k.
-static constexpr int kPrefetch = 8;  // value groups (of 4 entries per lane) prefetched ahead
+// L2 prefetch distance of the FP32 SpMV's value stream, in groups of 4 entries per lane.
+// Swept on GB300 at 128^3 Q2 (unroll 2): 2-4 groups 0.731-0.735 ms per launch, 6 0.747,
+// 8 0.757, 16 0.810.
+#ifndef FG_SPMV_PREFETCH
+#define FG_SPMV_PREFETCH 3
+#endif
+#ifndef FG_SPMV_UNROLL
+#define FG_SPMV_UNROLL 2
+#endif
+static constexpr int kPrefetch = FG_SPMV_PREFETCH;  // value groups (of 4 entries per lane) prefetched ahead
+static constexpr int kUnroll = FG_SPMV_UNROLL;      // value groups per unrolled step
 template <typename T, int MODE>
 __global__ void __launch_bounds__(RB)
     k_stencil_spmv(int64_t nslices, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
@@ -464,7 +474,7 @@ __global__ void __launch_bounds__(RB)
     const T* xb = x + base;
     T acc = 0;
     const int w4 = Bp >> 2;
-#pragma unroll 2
+#pragma unroll kUnroll
     for (int j = 0; j < w4; ++j) {
       // FP32: keep the value stream ahead of the gathers by asking L2 for this lane's values
       // kPrefetch groups ahead (no registers held; a hint only, kept inside the slice).  The
