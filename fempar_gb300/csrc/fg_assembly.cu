@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
                         double* __restrict__ E, double* __restrict__ EV) {
   using S = typename PoissonShapeSel<P, FF>::type;
   constexpr bool STREAM = FF && P <= 2;
-  constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND, NP1 = S::NP1;
+  constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND;
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   double* base = smem + (size_t)wib * (S::SM_BYTES_WARP / 8);
@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(ElastShape<P>::WARPS * 32)
                            const double* __restrict__ coef, double coef_const, double nu, SourceSpec src,
                            double* __restrict__ E, double* __restrict__ EV) {
   using S = ElastShape<P>;
-  constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND, NP1 = S::NP1;
+  constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND;
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   double* base = smem + (size_t)wib * (S::SM_BYTES_WARP / 8);
