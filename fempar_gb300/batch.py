@@ -113,11 +113,6 @@ def lattice_index_map(dof_map, n, p):
     return out
 
 
-def interior_to_free(problem_oracle, n, p):
-    """lattice_index_map for an oracle problem (test helper)."""
-    return lattice_index_map(problem_oracle.dof_map(), n, p)
-
-
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--count", type=int, default=4096)

@@ -1,20 +1,25 @@
 // fg_noalloc.cu -- fg_system_spmv_device_noalloc: y = A x without any device allocation.
 //
-// For callers that cannot call cudaMalloc: work inside a CUDA stream capture (cudaMalloc
-// is not capturable), serving loops that reserve all of their HBM up front, host
-// frameworks whose caching allocator owns the device memory.  fg_system_spmv_device
-// stages x and y in the solver's padded vector layout inside work buffers that the system
-// allocates the first time they are needed; this variant stages them in the file-scope
-// device array below instead, so a call allocates nothing.
+// For callers that cannot call cudaMalloc: serving loops that reserve all of their HBM up
+// front and may not grow it, and host frameworks whose caching allocator owns the device
+// memory (a cudaMalloc behind its back can fail or fragment its pool).
+// fg_system_spmv_device stages x and y in the solver's padded vector layout inside work
+// buffers that the system allocates the first time they are needed; this variant stages
+// them in the file-scope device array below instead, so a call allocates nothing.
 //
 // The array is FG_NOALLOC_SCRATCH_BYTES (32 MiB) on every GPU that loads the library,
-// held until the process exits.  Its host-side name is only a stand-in: host code must
-// not pass `g_noalloc_scratch` to a kernel.  The first call on a device looks up the
+// held until the process exits.  With lazy module loading (the CUDA default) the module,
+// and with it the array, is loaded on a device at the first call there; that takes 32 MiB
+// outside the context's HBM budget, so a caller that reserves its HBM up front makes the
+// first call before reserving.  The array's host-side name is only a stand-in: host code
+// must not pass `g_noalloc_scratch` to a kernel.  The first call on a device looks up the
 // array's device address there with cudaGetSymbolAddress (once per device, with that
 // device current) and caches it; make that first call before any stream capture.  All
-// calls share the array and it keeps the last call's contents, so every call first
-// clears the part of the staged x vector that must read zero (entries of nodes that are
-// not free dofs).  Calls that overlap on the GPU race on the array.
+// calls share the array and it keeps the last call's contents, so every call first clears
+// the part of the staged x vector that must read zero (entries of nodes that are not free
+// dofs).  Calls that overlap on the GPU race on the array.  The call is synchronous: it
+// waits on the context's stream until y holds the result, and leaves the caller's current
+// device as it found it.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -109,14 +114,27 @@ extern "C" fg_status fg_system_spmv_device_noalloc(fg_system* sys, int precision
               need, (long long)sp->nvec, (unsigned)FG_NOALLOC_SCRATCH_BYTES);
     return FG_ERR_BADARG;
   }
-  cudaError_t e = cudaSetDevice(ctx->device);
+  if (sp->nfree == 0) return FG_OK;  // nothing to multiply (all dofs Dirichlet), as fg_system_spmv_device
+  int prev = -1;
+  cudaError_t e = cudaGetDevice(&prev);
+  if (e != cudaSuccess) {
+    set_error("cudaGetDevice: %s", cudaGetErrorString(e));
+    return FG_ERR_CUDA;
+  }
+  e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) {
     set_error("cudaSetDevice: %s", cudaGetErrorString(e));
     return FG_ERR_CUDA;
   }
   void* scratch = nullptr;
-  FG_TRY(scratch_address(ctx->device, &scratch));
-  if (precision == FG_MIXED)
-    return spmv_noalloc<float>(sys, precision, (const float*)x, (float*)y, (unsigned char*)scratch);
-  return spmv_noalloc<double>(sys, precision, (const double*)x, (double*)y, (unsigned char*)scratch);
+  fg_status st = scratch_address(ctx->device, &scratch);
+  if (st == FG_OK) {
+    if (precision == FG_MIXED)
+      st = spmv_noalloc<float>(sys, precision, (const float*)x, (float*)y, (unsigned char*)scratch);
+    else
+      st = spmv_noalloc<double>(sys, precision, (const double*)x, (double*)y, (unsigned char*)scratch);
+  }
+  // the caller's current device is left as it was
+  if (prev != ctx->device) cudaSetDevice(prev);
+  return st;
 }

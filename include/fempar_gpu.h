@@ -247,21 +247,25 @@ fg_status fg_system_spmv_device(fg_system* sys, int precision, const void* x, vo
 /* y = A x like fg_system_spmv_device, for callers that must not allocate device memory.
  * No counterpart in the reference: FEMPAR's sparse_matrix_t%apply runs on host arrays.
  *
- * Who needs it: a caller inside a CUDA stream capture (cudaMalloc is not capturable), a
- * serving loop that pre-reserves all of its HBM and may not grow it, or a host framework
- * whose caching allocator owns the device memory.  fg_system_spmv_device stages x and y
- * in the solver's padded layout in work buffers the system allocates on first use; this
- * variant stages them instead in one file-scope device array of FG_NOALLOC_SCRATCH_BYTES
- * (32 MiB) that the library holds on every GPU that loads it, until the process exits.
+ * Who needs it: a serving loop that pre-reserves all of its HBM and may not grow it, or a
+ * host framework whose caching allocator owns the device memory (a cudaMalloc behind its
+ * back can fail or fragment its pool).  fg_system_spmv_device stages x and y in the
+ * solver's padded layout in work buffers the system allocates on first use; this variant
+ * stages them instead in one file-scope device array of FG_NOALLOC_SCRATCH_BYTES (32 MiB)
+ * that the library holds on every GPU that loads it, until the process exits.  With lazy
+ * module loading (the CUDA default) that array is loaded on a device at the first call
+ * there, outside the context's HBM budget: make the first call before reserving HBM.
  *
  * Limit: 2 * fg_space_info.solver_vec_len * (8 for FG_FP64, 4 for FG_MIXED) bytes must fit
  * the array (solver_vec_len <= 2,097,152 in FP64, <= 4,194,304 in FP32); larger systems are
  * rejected with FG_ERR_BADARG and a message in fg_last_error().  x and y are device
- * pointers of num_free entries (double, or float for FG_MIXED).
+ * pointers of num_free entries (double, or float for FG_MIXED).  A system without free
+ * dofs returns FG_OK at once.
  * The first call on a device looks up the array's device address there (once per
  * device), so make that first call before any stream capture.  All calls share the one
  * array: calls that overlap on the GPU (other host threads, other contexts of the same
- * device) race on it; serialise them.  The call returns after the result is in y.
+ * device) race on it; serialise them.  The call is synchronous (it returns after the
+ * result is in y) and leaves the caller's current device unchanged.
  * Calls no cudaMalloc/cudaFree and no allocating library routine. */
 #define FG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 fg_status fg_system_spmv_device_noalloc(fg_system* sys, int precision, const void* x, void* y);

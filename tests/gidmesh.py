@@ -9,8 +9,12 @@ shape of the reference's GiD test meshes.  Arrays use the keys of ``oracle.gid.r
 from __future__ import annotations
 
 import itertools
+import json
+import os
 
 import numpy as np
+
+GOLDEN_GID = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gid_cube_hexas.json")
 
 PERMU_3DQ1 = (1, 2, 4, 3, 5, 6, 8, 7)
 
@@ -254,3 +258,13 @@ def cube_in_cube(refine=0, inner=(0.3, 0.7), seed=None):
             "bvef_verts": np.array([v for g in given for v in g[0]], dtype=np.int32),
             "bvef_set": np.array([g[1] for g in given], dtype=np.int32),
             "bvef_geo": np.ones(len(given), np.int32)}
+
+
+def reference_mesh(name):
+    """The reference's cube_hexas GiD mesh of test `name` ("test_poisson" or "par_test_poisson"),
+    as tests/golden/make_golden.py parsed it from
+    Sources/Tests/Data/<name>/cube_hexas.gid/cube_hexas.mesh (keys of ``oracle.gid.read_gid``)."""
+    m = json.load(open(GOLDEN_GID))["meshes"][name]
+    types = {"coords": np.float64, "cells": np.int32, "cell_set": np.int32, "cell_geo": np.int32,
+             "bvef_ptr": np.int64, "bvef_verts": np.int32, "bvef_set": np.int32, "bvef_geo": np.int32}
+    return {"dim": m["dim"], **{k: np.asarray(m[k], dtype=t) for k, t in types.items()}}

@@ -12,16 +12,22 @@ Reads the reference's own test data as text (nothing of the reference is run):
   ``tutorial01_convergence.json``.
 * ``Sources/Tests/Data/par_test_pb_bddc_linear_elasticity/test1_convergence`` --
   the BDDC elasticity CG iteration log -> ``bddc_elasticity_iterations.json``.
+* ``Sources/Tests/Data/{test_poisson,par_test_poisson}/cube_hexas.gid/cube_hexas.mesh`` --
+  the hexahedral GiD meshes the reference's test_poisson runs, parsed by the oracle's
+  restated reader (``oracle/gid.py``) -> ``gid_cube_hexas.json``.
 
-Usage:  python tests/golden/make_golden.py [FEMPAR_ROOT]   (default /root/reference)
+Usage:  python tests/golden/make_golden.py FEMPAR_SOURCE_TREE
+        (or set FEMPAR_SOURCE_TREE in the environment)
 """
 import json
 import os
 import re
 import sys
 
-ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FEMPAR_SOURCE_TREE")
 OUT = os.path.dirname(os.path.abspath(__file__))
+if __name__ == "__main__" and not ROOT:
+    sys.exit("usage: python tests/golden/make_golden.py FEMPAR_SOURCE_TREE")
 
 
 def gauss_legendre_table():
@@ -72,10 +78,22 @@ def bddc_iterations():
             "log": lines}
 
 
+def gid_meshes():
+    sys.path.insert(0, os.path.join(OUT, "..", "..", "oracle"))
+    import gid
+    out = {}
+    for name in ("test_poisson", "par_test_poisson"):
+        rel = f"Sources/Tests/Data/{name}/cube_hexas.gid/cube_hexas.mesh"
+        m = gid.read_gid(os.path.join(ROOT, rel))
+        out[name] = {"source": rel, **{k: (v.tolist() if hasattr(v, "tolist") else v) for k, v in m.items()}}
+    return {"reader": "oracle/gid.py (mesh.f90:337-486 restated)", "meshes": out}
+
+
 if __name__ == "__main__":
     for name, fn in (("gauss_legendre_table.json", gauss_legendre_table),
                      ("tutorial01_convergence.json", convergence_tables),
-                     ("bddc_elasticity_iterations.json", bddc_iterations)):
+                     ("bddc_elasticity_iterations.json", bddc_iterations),
+                     ("gid_cube_hexas.json", gid_meshes)):
         with open(os.path.join(OUT, name), "w") as f:
             json.dump(fn(), f, indent=1)
         print("wrote", name)

@@ -46,8 +46,8 @@ def oracle_solution(q):
     if P.nfree == 0:
         return np.zeros(0)
     ref = P.cg(precond=1, rtol=1e-13, maxit=100000)
-    from fempar_gb300.batch import interior_to_free
-    idx = interior_to_free(P, n, p)
+    from fempar_gb300.batch import lattice_index_map
+    idx = lattice_index_map(P.dof_map(), n, p)
     return ref["x"][idx]
 
 

@@ -7,16 +7,13 @@ method reproduces linear solutions only if the facet normals point the right way
 sides, the two cells' traces meet at the same physical points and the Nitsche terms carry
 the data, so the check pins the facet geometry.  Bar here: 1e-10.
 """
-import os
 
 import numpy as np
 import pytest
 
-import gid
 import gidmesh
 import oracle as O
 
-REF = "/root/reference/Sources/Tests/Data/test_poisson/cube_hexas.gid/cube_hexas.mesh"
 
 
 def linear_errors(P):
@@ -54,9 +51,7 @@ def test_unstructured_dg_recovers_linear_solution(order):
 
 @pytest.mark.parametrize("order", [1, 2, 3])
 def test_reference_gid_cube_dg(order):
-    if not os.path.exists(REF):
-        pytest.skip("reference test data not present")
-    e = linear_errors(O.UProblem(gid.read_gid(REF), order=order, dirichlet_ids=(), formulation=O.DG,
+    e = linear_errors(O.UProblem(gidmesh.reference_mesh("test_poisson"), order=order, dirichlet_ids=(), formulation=O.DG,
                                  source_fn=O.FN_ZERO, boundary_fn=O.FN_LINEAR))
     for k in ("mean_norm", "l1_norm", "l2_norm", "linfty_norm", "h1_seminorm", "w1infty_seminorm"):
         assert abs(e[k]) < 1e-10, (k, e[k])

@@ -8,7 +8,6 @@ Sources/Tests/Scripts/test_poisson:215-235).  The exact recovery needs the bound
 handed from faces to their edges and vertices and conforming own-dof permutations, so the
 same check on meshes with every cell orientation pins both.  Bar here: 1e-10.
 """
-import os
 
 import numpy as np
 import pytest
@@ -17,14 +16,8 @@ import gid
 import gidmesh
 import oracle as O
 
-REF_DATA = "/root/reference/Sources/Tests/Data"
-
-
 def ref_mesh(name):
-    path = os.path.join(REF_DATA, name, "cube_hexas.gid", "cube_hexas.mesh")
-    if not os.path.exists(path):
-        pytest.skip("reference test data not present")
-    return gid.read_gid(path)
+    return gidmesh.reference_mesh(name)
 
 
 def exact_linear_errors(mesh, order):
