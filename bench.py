@@ -15,7 +15,10 @@ drop-in is timed beside it.  e2e = the same through the public API with host buf
 per-cell coefficients copied in from pinned host memory and the solution copied out.
 
 --impl reference times the reference's CPU path (the C++ restatement in oracle/, the
-reference itself is Fortran and cannot be built here) on all host cores.
+reference itself is Fortran and cannot be built here) on all host cores: one complete solve
+of the full workload.  The GPU arm's cpu_baseline is the same full-size oracle run, continued
+to rtol 1e-13 to give the oracle solution the GPU solutions are compared with
+(error_vs_oracle).
 """
 from __future__ import annotations
 
@@ -35,9 +38,6 @@ sys.path.insert(0, ROOT)
 
 SEED = 20261203
 METRIC = "DOF/s to 1e-8 rel. residual, mixed vs plain FP64 on GB300; p50/p99 solve latency"
-# Jacobi-PCG iterations of this exact workload in FP64 (measured by the GPU arm of this
-# benchmark; the same algorithm on the CPU takes the same number of iterations).
-CFG2_FP64_ITERS = 1012
 
 
 def workload(n, seed=SEED):
@@ -127,50 +127,122 @@ def peaks():
         return None
 
 
-def cpu_baseline(iters_full, n_full, m=16, cg_iters=40, nthreads=1):
-    """Oracle on a bounded sample, scaled to the full workload by cells, nnz and iterations."""
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def workload_config(n, nfree, nnz_full, nnz_upper):
+    """The workload's description; both arms print exactly this dict (no run-dependent values)."""
+    b32, b64 = spmv_bytes(nfree, nnz_full, True), csr_bytes(nfree, nnz_full, False)
+    return {"workload": f"poisson_q2_{n}^3_perturbed_lognormal_jacobi_pcg_1e-8", "n": n, "order": 2,
+            "num_free_dofs": nfree, "nnz_full": nnz_full, "nnz_upper": nnz_upper, "precond": "jacobi",
+            "rtol": 1e-8, "criterion": "res_res, x0 = 0", "geometry": "interior vertices U(+-0.15h), trilinear",
+            "coefficient": "k = exp(N(0,1)) per cell", "source": "f = 1", "dirichlet": "u = 0 on the whole boundary",
+            "seed": SEED,
+            "l2": "inputs larger than L2 (FP32 matrix %.1f GB, FP64 CSR %.1f GB)" % (b32 / 1e9, b64 / 1e9)}
+
+
+def oracle_solve(n, nthreads, rtol, kernel="sym", maxit=200000, seed=SEED):
+    """The oracle (C++ restatement of the reference's serial path) on the full workload: mesh and
+    dof numbering, numeric assembly (element integration, COO append, sort_and_compress) and
+    Jacobi-PCG from x0 = 0, on `nthreads` host threads.  The CSR is bit-identical to the
+    serial restatement's; the threaded SpMV (the symmetric-storage kernel, or "gather": a full
+    CSR row gather) sums in another order, so iterates agree with the serial ones to rounding.
+    Returns the problem, the solve record and stage times (s)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
-    xyz, coef = workload(m, seed=SEED + 1)
-    t0 = time.perf_counter()
-    P = O.Problem([m, m, m], order=2, vertex_xyz=xyz, cell_coef=coef, source_fn=O.FN_CONST, fn_param=[1.0],
+    xyz, coef = workload(n, seed)
+    P = O.Problem([n, n, n], order=2, vertex_xyz=xyz, cell_coef=coef, source_fn=O.FN_CONST, fn_param=[1.0],
                   nthreads=nthreads)
-    t_asm = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    P.cg(precond=1, rtol=1e-30, maxit=cg_iters, nthreads=nthreads)
-    t_cg = time.perf_counter() - t0
-    ncells_full = n_full ** 3
-    nfree_full = (2 * n_full - 1) ** 3
-    # nnz of the upper layout scales with the number of lattice nodes
-    nnz_up_full = P.nnz_upper * (nfree_full / P.nfree)
-    t_full = t_asm / P.ncells * ncells_full + t_cg / (cg_iters * P.nnz_upper) * nnz_up_full * iters_full
-    return {"value": nfree_full / t_full, "unit": "DOF/s", "cores": nthreads, "kind": "port",
-            "sample": f"oracle on a {m}^3 Q2 sample of the same distribution ({P.nfree} dofs): full assembly "
-                      f"({t_asm:.2f} s) + {cg_iters} Jacobi-PCG iterations ({t_cg:.2f} s), scaled per cell and per "
-                      f"upper-CSR nonzero to {n_full}^3 with {iters_full} iterations"}
+    tm = P.timings()
+    nth = -nthreads if (kernel == "gather" and nthreads > 1) else nthreads
+    r = P.cg(precond=1, rtol=rtol, maxit=maxit, nthreads=nth, times=True, history=True)
+    bnorm = float(np.linalg.norm(P.rhs()))
+    return P, r, {"setup": float(tm["setup"]), "integrate": float(tm["integrate"]),
+                  "compress": float(tm["compress"]), "bnorm": bnorm}
+
+
+def time_to_rtol(r, bnorm, rtol):
+    """(iterations, seconds) at which the res_res test ||r_k|| <= rtol ||b|| first held, read off
+    a longer run's history (CG's iterates do not depend on its stopping test)."""
+    h = r["history"]
+    hit = np.nonzero(h <= rtol * bnorm)[0]
+    if hit.size == 0:
+        return None, None
+    k = int(hit[0])
+    return k + 1, float(r["times"][k])
+
+
+def cpu_baseline_full(n, nthreads, kernel, oracle_rtol):
+    """CPU baseline on the FULL workload (no sample, no scaling): the oracle's numeric assembly
+    plus Jacobi-PCG to rtol 1e-8, timed on `nthreads` host threads.  The PCG runs on to
+    `oracle_rtol`; the 1e-8 time is read at the iteration where the residual test first held,
+    and the solution at `oracle_rtol` is the oracle solution the GPU results are compared with."""
+    P, r, tm = oracle_solve(n, nthreads, oracle_rtol, kernel)
+    its8, t8 = time_to_rtol(r, tm["bnorm"], 1e-8)
+    t_asm = tm["integrate"] + tm["compress"]
+    rec = {"value": P.nfree / (t_asm + t8) if t8 else None, "unit": "DOF/s", "cores": nthreads, "kind": "port",
+           "sample": f"the full workload ({n}^3 Q2, {P.nfree} dofs), not a sample: oracle numeric assembly "
+                     f"({tm['integrate']:.2f} s integration + COO append, {tm['compress']:.2f} s sort_and_compress) + "
+                     f"{its8} Jacobi-PCG iterations to 1e-8 ({t8:.2f} s, {kernel} SpMV) on {nthreads} threads; "
+                     f"dof numbering ({tm['setup']:.2f} s) excluded as on the GPU",
+           "assembly_s": t_asm, "pcg_s": t8, "iterations": its8, "setup_s": tm["setup"], "threads": nthreads,
+           "spmv": kernel, "cpu": cpu_model()}
+    return P, r, rec
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return None
 
 
 def run_reference(args):
+    """The reference's CPU path (its C++ restatement: the reference is Fortran and no Fortran
+    compiler exists here) on every host thread.  Warm-up: W complete solves of a smaller mesh
+    of the same distribution.  Timed: ONE complete solve of the full workload (numeric assembly
+    + Jacobi-PCG to 1e-8); the line reports it over the K requested steps, so that
+    steps x ms_per_step is that solve's time."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    nth = os.cpu_count() or 1
-    vals = []
-    for s in range(args.warmup + args.steps):
-        cb = cpu_baseline(CFG2_FP64_ITERS, args.n, m=args.ref_m, cg_iters=20, nthreads=nth)
-        if s >= args.warmup:
-            vals.append(cb["value"])
-    v = statistics.median(vals)
-    nfree = (2 * args.n - 1) ** 3
+    nth = host_threads()
+    for _ in range(args.warmup):
+        oracle_solve(args.ref_warm_n, nth, 1e-8, args.oracle_kernel)
+    P, r, tm = oracle_solve(args.n, nth, 1e-8, args.oracle_kernel)
+    t_asm = tm["integrate"] + tm["compress"]
+    t_solve = t_asm + float(r["times"][-1])
+    v = P.nfree / t_solve
+    nnz_up = P.nnz_upper
+    cfg = workload_config(args.n, P.nfree, 2 * nnz_up - P.nfree, nnz_up)
+    ms = t_solve * 1e3 / max(1, args.steps)
     line = {"metric": METRIC, "value": v, "unit": "DOF/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": nfree / v * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (PCG64 seed {SEED})",
-            "config": {"workload": f"poisson_q{2}_{args.n}^3_perturbed_lognormal_jacobi_pcg_1e-8", "n": args.n,
-                       "order": 2, "num_free_dofs": nfree, "precision": "fp64",
-                       "note": "reference is Fortran (no compiler on the image): its path restated in C++ (oracle/)"},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": f"synthetic (PCG64 seed {SEED}): perturbed vertices U(+-0.15h), k=exp(N(0,1)) per cell, f=1",
+            "config": cfg,
+            "step_def": f"one complete solve of the workload is timed (numeric assembly {t_asm:.2f} s + "
+                        f"{r['iters']} PCG iterations {float(r['times'][-1]):.2f} s = {t_solve:.2f} s) and divided "
+                        f"over the {args.steps} steps: steps x ms_per_step = the solve time; warm-up = "
+                        f"{args.warmup} complete solves at {args.ref_warm_n}^3",
+            "solves_timed": 1, "solve_ms": t_solve * 1e3, "p50_ms": t_solve * 1e3, "p99_ms": t_solve * 1e3,
+            "iterations": r["iters"], "converged": bool(r["converged"]),
+            "assembly_ms": t_asm * 1e3, "pcg_ms": float(r["times"][-1]) * 1e3, "dof_numbering_ms": tm["setup"] * 1e3,
+            "implementation": "reference path restated in C++ (oracle/fempar_oracle.cpp; the reference is Fortran, "
+                              "no Fortran compiler on the image): COO append + sort_and_compress, upper-triangle CSR, "
+                              f"CG with Jacobi; {nth} OpenMP threads, {args.oracle_kernel} SpMV",
             "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": nth, "kind": "port",
-                             "sample": cb["sample"] + f"; OpenMP, {nth} threads"},
+                             "sample": f"the full workload ({args.n}^3), one complete solve on {nth} threads",
+                             "cpu": cpu_model()},
             "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -194,6 +266,54 @@ def replica_aggregate(dist, times_ms, units, device="cpu"):
     return [float(v) for v in t.tolist()], float(u.item())
 
 
+SHARP_WAVE = [50.0, 0.7, -0.05, -0.05, -0.05]
+
+
+def plain_method_gpu(fg, ctx, stream, reps=5):
+    """The reference's CPU-runnable case on the GPU, FP64 drop-in: Poisson on the unit cube,
+    32^3 Q1, the sharp circular wave as Dirichlet data and source, unpreconditioned CG to 1e-8
+    from x0 = 0.  DOF/s of numeric assembly + solve (CUDA events, median of `reps`)."""
+    import torch
+    tri = fg.SerialTriangulation(ctx, (32, 32, 32))
+    sp = fg.SerialFESpace(tri, order=1, dirichlet_ids=fg.ALL_BOUNDARY_IDS)
+    integ = fg.PoissonIntegration(source_fn=fg.FG_FN_SHARP_WAVE, boundary_fn=fg.FG_FN_SHARP_WAVE,
+                                  fn_param=SHARP_WAVE)
+    op = fg.FEAffineOperator(sp, integ).compute()
+    s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "identity")
+    s.set_parameters_from_pl({"ILS_RTOL": 1e-8, "ILS_MAX_NUM_ITERATIONS": 100000})
+    x = torch.empty(sp.num_free_dofs, dtype=torch.float64, device=f"cuda:{ctx.device}")
+    times = []
+    for _ in range(reps + 2):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        op.compute()
+        s.solve_device(x=x)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times[2:])
+    out = {"workload": "poisson_q1_32^3_sharp_wave_cg_1e-8 (unpreconditioned, FP64 drop-in)",
+           "num_free_dofs": sp.num_free_dofs, "value": sp.num_free_dofs / (ms * 1e-3), "unit": "DOF/s",
+           "ms_per_solve": ms, "iterations": s.info()["iterations"], "x": x.cpu().numpy()}
+    op.close()
+    return out
+
+
+def plain_method_cpu():
+    """The same case on the oracle, serial (the reference's own single-threaded path): numeric
+    assembly (integration, COO append, sort_and_compress) + CG, timed in full."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    P = O.Problem((32, 32, 32), order=1, source_fn=O.FN_SHARP_WAVE, boundary_fn=O.FN_SHARP_WAVE, fn_param=SHARP_WAVE)
+    tm = P.timings()
+    r = P.cg(precond=0, rtol=1e-8, maxit=100000, times=True)
+    t = float(tm["integrate"]) + float(tm["compress"]) + float(r["times"][-1])
+    return {"value": P.nfree / t, "unit": "DOF/s", "cores": 1, "kind": "port", "seconds": t,
+            "iterations": r["iters"], "x": r["x"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -203,7 +323,11 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-m", type=int, default=24)
+    ap.add_argument("--ref-warm-n", type=int, default=24)
+    ap.add_argument("--oracle-kernel", default="sym", choices=["sym", "gather"])
+    ap.add_argument("--oracle-rtol", type=float, default=1e-13)
+    ap.add_argument("--no-extra", action="store_true", help="skip the 32^3 Q1 and batched-problem legs")
+    ap.add_argument("--batch-count", type=int, default=4096)
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -360,29 +484,49 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    cb = None
-    if not args.no_cpu_baseline:
+    # ---- the other configurations, after the timed region (rank 0, one GPU) ----
+    cfg1, batch = None, None
+    if not args.no_extra and world == 1:
+        cfg1 = plain_method_gpu(fg, ctx, stream)
+        from fempar_gb300.batch import benchmark as batch_benchmark
+        batch = batch_benchmark(ctx, count=args.batch_count, runs=2, rtol=1e-8, check=8)
+    cb, oracle_err = None, None
+    if cfg1 is not None and not args.no_cpu_baseline:
+        c1 = plain_method_cpu()
+        xg = cfg1.pop("x")
+        cfg1["cpu_baseline"] = {k: v for k, v in c1.items() if k != "x"}
+        cfg1["error_vs_oracle"] = float(np.linalg.norm(xg - c1["x"]) / np.linalg.norm(c1["x"]))
+    elif cfg1 is not None:
+        cfg1.pop("x")
+    if not args.no_cpu_baseline and world == 1:
         try:
-            cb = cpu_baseline(iters64, n)
+            P, r, cb = cpu_baseline_full(n, host_threads(), args.oracle_kernel, args.oracle_rtol)
+            xo = r["x"]
+            no = float(np.linalg.norm(xo))
+            x64h, xmxh = x64.cpu().numpy(), xmx.cpu().numpy()
+            oracle_err = {"fp64": float(np.linalg.norm(x64h - xo) / no), "mixed": float(np.linalg.norm(xmxh - xo) / no),
+                          "oracle_rtol": args.oracle_rtol, "oracle_iterations": r["iters"],
+                          "oracle_converged": bool(r["converged"]),
+                          "def": "||x - x_oracle|| / ||x_oracle||, x_oracle = the oracle's Jacobi-PCG solution of the "
+                                 "same workload (CPU, FP64) to the rtol above; x = the GPU solutions at rtol 1e-8"}
+            del P
         except Exception as e:  # reported, never silently replaced
-            cb = {"value": None, "unit": "DOF/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+            cb = {"value": None, "unit": "DOF/s", "cores": host_threads(), "kind": "port", "sample": f"failed: {e}"}
     srt = sorted(tmx)
     line = {
         "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mx, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 matrix/SpMV/Jacobi + fp64 residual/dots/refinement",
         "data": f"synthetic (PCG64 seed {SEED}): perturbed vertices U(+-0.15h), k=exp(N(0,1)) per cell, f=1",
-        "config": {"workload": f"poisson_q2_{n}^3_perturbed_lognormal_jacobi_pcg_1e-8", "n": n, "order": 2,
-                   "num_free_dofs": nfree, "nnz_full": nnz, "nnz_upper": space.info.nnz_upper,
-                   "precond": "jacobi", "rtol": 1e-8, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (FP32 CSR %.1f GB, FP64 CSR %.1f GB)" % (b32 / 1e9, b64 / 1e9),
-                   "symbolic_s": t_symbolic},
+        "config": workload_config(n, nfree, nnz, space.info.nnz_upper),
+        "parallelism": "replicas" if world > 1 else "single", "symbolic_s": t_symbolic,
         "p50_ms": srt[len(srt) // 2], "p99_ms": srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))],
         "iterations": imx[-1]["iterations"], "outer_iterations": imx[-1]["outer_iterations"],
         "assembly_ms": ms_asm, "assembly_fp64_ms": ms_asm64,
         "mixed_integration": "float-float element matrices (FG_FAST_INTEGRATION); the fp64 arm integrates in FP64",
         "solve_ms": imx[-1]["solve_ms"],
         "error_vs_fp64": err_vs_fp64,
+        "error_vs_oracle": oracle_err,
         "fp64": {"value": v64, "ms_per_step": ms_64, "iterations": iters64, "dtype": "f64"},
         "mixed_vs_fp64": value / v64,
         "e2e": {"value": ve2e, "unit": "DOF/s", "h2d_bytes_per_step": int(coef.nbytes),
@@ -403,6 +547,7 @@ def main():
                           "ms_per_launch": ms64, "dfma_per_s": nent / (ms64 * 1e-3),
                           "format_bytes_per_launch": fmt64},
         "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches,
+        "plain_method_32_q1": cfg1, "batch": batch,
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -370,6 +370,7 @@ static void space_free(fg_space* sp) {
   dev_free(ctx, sp->d_st_scls);
   dev_free(ctx, sp->d_st_row);
   dev_free(ctx, sp->d_row2st);
+  dev_free(ctx, sp->d_st_slot2row);
   delete sp;
 }
 
@@ -598,7 +599,7 @@ static fg_status numeric_phase(fg_system* sys, const fg_integrand* g) {
     }
   }
   if (sp->layout == FG_LAYOUT_SELL) FG_TRY(system_fill_sell(sys));
-  else FG_TRY(system_fill_stencil(sys));
+  else if (!sys->direct) FG_TRY(system_fill_stencil(sys));
   FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return FG_OK;
 }
@@ -618,7 +619,9 @@ fg_status fg_assemble(fg_space* sp, const fg_integrand* g, fg_system** out) {
   const int64_t ncells = sp->mesh->ncells, nd = sp->tab.nd;
   fg_status s = FG_OK;
   auto A = [&](void** p, size_t b) { if (s == FG_OK) s = dev_alloc(ctx, p, b); };
-  A((void**)&sys->d_val, sizeof(double) * (sp->nnz > 0 ? sp->nnz : 1));
+  // the row gather writes the lattice-implicit layout directly where it can (the CSR values
+  // are then derived from it on export); otherwise it fills the CSR first
+  if (sys->lean || !stencil_direct_ok(sp)) A((void**)&sys->d_val, sizeof(double) * (sp->nnz > 0 ? sp->nnz : 1));
   if (sys->lean) {
     // solver-layout arrays are allocated after the element matrices are released
   } else if (sp->layout == FG_LAYOUT_SELL) {
@@ -677,6 +680,7 @@ fg_status fg_system_export_csr(fg_system* sys, int symmetric_storage, int one_ba
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
   FG_DEVICE_GUARD(ctx);
+  if (sys->direct) FG_TRY(system_ensure_csr(sys));
   if (!sys->d_val || !sp->d_rowptr || !sp->d_col) {
     set_error("the CSR of this system was released (FG_LEAN_SYSTEM / fg_space_release_pattern)");
     return FG_ERR_UNSUPPORTED;

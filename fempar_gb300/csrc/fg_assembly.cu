@@ -533,6 +533,135 @@ __global__ void __launch_bounds__(W * 32)
   if (lane == 0) rhs[r] = rsum;
 }
 
+// Row gather straight into the lattice-implicit layout: one block per slice (32 rows of one
+// class).  Each warp assembles rows of the slice in shared memory, in box-position order
+// (the column of position k is fixed by the class, so no search): the row's node sits in at
+// most 8 cells, visited in increasing cell index, and every position sums its contributions
+// in that order -- the reference's duplicate-summation order, so the values equal
+// k_scatter_rows' CSR values bit for bit.  A lane loads its column of every cell first
+// (latdof + element-matrix entry), then the sums run cell by cell.  The slice's 32 x Bp
+// block is then written out with consecutive threads on consecutive addresses, FP64 and
+// FP32, padding included: no clearing pass and no CSR in between.
+template <int P, int NC, int W>
+__global__ void __launch_bounds__(W * 32)
+    k_scatter_stencil(AsmGeom g, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
+                      const int32_t* __restrict__ slot2row, const int32_t* __restrict__ free2lat,
+                      const int32_t* __restrict__ latdof, const double* __restrict__ E, const double* __restrict__ EV,
+                      double* __restrict__ tval, float* __restrict__ tval32, double* __restrict__ rhs) {
+  constexpr int NP1 = P + 1, NN = NP1 * NP1 * NP1;
+  extern __shared__ double s_slice[];
+  const int64_t sl = blockIdx.x;
+  const StencilClass C = cls[scls[sl]];
+  const int Bp = C.Bp, stride = C.Bp + 4;  // +4 doubles: rows of the buffer start on shifted banks
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  for (int k = threadIdx.x; k < 32 * stride; k += W * 32) s_slice[k] = 0.0;
+  __syncthreads();
+  constexpr int ncomp = NC, ND = NN * NC;
+  constexpr int BCH = (ND + 31) / 32;  // column chunks per lane and cell
+  for (int rl = wib; rl < 32; rl += W) {
+    const int32_t r = slot2row[sl * 32 + rl];
+    if (r < 0) continue;  // padding row of the class's last slice: zeros
+    double* acc = s_slice + rl * stride;
+    const int32_t slot = free2lat[r];
+    const int64_t L = slot / ncomp;
+    const int comp = slot % ncomp;
+    const int I = (int)(L % g.Ln[0]);
+    const int J = (int)((L / g.Ln[0]) % g.Ln[1]);
+    const int K = (int)(L / ((int64_t)g.Ln[0] * g.Ln[1]));
+    int clo[3], chi[3];
+    const int IJK[3] = {I, J, K};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int cc = IJK[d] / P;
+      clo[d] = (IJK[d] % P == 0) ? cc - 1 : cc;
+      chi[d] = cc;
+      if (clo[d] < 0) clo[d] = 0;
+      if (chi[d] > g.n[d] - 1) chi[d] = g.n[d] - 1;
+    }
+    const int nci = chi[0] - clo[0] + 1, ncj = chi[1] - clo[1] + 1, nck = chi[2] - clo[2] + 1;
+    const int ncell = nci * ncj * nck;
+    double v[8][BCH];
+    int pos[8][BCH];
+    double ev[8];
+    // loads first (up to 8 cells x BCH columns per lane in flight), in increasing cell order
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      ev[q] = 0.0;
+#pragma unroll
+      for (int h = 0; h < BCH; ++h) pos[q][h] = -1;
+      if (q < ncell) {
+        const int ci = clo[0] + q % nci, cj = clo[1] + (q / nci) % ncj, ck = clo[2] + q / (nci * ncj);
+        const int64_t c = (int64_t)ci + (int64_t)g.n[0] * (cj + (int64_t)g.n[1] * ck);
+        const int a = (I - P * ci) + NP1 * ((J - P * cj) + NP1 * (K - P * ck)) + comp * NN;
+        const double* Erow = E + ((size_t)c * ND + a) * ND;
+#pragma unroll
+        for (int h = 0; h < BCH; ++h) {
+          const int b = lane + 32 * h;
+          if (b < ND) {
+            const int bnode = b % NN, bcomp = b / NN;
+            const int bi = bnode % NP1, bj = (bnode / NP1) % NP1, bk = bnode / (NP1 * NP1);
+            const int Mi = P * ci + bi, Mj = P * cj + bj, Mk = P * ck + bk;
+            const int64_t M = (int64_t)Mi + (int64_t)g.Ln[0] * (Mj + (int64_t)g.Ln[1] * Mk);
+            if (latdof[M * ncomp + bcomp] > 0) {
+              pos[q][h] = bcomp + ncomp * ((Mi - I - C.lo[0]) + C.w[0] * ((Mj - J - C.lo[1]) + C.w[1] * (Mk - K - C.lo[2])));
+              v[q][h] = Erow[b];
+            }
+          }
+        }
+        if (lane == 0) ev[q] = EV[c * ND + a];
+      }
+    }
+    double rsum = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (q < ncell) {
+        // the columns of one cell are distinct positions: lanes never collide within a cell
+#pragma unroll
+        for (int h = 0; h < BCH; ++h)
+          if (pos[q][h] >= 0) acc[pos[q][h]] = acc[pos[q][h]] + v[q][h];
+        rsum = rsum + ev[q];
+        __syncwarp();
+      }
+    }
+    if (lane == 0) rhs[r] = rsum;
+  }
+  __syncthreads();
+  const int64_t vb = C.vbase + (sl - C.sbase) * 32 * (int64_t)Bp;
+  for (int k = threadIdx.x; k < 32 * Bp; k += W * 32) {
+    const int grp = k >> 7, w = k & 127;
+    const double x = s_slice[(w >> 2) * stride + grp * 4 + (w & 3)];
+    tval[vb + k] = x;
+    tval32[vb + k] = (float)x;
+  }
+}
+
+// shared memory of k_scatter_stencil for the widest class (bytes)
+static size_t scatter_stencil_smem(const fg_space* sp) { return sizeof(double) * 32 * (size_t)(sp->st_max_bp + 4); }
+
+bool stencil_direct_ok(const fg_space* sp) {
+  return sp->layout == FG_LAYOUT_STENCIL && !sp->dg && !sp->explicit_nodes && sp->mesh->dim == 3 &&
+         sp->st_max_bp > 0 && scatter_stencil_smem(sp) <= 110 * 1024;
+}
+
+template <int P, int NC>
+static fg_status launch_scatter_stencil(fg_system* sys, const AsmGeom& g) {
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  constexpr int W = 8;
+  const size_t smem = scatter_stencil_smem(sp);
+  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_scatter_stencil<P, NC, W>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (sp->st_nslices > 0) {
+    ctx->launches += 1;
+    k_scatter_stencil<P, NC, W><<<(unsigned)sp->st_nslices, W * 32, smem, ctx->stream>>>(
+        g, sp->d_st_scls, sp->d_st_cls, sp->d_st_slot2row, sp->d_free2lat, sp->d_latdof, sys->d_elmat, sys->d_elvec,
+        sys->d_tval, sys->d_tval32, sys->d_rhs);
+    FG_CUDA_TRY(cudaGetLastError());
+  }
+  sys->direct = true;
+  return FG_OK;
+}
+
 __global__ void k_dirichlet_values(int64_t ndir, const double* xyz, int fn, SourceSpec prm, double* gv) {
   int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (d >= ndir) return;
@@ -590,6 +719,8 @@ static fg_status launch_poisson(fg_system* sys) {
   const int64_t n = sp->nfree;
   if (sp->dg) return dg_assemble_rows(sys);
   if (sp->explicit_nodes) return usystem_scatter(sys);
+  sys->direct = false;
+  if (!sys->lean && stencil_direct_ok(sp) && sys->d_tval && sys->d_tval32) return launch_scatter_stencil<P, 1>(sys, g);
   if (n > 0) {
     constexpr int CAP = P == 1 ? 32 : (P == 2 ? 128 : 512);
     k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,
@@ -816,6 +947,8 @@ static fg_status launch_elasticity(fg_system* sys) {
   FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
   if (sp->explicit_nodes) return usystem_scatter(sys);
+  sys->direct = false;
+  if (!sys->lean && stencil_direct_ok(sp) && sys->d_tval && sys->d_tval32) return launch_scatter_stencil<P, 3>(sys, g);
   if (n > 0) {
     constexpr int CAP = P == 1 ? 128 : P == 2 ? 512 : 1056;  // (2P+1)^3 * 3 box entries, rounded up to 32
     constexpr int W = P == 3 ? 2 : 8;                         // warps (rows) per block: static smem <= 48 KB

@@ -152,6 +152,8 @@ struct fg_space {
   uint8_t* d_st_scls = nullptr;   // class of each slice
   int32_t* d_st_row = nullptr;    // 32*st_nslices: solver vector index of each row slot
   int32_t* d_row2st = nullptr;    // free row -> row slot
+  int32_t* d_st_slot2row = nullptr;  // 32*st_nslices: free row of each row slot (-1: padding)
+  int st_max_bp = 0;              // largest Bp of the classes
   std::vector<fg::StencilClass> h_st_cls;
   // unstructured mesh: nodes (nlat of them) are vertices, edge, face and cell interior nodes
   int32_t* d_cellnode = nullptr;  // nn*ncells node ids
@@ -192,6 +194,8 @@ struct fg_system {
   int red_blocks = 0;
   fg_integrand integ;             // last integrand (host copy of scalars)
   bool lean = false;              // FG_LEAN_SYSTEM: element matrices and CSR values released
+  bool direct = false;            // assembled straight into the lattice-implicit layout: the CSR
+                                  // values (d_val) are derived from it only when exported
 };
 
 namespace fg {
@@ -249,6 +253,13 @@ fg_status system_fill_sell(fg_system* sys);
 // fg_stencil.cu
 fg_status space_build_stencil(fg_space* sp);
 fg_status system_fill_stencil(fg_system* sys);
+// true when the row gather can write the lattice-implicit layout directly (3D structured
+// continuous spaces whose widest class fits the kernel's shared-memory slice buffer)
+bool stencil_direct_ok(const fg_space* sp);
+// CSR values (d_val) of a directly assembled system, from its FP64 lattice-implicit values
+fg_status system_ensure_csr(fg_system* sys);
+// inverse diagonal from the FP64 lattice-implicit values (same numbers as from the CSR)
+fg_status system_inv_diag_stencil(fg_system* sys);
 
 // fg_solver.cu
 fg_status system_prepare_diag(fg_system* sys);

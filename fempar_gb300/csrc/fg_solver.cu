@@ -627,6 +627,7 @@ fg_status system_prepare_diag(fg_system* sys) {
     FG_CUDA_TRY(cudaMemsetAsync(sys->d_idiag, 0, sizeof(double) * nv, ctx->stream));
     FG_CUDA_TRY(cudaMemsetAsync(sys->d_idiag32, 0, sizeof(float) * nv, ctx->stream));
   }
+  if (sp->layout == FG_LAYOUT_STENCIL && sys->d_tval) return system_inv_diag_stencil(sys);
   if (n > 0) {
     ctx->launches += 1;
     k_inv_diag<<<nblk(n, 256), 256, 0, ctx->stream>>>(n, sp->d_rowptr, sp->d_col, sys->d_val, sp->d_row2vec,

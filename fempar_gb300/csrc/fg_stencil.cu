@@ -39,7 +39,7 @@ __global__ void k_class_keys(int64_t nslots, int ncomp, int p, int Ln0, int Ln1,
 __global__ void k_stencil_rows(int64_t nfree, int ncomp, int p, const int Ln[3], int halo, const int Pn[3],
                                const uint8_t* skeys, const int32_t* svals, const int64_t* cls_start,
                                const StencilClass* cls, const int32_t* latdof, int32_t* st_row, int32_t* row2st,
-                               int32_t* row2vec) {
+                               int32_t* row2vec, int32_t* slot2row) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nfree) return;
   const int k = skeys[i];
@@ -54,6 +54,7 @@ __global__ void k_stencil_rows(int64_t nfree, int ncomp, int p, const int Ln[3],
   const int64_t slot = (int64_t)cls[k].sbase * 32 + (i - cls_start[k]);
   const int32_t r = latdof[s] - 1;
   st_row[slot] = (int32_t)st;
+  slot2row[slot] = r;
   row2st[r] = (int32_t)slot;
   row2vec[r] = (int32_t)(st + cls[k].ownoff);
 }
@@ -195,6 +196,8 @@ fg_status space_build_stencil(fg_space* sp) {
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_scls, hscls.size()));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_row, sizeof(int32_t) * (nsl > 0 ? nsl * 32 : 1)));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_row2st, sizeof(int32_t) * (sp->nfree > 0 ? sp->nfree : 1)));
+  FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_slot2row, sizeof(int32_t) * (nsl > 0 ? nsl * 32 : 1)));
+  FG_CUDA_TRY(cudaMemsetAsync(sp->d_st_slot2row, 0xff, sizeof(int32_t) * (nsl > 0 ? nsl * 32 : 1), ctx->stream));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_row2vec, sizeof(int32_t) * (sp->nfree > 0 ? sp->nfree : 1)));
   FG_TRY(dev_alloc(ctx, (void**)&d_cstart, sizeof(int64_t) * (ncls + 1)));
   FG_TRY(dev_alloc(ctx, (void**)&d_dims, sizeof(int) * 8));
@@ -207,7 +210,8 @@ fg_status space_build_stencil(fg_space* sp) {
   if (sp->nfree > 0) {
     k_stencil_rows<<<nblk(sp->nfree, 256), 256, 0, ctx->stream>>>(sp->nfree, ncomp, p, d_dims, p, d_dims + 3, skeys,
                                                                    svals, d_cstart, sp->d_st_cls, sp->d_latdof,
-                                                                   sp->d_st_row, sp->d_row2st, sp->d_row2vec);
+                                                                   sp->d_st_row, sp->d_row2st, sp->d_row2vec,
+                                                                   sp->d_st_slot2row);
     FG_CUDA_TRY(cudaGetLastError());
     k_stencil_pad<<<nblk(nsl, 256), 256, 0, ctx->stream>>>(nsl, sp->d_st_scls, sp->d_st_cls, sp->d_st_row);
     FG_CUDA_TRY(cudaGetLastError());
@@ -215,6 +219,8 @@ fg_status space_build_stencil(fg_space* sp) {
   }
   FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   sp->h_st_cls = cls;
+  sp->st_max_bp = 0;
+  for (const StencilClass& C : cls) sp->st_max_bp = std::max(sp->st_max_bp, C.Bp);
   dev_free(ctx, keys);
   dev_free(ctx, skeys);
   dev_free(ctx, vals);
@@ -235,6 +241,84 @@ fg_status system_fill_stencil(fg_system* sys) {
   k_stencil_vals<<<nblk(sp->nfree * 32, 256), 256, 0, ctx->stream>>>(
       sp->nfree, sp->ncomp, sp->order, sp->Ln[0], sp->Ln[1], sp->d_rowptr, sp->d_col, sys->d_val, sp->d_free2lat,
       sp->d_row2st, sp->d_st_scls, sp->d_st_cls, sys->d_tval, sys->d_tval32);
+  FG_CUDA_TRY(cudaGetLastError());
+  ctx->launches += 1;
+  return FG_OK;
+}
+
+// CSR values from the lattice-implicit FP64 values (the inverse of k_stencil_vals)
+__global__ void k_stencil_to_csr(int64_t nfree, int ncomp, int Ln0, int Ln1, const int64_t* rowptr,
+                                 const int32_t* col, const double* sval, const int32_t* free2lat,
+                                 const int32_t* row2st, const uint8_t* scls, const StencilClass* cls, double* val) {
+  const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= nfree) return;
+  const int32_t slot = row2st[r];
+  const int64_t sl = slot >> 5;
+  const int rl = slot & 31;
+  const StencilClass& C = cls[scls[sl]];
+  const int64_t vb = C.vbase + (sl - C.sbase) * 32 * (int64_t)C.Bp + 4 * rl;
+  const int64_t L = free2lat[r] / ncomp;
+  const int I = (int)(L % Ln0), J = (int)((L / Ln0) % Ln1), K = (int)(L / ((int64_t)Ln0 * Ln1));
+  const int lox = I + C.lo[0], loy = J + C.lo[1], loz = K + C.lo[2];
+  const int64_t s = rowptr[r], e = rowptr[r + 1];
+  for (int64_t t = s + lane; t < e; t += 32) {
+    const int32_t sl2 = free2lat[col[t]];
+    const int64_t L2 = sl2 / ncomp;
+    const int c2 = sl2 % ncomp;
+    const int mx = (int)(L2 % Ln0) - lox, my = (int)((L2 / Ln0) % Ln1) - loy,
+              mz = (int)(L2 / ((int64_t)Ln0 * Ln1)) - loz;
+    const int pos = c2 + ncomp * (mx + C.w[0] * (my + C.w[1] * mz));
+    val[t] = sval[vb + (int64_t)(pos >> 2) * 128 + (pos & 3)];
+  }
+}
+
+fg_status system_ensure_csr(fg_system* sys) {
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  if (!sys->direct) return FG_OK;
+  if (!sys->d_tval || !sp->d_rowptr || !sp->d_col) {
+    set_error("the CSR of this system was released (FG_LEAN_SYSTEM / fg_space_release_pattern)");
+    return FG_ERR_UNSUPPORTED;
+  }
+  if (!sys->d_val) FG_TRY(dev_alloc(ctx, (void**)&sys->d_val, sizeof(double) * (sp->nnz > 0 ? sp->nnz : 1)));
+  if (sp->nfree > 0) {
+    k_stencil_to_csr<<<nblk(sp->nfree * 32, 256), 256, 0, ctx->stream>>>(
+        sp->nfree, sp->ncomp, sp->Ln[0], sp->Ln[1], sp->d_rowptr, sp->d_col, sys->d_tval, sp->d_free2lat,
+        sp->d_row2st, sp->d_st_scls, sp->d_st_cls, sys->d_val);
+    FG_CUDA_TRY(cudaGetLastError());
+    ctx->launches += 1;
+  }
+  sys->direct = false;  // d_val now holds the values (until the next direct assembly)
+  return FG_OK;
+}
+
+// 1/diagonal of every free row, read at the diagonal box position of its class (the node
+// itself, component = the row's); entries of non-free vector slots stay 0
+__global__ void k_inv_diag_stencil(int64_t nfree, int ncomp, const int32_t* free2lat, const int32_t* row2st,
+                                   const int32_t* row2vec, const uint8_t* scls, const StencilClass* cls,
+                                   const double* sval, double* d64, float* d32) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nfree) return;
+  const int32_t slot = row2st[r];
+  const int64_t sl = slot >> 5;
+  const int rl = slot & 31;
+  const StencilClass& C = cls[scls[sl]];
+  const int c = free2lat[r] % ncomp;
+  const int pos = c + ncomp * (-C.lo[0] + C.w[0] * (-C.lo[1] + C.w[1] * (-C.lo[2])));
+  const double d = sval[C.vbase + (sl - C.sbase) * 32 * (int64_t)C.Bp + 4 * rl + (int64_t)(pos >> 2) * 128 + (pos & 3)];
+  const double inv = 1.0 / d;
+  d64[row2vec[r]] = inv;
+  d32[row2vec[r]] = (float)inv;
+}
+
+fg_status system_inv_diag_stencil(fg_system* sys) {
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  if (sp->nfree == 0) return FG_OK;
+  k_inv_diag_stencil<<<nblk(sp->nfree, 256), 256, 0, ctx->stream>>>(sp->nfree, sp->ncomp, sp->d_free2lat, sp->d_row2st,
+                                                                    sp->d_row2vec, sp->d_st_scls, sp->d_st_cls,
+                                                                    sys->d_tval, sys->d_idiag, sys->d_idiag32);
   FG_CUDA_TRY(cudaGetLastError());
   ctx->launches += 1;
   return FG_OK;

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <vector>
 #ifdef _OPENMP
@@ -24,6 +25,17 @@
 #endif
 
 namespace {
+
+// std::vector allocator that leaves new elements uninitialised, so the large CSR arrays are
+// first touched by the threads that fill them instead of being zeroed serially.
+template <class T>
+struct NoInit : std::allocator<T> {
+  template <class U> struct rebind { using other = NoInit<U>; };
+  NoInit() = default;
+  template <class U> NoInit(const NoInit<U>&) noexcept {}
+  template <class U, class... A> void construct(U* q, A&&... a) { ::new ((void*)q) U(std::forward<A>(a)...); }
+  template <class U> void construct(U* q) noexcept { ::new ((void*)q) U; }
+};
 
 double now_s() {
   using namespace std::chrono;
@@ -331,8 +343,8 @@ struct orc_problem {
   // COO (upper, free only) and CSR
   int64_t coo_n = 0;
   std::vector<int64_t> irp;                 // nfree+1, 1-based
-  std::vector<int32_t> ja;                  // 1-based
-  std::vector<double> val;
+  std::vector<int32_t, NoInit<int32_t>> ja;  // 1-based
+  std::vector<double, NoInit<double>> val;
   std::vector<double> rhs;
   double t_setup = 0, t_integrate = 0, t_compress = 0;
   std::vector<double> qp_source;            // copy of per-qp source if given
@@ -1051,7 +1063,140 @@ void dg_facets(orc_problem& P, std::vector<int32_t>& cia, std::vector<int32_t>& 
     }
 }
 
+// Multi-threaded form of assemble() for the continuous Galerkin path, used when nthreads > 1.
+// It produces the same CSR, bit for bit, as the serial COO append + sort_and_compress below:
+// the cells are cut into nthreads consecutive chunks; pass A counts each chunk's upper free
+// entries per row, so every (chunk, row) gets its slot range inside the row; pass B
+// integrates the chunk's cells in order and writes each entry into its slot.  Every row then
+// holds its entries in append (cell) order, exactly the order the stable counting sort by
+// row gives; each row is stably sorted by column (insertion sort) and its duplicates summed
+// in that order, as row_compress does.  The rhs is summed in cell order.
+void assemble_parallel(orc_problem& P, int T) {
+  const int nd = P.nd;
+  const int64_t nr = P.nfree, nc = P.ncells;
+  std::vector<double> invj0, det0, xq0;
+  if (P.p.translated_jacobian) cell_geometry(P, 0, invj0, det0, xq0);
+  std::vector<int64_t> cb(T + 1);
+  for (int t = 0; t <= T; ++t) cb[t] = nc * t / T;
+  // slot[t*nr + r]: entries of row r from chunk t (pass A), then the chunk's next slot in the row
+  std::unique_ptr<uint32_t[]> slot(new uint32_t[(size_t)T * (size_t)nr]);
+  std::unique_ptr<uint32_t[]> rowcnt(new uint32_t[(size_t)nr + 1]);
+  std::vector<int64_t> rstart(nr + 1, 0), tsum(T + 1, 0);
+  std::unique_ptr<double[]> evall(new double[(size_t)nc * nd]);
+  std::unique_ptr<int32_t[]> cja;
+  std::unique_ptr<double[]> cval;
+#pragma omp parallel num_threads(T)
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    uint32_t* cnt = slot.get() + (size_t)t * nr;
+    std::fill(cnt, cnt + nr, 0u);
+    for (int64_t c = cb[t]; c < cb[t + 1]; ++c) {
+      const int32_t* gid = &P.gids[(size_t)c * nd];
+      for (int j = 0; j < nd; ++j) {
+        const int32_t jas = gid[j];
+        if (jas < 1) continue;
+        for (int i = 0; i < nd; ++i) {
+          const int32_t ias = gid[i];
+          if (ias < 1 || ias > jas) continue;
+          cnt[ias - 1]++;
+        }
+      }
+    }
+#pragma omp barrier
+    const int64_t r0 = nr * t / T, r1 = nr * (t + 1) / T;
+    int64_t mine = 0;
+    for (int64_t r = r0; r < r1; ++r) {
+      uint32_t acc = 0;
+      for (int u = 0; u < T; ++u) {
+        uint32_t k = slot[(size_t)u * nr + r];
+        slot[(size_t)u * nr + r] = acc;
+        acc += k;
+      }
+      rowcnt[r] = acc;
+      mine += acc;
+    }
+    tsum[t + 1] = mine;
+#pragma omp barrier
+#pragma omp single
+    {
+      for (int u = 0; u < T; ++u) tsum[u + 1] += tsum[u];
+      cja.reset(new int32_t[(size_t)tsum[T]]);
+      cval.reset(new double[(size_t)tsum[T]]);
+    }
+    int64_t run = tsum[t];
+    for (int64_t r = r0; r < r1; ++r) { rstart[r] = run; run += rowcnt[r]; }
+    if (t == T - 1) rstart[nr] = run;
+#pragma omp barrier
+    std::vector<double> em((size_t)nd * nd);
+    for (int64_t c = cb[t]; c < cb[t + 1]; ++c) {
+      double* ev = &evall[(size_t)c * nd];
+      integrate_cell(P, c, P.p.translated_jacobian && c > 0 ? &invj0 : nullptr,
+                     P.p.translated_jacobian && c > 0 ? &det0 : nullptr, em.data(), ev);
+      const int32_t* gid = &P.gids[(size_t)c * nd];
+      for (int j = 0; j < nd; ++j) {
+        const int32_t jas = gid[j];
+        if (jas < 1) continue;
+        for (int i = 0; i < nd; ++i) {
+          const int32_t ias = gid[i];
+          if (ias < 1 || ias > jas) continue;
+          const int64_t pos = rstart[ias - 1] + cnt[ias - 1]++;
+          cja[pos] = jas;
+          cval[pos] = em[i + (size_t)nd * j];
+        }
+      }
+    }
+  }
+  double t0 = now_s();
+  P.coo_n = tsum[T];
+  // rhs (serial_scalar_array_add_multiple_entries) in cell order
+  P.rhs.assign(nr, 0.0);
+  for (int64_t c = 0; c < nc; ++c) {
+    const int32_t* gid = &P.gids[(size_t)c * nd];
+    const double* ev = &evall[(size_t)c * nd];
+    for (int i = 0; i < nd; ++i) if (gid[i] > 0) P.rhs[gid[i] - 1] = P.rhs[gid[i] - 1] + ev[i];
+  }
+  evall.reset();
+  slot.reset();
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(T)
+  for (int64_t r = 0; r < nr; ++r) {
+    const int64_t s = rstart[r], e = rstart[r + 1];
+    int32_t* cj = cja.get();
+    double* cv = cval.get();
+    for (int64_t k = s + 1; k < e; ++k) {  // stable insertion sort by column
+      const int32_t kc = cj[k];
+      const double kv = cv[k];
+      int64_t m = k;
+      while (m > s && cj[m - 1] > kc) { cj[m] = cj[m - 1]; cv[m] = cv[m - 1]; --m; }
+      cj[m] = kc; cv[m] = kv;
+    }
+    int64_t w = s;
+    for (int64_t k = s; k < e; ++k) {
+      if (k > s && cj[w - 1] == cj[k]) cv[w - 1] = cv[w - 1] + cv[k];
+      else { cj[w] = cj[k]; cv[w] = cv[k]; ++w; }
+    }
+    rowcnt[r] = (uint32_t)(w - s);
+  }
+  P.irp.assign(nr + 1, 1);
+  for (int64_t r = 0; r < nr; ++r) P.irp[r + 1] = P.irp[r] + (int64_t)rowcnt[r];
+  P.ja.resize((size_t)(P.irp[nr] - 1));
+  P.val.resize((size_t)(P.irp[nr] - 1));
+#pragma omp parallel for schedule(static) num_threads(T)
+  for (int64_t r = 0; r < nr; ++r) {
+    const int64_t d = P.irp[r] - 1;
+    std::memcpy(&P.ja[d], &cja[rstart[r]], sizeof(int32_t) * rowcnt[r]);
+    std::memcpy(&P.val[d], &cval[rstart[r]], sizeof(double) * rowcnt[r]);
+  }
+  P.t_compress = now_s() - t0;
+}
+
 void assemble(orc_problem& P) {
+  if (P.p.nthreads > 1 && P.p.formulation != ORC_DG && P.nfree > 0) {
+    assemble_parallel(P, P.p.nthreads);
+    return;
+  }
   const int nd = P.nd;
   std::vector<double> invj0, det0, xq0;
   if (P.p.translated_jacobian) cell_geometry(P, 0, invj0, det0, xq0);
@@ -1158,26 +1303,140 @@ void spmv_sym(const orc_problem& P, const double* x, double* y) {
   }
 }
 
-struct FullCSR { std::vector<int64_t> rp; std::vector<int32_t> ci; std::vector<double> v; };
-void expand_full(const orc_problem& P, FullCSR& F) {
-  const int64_t n = P.nfree;
-  std::vector<int64_t> len(n, 0);
-  for (int64_t r = 0; r < n; ++r)
-    for (int64_t k = P.irp[r] - 1; k < P.irp[r + 1] - 1; ++k) {
-      len[r]++;
-      if (P.ja[k] - 1 != r) len[P.ja[k] - 1]++;
+// Multi-threaded symmetric-storage SpMV (the kernel above) for nthreads > 1.  Rows are cut
+// into nthreads ranges of equal stored entries; thread t writes y of its own rows directly
+// and the transposed contributions y(ic) += a x(ir) that land beyond its range into a private
+// spill buffer, added to y afterwards in thread order.  Deterministic for a thread count; it
+// sums in a different order than the serial kernel, so results agree to rounding.
+//
+// Gather form (full = true): the upper layout is first expanded to a full CSR (0-based, each
+// row's columns ascending, expanded on nthreads threads) and every row is a plain dot
+// product: twice the stored bytes, no scattered writes.
+struct SymPar {
+  int T = 1;
+  bool full = false;
+  std::vector<int64_t> rb;                  // row ranges
+  std::vector<std::vector<double>> spill;   // per thread: y(rb[t+1] .. max column)
+  std::vector<int64_t> frp;                 // full CSR
+  std::vector<int32_t, NoInit<int32_t>> fci;
+  std::vector<double, NoInit<double>> fv;
+  void setup_full(const orc_problem& P, int nth) {
+    T = nth;
+    full = true;
+    const int64_t n = P.nfree;
+    std::unique_ptr<uint32_t[]> cnt(new uint32_t[(size_t)n]);
+#pragma omp parallel for schedule(static) num_threads(T)
+    for (int64_t r = 0; r < n; ++r) cnt[r] = (uint32_t)(P.irp[r + 1] - P.irp[r]);
+#pragma omp parallel for schedule(static) num_threads(T)
+    for (int64_t r = 0; r < n; ++r)
+      for (int64_t k = P.irp[r]; k < P.irp[r + 1] - 1; ++k) {  // off-diagonal entries (diagonal first)
+        const int64_t c = P.ja[k] - 1;
+#pragma omp atomic
+        cnt[c]++;
+      }
+    frp.assign(n + 1, 0);
+    for (int64_t r = 0; r < n; ++r) frp[r + 1] = frp[r] + cnt[r];
+    fci.resize((size_t)frp[n]);
+    fv.resize((size_t)frp[n]);
+    // lower part of row c: cursor from the row's start, filled in any order, sorted below
+    std::unique_ptr<int64_t[]> cur(new int64_t[(size_t)n]);
+#pragma omp parallel for schedule(static) num_threads(T)
+    for (int64_t r = 0; r < n; ++r) cur[r] = frp[r];
+#pragma omp parallel for schedule(static) num_threads(T)
+    for (int64_t r = 0; r < n; ++r)
+      for (int64_t k = P.irp[r]; k < P.irp[r + 1] - 1; ++k) {
+        const int64_t c = P.ja[k] - 1;
+        int64_t pos;
+#pragma omp atomic capture
+        pos = cur[c]++;
+        fci[pos] = (int32_t)r;
+        fv[pos] = P.val[k];
+      }
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(T)
+    for (int64_t r = 0; r < n; ++r) {
+      const int64_t s = frp[r], m = cur[r];
+      for (int64_t k = s + 1; k < m; ++k) {
+        const int32_t kc = fci[k];
+        const double kv = fv[k];
+        int64_t q = k;
+        while (q > s && fci[q - 1] > kc) { fci[q] = fci[q - 1]; fv[q] = fv[q - 1]; --q; }
+        fci[q] = kc; fv[q] = kv;
+      }
+      int64_t w = m;
+      for (int64_t k = P.irp[r] - 1; k < P.irp[r + 1] - 1; ++k) { fci[w] = P.ja[k] - 1; fv[w] = P.val[k]; ++w; }
     }
-  F.rp.assign(n + 1, 0);
-  for (int64_t r = 0; r < n; ++r) F.rp[r + 1] = F.rp[r] + len[r];
-  F.ci.resize(F.rp[n]); F.v.resize(F.rp[n]);
-  std::vector<int64_t> pos(F.rp.begin(), F.rp.end() - 1);
-  for (int64_t r = 0; r < n; ++r)
-    for (int64_t k = P.irp[r] - 1; k < P.irp[r + 1] - 1; ++k) {
-      int64_t c = P.ja[k] - 1;
-      F.ci[pos[r]] = (int32_t)c; F.v[pos[r]++] = P.val[k];
-      if (c != r) { F.ci[pos[c]] = (int32_t)r; F.v[pos[c]++] = P.val[k]; }
+  }
+  void apply_full(const double* x, double* y) const {
+    const int64_t n = (int64_t)frp.size() - 1;
+#pragma omp parallel for schedule(static, 4096) num_threads(T)
+    for (int64_t r = 0; r < n; ++r) {
+      double acc = 0.0;
+      for (int64_t k = frp[r]; k < frp[r + 1]; ++k) acc = acc + fv[k] * x[fci[k]];
+      y[r] = acc;
     }
-}
+  }
+  void setup(const orc_problem& P, int nth) {
+    T = nth;
+    const int64_t n = P.nfree, nnz = P.irp[n] - 1;
+    rb.assign(T + 1, n);
+    rb[0] = 0;
+    for (int t = 1; t < T; ++t)
+      rb[t] = std::lower_bound(P.irp.begin(), P.irp.begin() + n, 1 + nnz * t / T) - P.irp.begin();
+    for (int t = 1; t <= T; ++t) rb[t] = std::max(rb[t], rb[t - 1]);
+    spill.assign(T, {});
+#pragma omp parallel for schedule(static, 1) num_threads(T)
+    for (int t = 0; t < T; ++t) {
+      int64_t hi = rb[t + 1] - 1;
+      for (int64_t r = rb[t]; r < rb[t + 1]; ++r)
+        if (P.irp[r + 1] > P.irp[r]) hi = std::max<int64_t>(hi, P.ja[P.irp[r + 1] - 2] - 1);
+      spill[t].assign((size_t)std::max<int64_t>(0, hi - rb[t + 1] + 1), 0.0);
+    }
+  }
+  void apply(const orc_problem& P, const double* x, double* y) {
+    if (full) { apply_full(x, y); return; }
+#pragma omp parallel num_threads(T)
+    {
+      int t = 0;
+#ifdef _OPENMP
+      t = omp_get_thread_num();
+#endif
+      const int64_t a = rb[t], b = rb[t + 1];
+      double* sp = spill[t].data();
+      const int64_t ns = (int64_t)spill[t].size();
+      for (int64_t i = a; i < b; ++i) y[i] = 0.0;
+      for (int64_t k = 0; k < ns; ++k) sp[k] = 0.0;
+      const int32_t* ja = P.ja.data();
+      const double* va = P.val.data();
+      for (int64_t ir = a; ir < b; ++ir) {
+        const int64_t s = P.irp[ir] - 1, e = P.irp[ir + 1] - 1;
+        if (s >= e) continue;
+        // y(ir) in a register: the off-diagonal columns are > ir, so the sequence of sums
+        // into y(ir) is the serial kernel's
+        double acc = y[ir] + x[ja[s] - 1] * va[s];
+        const double xr = x[ir];
+        int64_t iz = s + 1;
+        for (; iz < e && ja[iz] - 1 < b; ++iz) {
+          const int64_t ic = ja[iz] - 1;
+          acc = acc + x[ic] * va[iz];
+          y[ic] = y[ic] + xr * va[iz];
+        }
+        for (; iz < e; ++iz) {
+          const int64_t ic = ja[iz] - 1;
+          acc = acc + x[ic] * va[iz];
+          sp[ic - b] = sp[ic - b] + xr * va[iz];
+        }
+        y[ir] = acc;
+      }
+#pragma omp barrier
+      for (int u = 0; u < T; ++u) {
+        const int64_t bu = rb[u + 1];
+        const double* su = spill[u].data();
+#pragma omp for schedule(static)
+        for (int64_t k = 0; k < (int64_t)spill[u].size(); ++k) y[bu + k] = y[bu + k] + su[k];
+      }
+    }
+  }
+};
 
 }  // namespace
 
@@ -1277,30 +1536,44 @@ void orc_get_timings(const orc_problem* h, double* t3) { t3[0] = h->t_setup; t3[
 void orc_spmv(const orc_problem* h, const double* x, double* y) { spmv_sym(*h, x, y); }
 
 // cg_solve_body (cg.f90:101-238) with init_convergence_data / update_convergence_data...
-// (cg.f90:279-407).  Vector kernels are the reference's BLAS calls restated as loops.
-int orc_cg(const orc_problem* h, int precond, double rtol, double atol, int maxit, int criterion,
-           const double* b, const double* x0, double* x, int* iters, double* history, int nthreads) {
+// (cg.f90:279-407).  Vector kernels are the reference's BLAS calls restated as loops; with
+// nthreads > 1 they run on that many threads (reductions summed in thread order) and the
+// SpMV is SymPar's.  it_time (optional, length maxit) receives the seconds from the call's
+// start (set-up included) to the end of each iteration.
+int orc_cg_timed(const orc_problem* h, int precond, double rtol, double atol, int maxit, int criterion,
+                 const double* b, const double* x0, double* x, int* iters, double* history, int nthreads,
+                 double* it_time) {
+  const double t_start = now_s();
   const int64_t n = h->nfree;
-  std::vector<double> r(n), z(n), p(n), Ap(n), idiag(n, 1.0);
-  const int nth = nthreads > 0 ? nthreads : 1;
-  FullCSR F;
-  if (nth > 1) expand_full(*h, F);
+  const bool gather = nthreads < -1;
+  const int nth = gather ? -nthreads : (nthreads > 0 ? nthreads : 1);
+  std::vector<double, NoInit<double>> r(n), z(n), p(n), Ap(n), idiag(n);
+  SymPar S;
+  if (gather) S.setup_full(*h, nth);
+  else if (nth > 1) S.setup(*h, nth);
   auto A = [&](const double* in, double* out) {
-    if (nth > 1) {
-#pragma omp parallel for schedule(static) num_threads(nth)
-      for (int64_t i = 0; i < n; ++i) {
-        double acc = 0.0;
-        for (int64_t k = F.rp[i]; k < F.rp[i + 1]; ++k) acc += F.v[k] * in[F.ci[k]];
-        out[i] = acc;
-      }
-    } else spmv_sym(*h, in, out);
+    if (nth > 1) S.apply(*h, in, out);
+    else spmv_sym(*h, in, out);
   };
+  std::vector<double> part(nth);
   auto dot = [&](const double* a, const double* c) {
+    if (nth == 1) {
+      double s = 0.0;
+      for (int64_t i = 0; i < n; ++i) s = s + a[i] * c[i];
+      return s;
+    }
+#pragma omp parallel num_threads(nth)
+    {
+      int t = 0;
+#ifdef _OPENMP
+      t = omp_get_thread_num();
+#endif
+      double s = 0.0;
+      for (int64_t i = n * t / nth; i < n * (t + 1) / nth; ++i) s = s + a[i] * c[i];
+      part[t] = s;
+    }
     double s = 0.0;
-    if (nth > 1) {
-#pragma omp parallel for reduction(+ : s) schedule(static) num_threads(nth)
-      for (int64_t i = 0; i < n; ++i) s += a[i] * c[i];
-    } else for (int64_t i = 0; i < n; ++i) s = s + a[i] * c[i];
+    for (int t = 0; t < nth; ++t) s = s + part[t];
     return s;
   };
   auto nrm2 = [&](const double* a) { return std::sqrt(dot(a, a)); };
@@ -1309,22 +1582,25 @@ int orc_cg(const orc_problem* h, int precond, double rtol, double atol, int maxi
 #pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
     for (int64_t i = 0; i < n; ++i) yy[i] = alpha * xx[i] + beta * yy[i];
   };
-  if (precond == 1) {
-    // extract_diagonal (csr_sparse_matrix.f90:4231-4256) + entrywise_invert
-    for (int64_t i = 0; i < n; ++i) {
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+  for (int64_t i = 0; i < n; ++i) {
+    double d = 1.0;
+    if (precond == 1) {
+      // extract_diagonal (csr_sparse_matrix.f90:4231-4256) + entrywise_invert
       int64_t s = h->irp[i] - 1, e = h->irp[i + 1] - 1;
       const int32_t* lo = h->ja.data() + s;
       const int32_t* hi = h->ja.data() + e;
       const int32_t* it = std::lower_bound(lo, hi, (int32_t)(i + 1));
-      double d = (it != hi && *it == (int32_t)(i + 1)) ? h->val[s + (it - lo)] : 0.0;
-      idiag[i] = 1.0 / d;
+      d = (it != hi && *it == (int32_t)(i + 1)) ? h->val[s + (it - lo)] : 0.0;
+      d = 1.0 / d;
     }
+    idiag[i] = d;
+    x[i] = x0 ? x0[i] : 0.0;
   }
   auto M = [&](const double* in, double* out) {
 #pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
     for (int64_t i = 0; i < n; ++i) out[i] = precond == 1 ? idiag[i] * in[i] : in[i];
   };
-  for (int64_t i = 0; i < n; ++i) x[i] = x0 ? x0[i] : 0.0;
   double b_nrm_M = 0.0;
   if (criterion == ORC_RES_NRMGIVEN_RHS_NRMGIVEN) { M(b, r.data()); b_nrm_M = std::sqrt(dot(b, r.data())); }
   A(x, r.data());
@@ -1332,6 +1608,7 @@ int orc_cg(const orc_problem* h, int precond, double rtol, double atol, int maxi
   M(r.data(), z.data());
   double r_z = dot(r.data(), z.data());
   double r_nrm_M = std::sqrt(r_z);
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
   for (int64_t i = 0; i < n; ++i) p[i] = z[i];
   double rhs_test = 0.0;
   switch (criterion) {
@@ -1362,16 +1639,24 @@ int orc_cg(const orc_problem* h, int precond, double rtol, double atol, int maxi
     }
     if (history) history[it - 1] = err;
     conv = err <= rhs_test;
+    if (!conv && it < maxit) {
+      M(r.data(), z.data());
+      double beta = 1.0 / r_z;
+      r_z = dot(r.data(), z.data());
+      beta = beta * r_z;
+      r_nrm_M = std::sqrt(r_z);
+      axpby(1.0, z.data(), beta, p.data());
+    }
+    if (it_time) it_time[it - 1] = now_s() - t_start;
     if (conv || it >= maxit) break;
-    M(r.data(), z.data());
-    double beta = 1.0 / r_z;
-    r_z = dot(r.data(), z.data());
-    beta = beta * r_z;
-    r_nrm_M = std::sqrt(r_z);
-    axpby(1.0, z.data(), beta, p.data());
   }
   if (iters) *iters = it;
   return conv ? 0 : 1;
+}
+
+int orc_cg(const orc_problem* h, int precond, double rtol, double atol, int maxit, int criterion,
+           const double* b, const double* x0, double* x, int* iters, double* history, int nthreads) {
+  return orc_cg_timed(h, precond, rtol, atol, maxit, criterion, b, x0, x, iters, history, nthreads, nullptr);
 }
 
 double orc_energy_error(const orc_problem* h, const double* x) {

@@ -72,7 +72,9 @@ typedef struct {
   const double* qp_source;  /* ORC_FN_QP_VALUES: ncells*nq*ncomp values      */
   int boundary_fn;          /* ORC_FN_* for the Dirichlet data               */
   int translated_jacobian;  /* 1 = reuse cell-1 Jacobian (reference structured-mesh shortcut) */
-  int nthreads;             /* threads for the element loop (1 = reference serial order) */
+  int nthreads;             /* threads for the assembly (1 = the reference's serial COO append and
+                               sort_and_compress; >1 = the same CSR, bit for bit, built by chunks
+                               of cells on that many threads) */
   int formulation;          /* ORC_CG, or ORC_DG: tutorial_01's interior-penalty dG (Poisson, k = 1) */
 } orc_params;
 
@@ -135,6 +137,17 @@ enum { ORC_RES_RES = 0, ORC_RES_RHS = 1, ORC_DELTA_RHS = 2, ORC_DELTA_DELTA = 3,
  * history (optional, length maxit) receives the per-iteration error estimate. */
 int orc_cg(const orc_problem* h, int precond, double rtol, double atol, int maxit, int criterion,
            const double* b, const double* x0, double* x, int* iters, double* history, int nthreads);
+
+/* orc_cg with per-iteration timestamps: it_time (optional, length maxit) receives the seconds
+ * from the call's start (its set-up included) to the end of each iteration.  With
+ * nthreads > 1 the SpMV is the symmetric-storage kernel on nthreads threads (each thread's
+ * rows, transposed contributions past its rows in a private buffer added in thread order)
+ * and reductions are summed in thread order: deterministic for a thread count, equal to the
+ * serial kernel's results to rounding.  nthreads < -1: the same on -nthreads threads with the
+ * matrix first expanded to a full CSR and a row-gather SpMV (twice the bytes, no scatter). */
+int orc_cg_timed(const orc_problem* h, int precond, double rtol, double atol, int maxit, int criterion,
+                 const double* b, const double* x0, double* x, int* iters, double* history, int nthreads,
+                 double* it_time);
 
 /* y = A x with the reference symmetric-storage kernel. */
 void orc_spmv(const orc_problem* h, const double* x, double* y);

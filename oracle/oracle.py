@@ -103,6 +103,8 @@ def lib():
         L.orc_get_timings.argtypes = [vp, vp]
         L.orc_cg.restype = i32
         L.orc_cg.argtypes = [vp, i32, dbl, dbl, i32, i32, vp, vp, vp, C.POINTER(C.c_int), vp, i32]
+        L.orc_cg_timed.restype = i32
+        L.orc_cg_timed.argtypes = [vp, i32, dbl, dbl, i32, i32, vp, vp, vp, C.POINTER(C.c_int), vp, i32, vp]
         L.orc_spmv.argtypes = [vp, vp, vp]
         L.orc_energy_error.restype = dbl
         L.orc_energy_error.argtypes = [vp, vp]
@@ -245,17 +247,23 @@ class Problem:
         return y
 
     def cg(self, b=None, precond=0, rtol=1e-6, atol=0.0, maxit=1000, criterion=RES_RES, x0=None,
-           history=False, nthreads=1):
+           history=False, nthreads=1, times=False):
+        """PCG (cg.f90).  history: per-iteration error estimate; times: seconds from the call's
+        start to the end of each iteration.  nthreads > 1: threaded symmetric-storage SpMV;
+        nthreads < -1: |nthreads| threads on a full-CSR row-gather SpMV."""
         b = self.rhs() if b is None else np.ascontiguousarray(b, dtype=np.float64)
         x = np.zeros(self.nfree)
         it = C.c_int(0)
         hist = np.zeros(maxit) if history else None
+        tim = np.zeros(maxit) if times else None
         x0 = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
-        rc = lib().orc_cg(self.h, precond, rtol, atol, maxit, criterion, _ptr(b), _ptr(x0), _ptr(x),
-                          C.byref(it), _ptr(hist), nthreads)
+        rc = lib().orc_cg_timed(self.h, precond, rtol, atol, maxit, criterion, _ptr(b), _ptr(x0), _ptr(x),
+                                C.byref(it), _ptr(hist), nthreads, _ptr(tim))
         out = {"x": x, "iters": it.value, "converged": rc == 0}
         if history:
             out["history"] = hist[: it.value]
+        if times:
+            out["times"] = tim[: it.value]
         return out
 
     def error_norms(self, x, fn, fn_param=()):

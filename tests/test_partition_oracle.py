@@ -105,7 +105,7 @@ def _rank_main(rank, world, port, n, nparts, order, out):
 @pytest.mark.parametrize("world,n,nparts,order", [(2, (4, 2, 2), (2, 1, 1), 2), (4, (4, 4, 2), (2, 2, 1), 2)])
 def test_neighbours_exchange_between_processes(world, n, nparts, order):
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.spawn(_rank_main, args=(world, port, n, nparts, order, out), nprocs=world, join=True)
     for r in range(world):

@@ -33,7 +33,7 @@ def _rank_main(rank, world, port, out):
 def test_replica_aggregate_two_gloo_ranks():
     world = 2
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.spawn(_rank_main, args=(world, port, out), nprocs=world, join=True)
     for r in range(world):
