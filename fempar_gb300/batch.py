@@ -113,11 +113,13 @@ def lattice_index_map(dof_map, n, p):
     return out
 
 
-def benchmark(ctx, count=4096, nmin=8, nmax=48, threads=0, runs=3, rtol=1e-8, check=16, seed=SEED):
+def benchmark(ctx, count=4096, nmin=8, nmax=48, threads=0, runs=3, rtols=(1e-8,), check=16, seed=SEED):
     """The batched benchmark on `ctx`: `count` problems of the cfg-style distribution, solved
-    `runs` times to `rtol` in one persistent launch each; a sample of `check` problems is also
-    solved by the plain FP64 drop-in (assembled CSR, Jacobi-CG) at `rtol` (timed) and at 1e-13,
-    and the batch solutions are compared with both.  Returns a JSON-ready dict."""
+    `runs` times in one persistent launch each, for every residual tolerance in `rtols`.  A
+    sample of `check` problems is also solved by the plain FP64 drop-in (assembled CSR,
+    Jacobi-CG) at each tolerance (timed) and at 1e-13, and the batch solutions are compared
+    with both.  Returns a JSON-ready dict: the first tolerance's figures at the top level,
+    every tolerance's under "by_rtol"."""
     import torch
 
     from .fe import FEAffineOperator, IterativeLinearSolver, PoissonIntegration, SerialFESpace, SerialTriangulation
@@ -128,34 +130,13 @@ def benchmark(ctx, count=4096, nmin=8, nmax=48, threads=0, runs=3, rtol=1e-8, ch
     for q in probs:
         n, p = q["n"], q["order"]
         q["qp_source"] = torch.randn(n ** 3 * (p + 1) ** 3, dtype=torch.float64, device=dev, generator=g)
-        q["x"] = torch.zeros(max(p * n - 1, 0) ** 3, dtype=torch.float64, device=dev)
-    t0 = time.perf_counter()
-    B = BatchSolver(ctx, probs, rtol=rtol, threads=threads)
-    plan_s = time.perf_counter() - t0
-    times = []
-    for _ in range(runs):
-        res = B.run()
-        times.append(B.info()["run_ms"])
-    info = B.info()
-    dofs = info["total_dofs"]
-    its = np.array([r["iterations"] for r in res])
-    # algorithmic stencil work: iterations x interior nodes x mean stencil width x 2 flops
-    width = {1: 27.0, 2: 64.0, 3: 125.0}
-    flops = sum(2.0 * r["iterations"] * max(q["order"] * q["n"] - 1, 0) ** 3 * width[q["order"]]
-                for q, r in zip(probs, res))
-    out = {"metric": "batched Poisson: DOF/s to rtol (assembly + Jacobi-PCG), one persistent launch",
-           "rtol": rtol, "problems": count, "total_dofs": dofs, "run_ms": min(times), "runs_ms": times,
-           "dof_per_s": dofs / (min(times) * 1e-3), "plan_s": plan_s, "info": info,
-           "iterations": {"mean": float(its.mean()), "max": int(its.max())},
-           "stencil_tflop": flops / 1e12, "stencil_tflops_per_s": flops / (min(times) * 1e-3) / 1e12,
-           "refinements_mean": float(np.mean([r["refinements"] for r in res])),
-           "all_converged": all(r["status"] == 0 for r in res)}
-    # a sample through the general assembled FP64 path (same inputs)
     rng = np.random.Generator(np.random.PCG64(seed + 1))
-    errs, errs_same, errs_fp64, t64, d64 = [], [], [], 0.0, 0
     small = [i for i, q in enumerate(probs) if (q["order"] * q["n"] - 1) ** 3 <= 2000000]
-    for i in rng.choice(small, size=min(check, len(small)), replace=False):
-        q = probs[int(i)]
+    sample = [int(i) for i in rng.choice(small, size=min(check, len(small)), replace=False)]
+    # FP64 reference solutions of the sample (drop-in at 1e-13), kept on the host
+    ref = {}
+    for i in sample:
+        q = probs[i]
         n, p = q["n"], q["order"]
         tri = SerialTriangulation(ctx, (n, n, n))
         sp = SerialFESpace(tri, order=p, dirichlet_ids=list(range(1, 27)))
@@ -163,31 +144,61 @@ def benchmark(ctx, count=4096, nmin=8, nmax=48, threads=0, runs=3, rtol=1e-8, ch
                                                      qp_source=q["qp_source"].cpu().numpy())).compute()
         s = IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
         s.set_parameters_from_pl({"ILS_RTOL": 1e-13, "ILS_MAX_NUM_ITERATIONS": 200000})
-        x64 = s.solve()
-        # the plain FP64 drop-in at the same rtol: assembly + solve, timed
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        op.compute()
-        s8 = IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
-        s8.set_parameters_from_pl({"ILS_RTOL": rtol, "ILS_MAX_NUM_ITERATIONS": 200000})
-        x8 = s8.solve()
-        t64 += time.perf_counter() - t1
-        d64 += sp.num_free_dofs
-        idx = lattice_index_map(sp.get_dof_map(), n, p)
-        xb = q["x"].cpu().numpy()
-        errs.append(float(np.linalg.norm(xb - x64[idx]) / np.linalg.norm(x64)))
-        errs_same.append(float(np.linalg.norm(xb - x8[idx]) / np.linalg.norm(x8)))
-        errs_fp64.append(float(np.linalg.norm(x8 - x64) / np.linalg.norm(x64)))
-        op.close()
-    out["max_err_vs_fp64_rtol1e-13"] = max(errs) if errs else None
-    out["max_err_vs_fp64_same_rtol"] = max(errs_same) if errs_same else None
-    # what the stopping rule itself allows: the FP64 drop-in at rtol vs the same at 1e-13
-    out["max_err_fp64_dropin_vs_rtol1e-13"] = max(errs_fp64) if errs_fp64 else None
-    if d64:
-        out["fp64_dropin_sample"] = {"problems": len(errs), "dofs": d64, "seconds": t64, "dof_per_s": d64 / t64}
-        out["batch_over_fp64_dropin"] = out["dof_per_s"] / (d64 / t64)
-    B.close()
-    return out
+        ref[i] = (s.solve(), lattice_index_map(sp.get_dof_map(), n, p), tri, sp, op)
+    by = {}
+    for rtol in rtols:
+        for q in probs:
+            q["x"] = torch.zeros(max(q["order"] * q["n"] - 1, 0) ** 3, dtype=torch.float64, device=dev)
+        t0 = time.perf_counter()
+        B = BatchSolver(ctx, probs, rtol=rtol, threads=threads)
+        plan_s = time.perf_counter() - t0
+        times = []
+        for _ in range(runs):
+            res = B.run()
+            times.append(B.info()["run_ms"])
+        info = B.info()
+        dofs = info["total_dofs"]
+        its = np.array([r["iterations"] for r in res])
+        # algorithmic stencil work: iterations x interior nodes x mean stencil width x 2 flops
+        width = {1: 27.0, 2: 64.0, 3: 125.0}
+        flops = sum(2.0 * r["iterations"] * max(q["order"] * q["n"] - 1, 0) ** 3 * width[q["order"]]
+                    for q, r in zip(probs, res))
+        rec = {"rtol": rtol, "problems": count, "total_dofs": dofs, "run_ms": min(times), "runs_ms": times,
+               "dof_per_s": dofs / (min(times) * 1e-3), "plan_s": plan_s, "info": info,
+               "iterations": {"mean": float(its.mean()), "max": int(its.max())},
+               "stencil_tflop": flops / 1e12, "stencil_tflops_per_s": flops / (min(times) * 1e-3) / 1e12,
+               "refinements_mean": float(np.mean([r["refinements"] for r in res])),
+               "all_converged": all(r["status"] == 0 for r in res)}
+        errs, errs_same, errs_fp64, t64, d64 = [], [], [], 0.0, 0
+        for i in sample:
+            q = probs[i]
+            x13, idx, tri, sp, op = ref[i]
+            # the plain FP64 drop-in at the same rtol: assembly + solve, timed
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            op.compute()
+            s8 = IterativeLinearSolver().set_type_from_string("CG").set_operators(op, "jacobi")
+            s8.set_parameters_from_pl({"ILS_RTOL": rtol, "ILS_MAX_NUM_ITERATIONS": 200000})
+            x8 = s8.solve()
+            t64 += time.perf_counter() - t1
+            d64 += sp.num_free_dofs
+            xb = q["x"].cpu().numpy()
+            errs.append(float(np.linalg.norm(xb - x13[idx]) / np.linalg.norm(x13)))
+            errs_same.append(float(np.linalg.norm(xb - x8[idx]) / np.linalg.norm(x8)))
+            errs_fp64.append(float(np.linalg.norm(x8 - x13) / np.linalg.norm(x13)))
+        rec["max_err_vs_fp64_rtol1e-13"] = max(errs) if errs else None
+        rec["max_err_vs_fp64_same_rtol"] = max(errs_same) if errs_same else None
+        # what the stopping rule itself allows: the FP64 drop-in at rtol vs the same at 1e-13
+        rec["max_err_fp64_dropin_vs_rtol1e-13"] = max(errs_fp64) if errs_fp64 else None
+        if d64:
+            rec["fp64_dropin_sample"] = {"problems": len(errs), "dofs": d64, "seconds": t64, "dof_per_s": d64 / t64}
+            rec["batch_over_fp64_dropin"] = rec["dof_per_s"] / (d64 / t64)
+        by[str(rtol)] = rec
+        B.close()
+    for i in sample:
+        ref[i][4].close()
+    return {"metric": "batched Poisson: DOF/s to rtol (assembly + Jacobi-PCG), one persistent launch",
+            **by[str(rtols[0])], "by_rtol": by}
 
 
 def main():
@@ -197,7 +208,7 @@ def main():
     ap.add_argument("--nmax", type=int, default=48)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--runs", type=int, default=3)
-    ap.add_argument("--rtol", type=float, default=1e-8)
+    ap.add_argument("--rtol", type=float, nargs="+", default=[1e-8])
     ap.add_argument("--check", type=int, default=16, help="problems checked against FP64 assembled solves")
     args = ap.parse_args()
     from . import build
@@ -205,7 +216,7 @@ def main():
     build.build()
     ctx = Context(0)
     out = benchmark(ctx, count=args.count, nmin=args.nmin, nmax=args.nmax, threads=args.threads, runs=args.runs,
-                    rtol=args.rtol, check=args.check)
+                    rtols=tuple(args.rtol), check=args.check)
     print(json.dumps(out), flush=True)
 
 
