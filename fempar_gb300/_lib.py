@@ -32,7 +32,7 @@ EXPORTS = [
     "fg_mesh_create_structured", "fg_mesh_destroy", "fg_mesh_create_unstructured", "fg_mesh_read_gid",
     "fg_mesh_get_info", "fg_mesh_get_vefs",
     "fg_space_create", "fg_space_create_dg", "fg_space_destroy", "fg_space_release_pattern", "fg_space_get_info", "fg_space_get_dof_map",
-    "fg_space_get_dirichlet_coords",
+    "fg_space_get_dirichlet_coords", "fg_space_get_qp_coords",
     "fg_assemble", "fg_system_reassemble", "fg_system_destroy",
     "fg_system_export_csr", "fg_system_export_rhs", "fg_system_export_dirichlet_values",
     "fg_system_spmv_device", "fg_system_spmv_device_noalloc", "fg_system_spmv_solver_layout_device",
@@ -269,6 +269,7 @@ def lib():
         "fg_space_get_info": (i32, [vp, C.POINTER(SpaceInfo)]),
         "fg_space_get_dof_map": (i32, [vp, vp]),
         "fg_space_get_dirichlet_coords": (i32, [vp, vp]),
+        "fg_space_get_qp_coords": (i32, [vp, vp, i32]),
         "fg_assemble": (i32, [vp, C.POINTER(Integrand), pp]),
         "fg_system_reassemble": (i32, [vp, C.POINTER(Integrand)]),
         "fg_system_destroy": (i32, [vp]),

@@ -546,6 +546,29 @@ fg_status fg_space_get_dirichlet_coords(fg_space* sp, double* xyz) {
   return s;
 }
 
+fg_status fg_space_get_qp_coords(fg_space* sp, double* xyz, int on_device) {
+  FG_CHECK_ARG(sp && xyz, "space/out");
+  fg_ctx* ctx = sp->mesh->ctx;
+  FG_DEVICE_GUARD(ctx);
+  const int64_t n = sp->mesh->ncells * sp->tab.nq * 3;
+  if (n == 0) return FG_OK;
+  if (on_device) {
+    FG_TRY(space_qp_coords(sp, xyz));
+    FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return FG_OK;
+  }
+  double* d = nullptr;
+  FG_TRY(dev_alloc(ctx, (void**)&d, sizeof(double) * n));
+  fg_status s = space_qp_coords(sp, d);
+  if (s == FG_OK) {
+    cudaError_t e = cudaMemcpyAsync(xyz, d, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { set_error("%s", cudaGetErrorString(e)); s = FG_ERR_CUDA; }
+  }
+  dev_free(ctx, d);
+  return s;
+}
+
 static void system_free(fg_system* sys) {
   fg_ctx* ctx = sys->space->mesh->ctx;
   void* ptrs[] = {sys->d_val, sys->d_val32, sys->d_rhs, sys->d_gvals, sys->d_elmat, sys->d_elvec, sys->d_coef,

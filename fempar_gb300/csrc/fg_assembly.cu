@@ -662,6 +662,49 @@ static fg_status launch_scatter_stencil(fg_system* sys, const AsmGeom& g) {
   return FG_OK;
 }
 
+// Physical coordinates of every cell's quadrature points: x_q = sum_k N_k(xi_q) x_k with the
+// trilinear geometry, in the integration kernels' summation order (cell_map quadrature-point
+// coordinates, sbm_cell_map.i90:673-686).  Thread per (cell, point); xyz[(c*nq + q)*3 + l].
+__global__ void k_qp_coords(AsmGeom g, int64_t ncells, int nq, const double* __restrict__ coords,
+                            const double* __restrict__ gshp, double* __restrict__ xyz) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= ncells * nq) return;
+  const int64_t c = t / nq;
+  const int q = (int)(t % nq);
+  int ci = 0, cj = 0, ck = 0;
+  if (!g.cellvert) {
+    ci = (int)(c % g.n[0]);
+    cj = (int)((c / g.n[0]) % g.n[1]);
+    ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
+  }
+  double x0 = 0.0, x1 = 0.0, x2 = 0.0;
+  for (int k = 0; k < 8; ++k) {
+    const int64_t v = asm_vertex(g, c, ci, cj, ck, k);
+    const double a = gshp[k * nq + q];
+    x0 = x0 + a * coords[v * 3 + 0];
+    x1 = x1 + a * coords[v * 3 + 1];
+    x2 = x2 + a * coords[v * 3 + 2];
+  }
+  xyz[t * 3 + 0] = x0;
+  xyz[t * 3 + 1] = x1;
+  xyz[t * 3 + 2] = x2;
+}
+
+fg_status space_qp_coords(fg_space* sp, double* d_xyz) {
+  if (sp->mesh->dim != 3) {
+    set_error("quadrature-point coordinates are exported for 3D hexahedral meshes");
+    return FG_ERR_UNSUPPORTED;
+  }
+  const int64_t total = sp->mesh->ncells * sp->tab.nq;
+  if (total == 0) return FG_OK;
+  AsmGeom g = make_geom(sp);
+  k_qp_coords<<<(unsigned)((total + 255) / 256), 256, 0, sp->mesh->ctx->stream>>>(
+      g, sp->mesh->ncells, sp->tab.nq, sp->mesh->d_coords, sp->dtab.gshp, d_xyz);
+  FG_CUDA_TRY(cudaGetLastError());
+  sp->mesh->ctx->launches += 1;
+  return FG_OK;
+}
+
 __global__ void k_dirichlet_values(int64_t ndir, const double* xyz, int fn, SourceSpec prm, double* gv) {
   int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (d >= ndir) return;

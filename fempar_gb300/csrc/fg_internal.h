@@ -220,6 +220,7 @@ fg_status space_export_upper(fg_space* sp, const double* d_val, int one_based, i
 // fg_assembly.cu
 fg_status system_interpolate_dirichlet(fg_system* sys, int boundary_fn, const double* prm);
 fg_status system_assemble(fg_system* sys);
+fg_status space_qp_coords(fg_space* sp, double* d_xyz);
 
 fg_status scan_i64(fg_ctx* ctx, int64_t* a, int64_t n, int64_t* total);
 fg_status space_count_upper(fg_space* sp);

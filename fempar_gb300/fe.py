@@ -212,6 +212,18 @@ class SerialFESpace:
         L.check(L.lib().fg_space_get_dirichlet_coords(self.h, _ptr(out)), "fg_space_get_dirichlet_coords")
         return out.reshape(-1, 3)
 
+    def get_qp_coords(self, out=None):
+        """Physical quadrature-point coordinates, (num_cells, qp_per_cell, 3): where a
+        user-defined source is evaluated before passing it as FG_FN_QP_VALUES.  out: an
+        optional torch CUDA float64 tensor of that many entries (filled on the device)."""
+        info = self.info
+        if out is not None:
+            L.check(L.lib().fg_space_get_qp_coords(self.h, _ptr(out), 1), "fg_space_get_qp_coords")
+            return out
+        xyz = np.zeros((info.num_cells, info.qp_per_cell, 3))
+        L.check(L.lib().fg_space_get_qp_coords(self.h, _ptr(xyz), 0), "fg_space_get_qp_coords")
+        return xyz
+
     def close(self):
         if getattr(self, "h", None):
             L.lib().fg_space_destroy(self.h)

@@ -144,6 +144,10 @@ module fempar_gpu_names
       import; integer(c_int32_t) :: fg_partition_comm_device
       type(c_ptr), value :: partition, x
     end function
+    function fg_space_get_qp_coords(space, xyz, on_device) bind(c, name="fg_space_get_qp_coords")
+      import; integer(c_int32_t) :: fg_space_get_qp_coords
+      type(c_ptr), value :: space; real(c_double) :: xyz(3, *); integer(c_int), value :: on_device
+    end function
     function fg_system_spmv_device_noalloc(sys, precision, x, y) bind(c, name="fg_system_spmv_device_noalloc")
       import; integer(c_int32_t) :: fg_system_spmv_device_noalloc
       type(c_ptr), value :: sys, x, y; integer(c_int), value :: precision

@@ -217,6 +217,14 @@ fg_status fg_space_get_dof_map(fg_space* space, int32_t* lst_dofs_gids);
  * that interpolate their own boundary function (interpolate_dirichlet_values,
  * sbm_serial_fe_space.i90:997-1176). */
 fg_status fg_space_get_dirichlet_coords(fg_space* space, double* xyz);
+/* Physical coordinates of every cell's quadrature points, xyz[(cell*qp_per_cell + q)*3 + l]
+ * (x fastest over the tensor Gauss rule), for callers that evaluate their own source function
+ * at the quadrature points -- what a discrete_integration_t's integrate_galerkin does through
+ * fe_cell_iterator%get_quadrature_points_coordinates (cell_map quadrature points,
+ * sbm_cell_map.i90:673-686; tutorial_01 modules :107,124) -- and pass the values as
+ * FG_FN_QP_VALUES.  on_device: xyz is a device pointer (num_cells*qp_per_cell*3 doubles).
+ * 3D hexahedral meshes. */
+fg_status fg_space_get_qp_coords(fg_space* space, double* xyz, int on_device);
 
 /* Numeric assembly: integrate every cell, impose strong Dirichlet lifting and assemble the
  * global CSR matrix (+ FP32 copy) and right-hand side on the device, deterministically.

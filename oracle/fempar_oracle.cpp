@@ -1531,6 +1531,13 @@ void orc_get_elmat(const orc_problem* h, int64_t cell, double* elmat, double* el
   integrate_cell(*h, cell, h->p.translated_jacobian && cell > 0 ? &invj0 : nullptr,
                  h->p.translated_jacobian && cell > 0 ? &det0 : nullptr, elmat, elvec);
 }
+void orc_get_qp_coords(const orc_problem* h, double* out) {
+  std::vector<double> invj, det, xq;
+  for (int64_t c = 0; c < h->ncells; ++c) {
+    cell_geometry(*h, c, invj, det, xq);
+    std::memcpy(out + (size_t)c * h->nq * 3, xq.data(), sizeof(double) * h->nq * 3);
+  }
+}
 void orc_get_timings(const orc_problem* h, double* t3) { t3[0] = h->t_setup; t3[1] = h->t_integrate; t3[2] = h->t_compress; }
 
 void orc_spmv(const orc_problem* h, const double* x, double* y) { spmv_sym(*h, x, y); }

@@ -125,6 +125,9 @@ void orc_get_rhs(const orc_problem* h, double* rhs);                     /* nfre
 void orc_get_dirichlet_values(const orc_problem* h, double* g);          /* ndir  */
 void orc_get_elmat(const orc_problem* h, int64_t cell, double* elmat, double* elvec); /* before lifting of elvec? no: after */
 
+/* Physical quadrature-point coordinates of every cell (sbm_cell_map.i90:673-686): ncells*nq*3. */
+void orc_get_qp_coords(const orc_problem* h, double* xyz);
+
 /* Stage timings of orc_create (seconds): mesh+numbering, integration+COO, sort_and_compress. */
 void orc_get_timings(const orc_problem* h, double* t3);
 

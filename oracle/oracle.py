@@ -101,6 +101,7 @@ def lib():
         L.orc_get_dirichlet_values.argtypes = [vp, vp]
         L.orc_get_elmat.argtypes = [vp, i64, vp, vp]
         L.orc_get_timings.argtypes = [vp, vp]
+        L.orc_get_qp_coords.argtypes = [vp, vp]
         L.orc_cg.restype = i32
         L.orc_cg.argtypes = [vp, i32, dbl, dbl, i32, i32, vp, vp, vp, C.POINTER(C.c_int), vp, i32]
         L.orc_cg_timed.restype = i32
@@ -234,6 +235,11 @@ class Problem:
         ev = np.zeros(self.nd)
         lib().orc_get_elmat(self.h, int(cell), _ptr(em), _ptr(ev))
         return em.T.copy(), ev  # stored column-major
+
+    def qp_coords(self):
+        out = np.zeros((self.ncells, self.nq, 3))
+        lib().orc_get_qp_coords(self.h, _ptr(out))
+        return out
 
     def timings(self):
         t = np.zeros(3)

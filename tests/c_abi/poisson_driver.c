@@ -1,8 +1,9 @@
 /* A C driver of the C-ABI: the steps of tutorial_01's serial Poisson driver (mesh, FE space
  * with strong Dirichlet conditions, affine operator, CG with Jacobi) through
  * include/fempar_gpu.h only.  It is what a Fortran shim calls through ISO_C_BINDING.
- * Usage: poisson_driver [n] [order]; prints one line with the dof count, the CG
- * iterations, the final residual estimate and the first upper-CSR row length. */
+ * Usage: poisson_driver [n] [order] [rtol] [solution_file]; prints one line with the dof
+ * count, the CG iterations, the final residual estimate and the first upper-CSR row length,
+ * and writes the solution (num_free doubles, native byte order) when a file is given. */
 #include <stdio.h>
 #include <stdlib.h>
 
@@ -19,6 +20,8 @@
 
 int main(int argc, char** argv) {
   const int n = argc > 1 ? atoi(argv[1]) : 8, order = argc > 2 ? atoi(argv[2]) : 2;
+  const double rtol = argc > 3 ? atof(argv[3]) : 1e-8;
+  const char* out_path = argc > 4 ? argv[4] : NULL;
   fg_ctx* ctx = NULL;
   fg_mesh* mesh = NULL;
   fg_space* space = NULL;
@@ -43,7 +46,8 @@ int main(int argc, char** argv) {
   fg_solver_params prm;
   fg_solver_params_default(&prm);
   prm.precond = FG_PREC_JACOBI;
-  prm.rtol = 1e-8;
+  prm.rtol = rtol;
+  prm.max_iters = 100000;
   double* x = (double*)calloc((size_t)info.num_free, sizeof(double));
   fg_solve_info sinfo;
   CHECK(fg_solve(sys, &prm, NULL, NULL, x, &sinfo));
@@ -54,6 +58,14 @@ int main(int argc, char** argv) {
   printf("dofs %lld iterations %d converged %d residual %.3e first_row %lld\n", (long long)info.num_free,
          sinfo.iterations, sinfo.converged, sinfo.error_estimate,
          (long long)(info.num_free > 0 ? irp[1] - irp[0] : 0));
+  if (out_path) {
+    FILE* f = fopen(out_path, "wb");
+    if (!f || fwrite(x, sizeof(double), (size_t)info.num_free, f) != (size_t)info.num_free) {
+      fprintf(stderr, "cannot write %s\n", out_path);
+      return 1;
+    }
+    fclose(f);
+  }
   free(x);
   free(irp);
   free(ja);

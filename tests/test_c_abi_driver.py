@@ -1,6 +1,6 @@
 """The C-ABI is usable from plain C: tests/c_abi/poisson_driver.c (tutorial_01's serial
 steps through include/fempar_gpu.h only) compiles with gcc -std=c11 -Wall -Werror and links
-against libfempar_gpu.so.  Running it needs a GPU; here it is built only."""
+against libfempar_gpu.so.  Running it needs a GPU: tests/test_gpu_c_driver.py runs it there."""
 import os
 import shutil
 import subprocess

@@ -68,6 +68,30 @@ def test_served_solution_matches_oracle(S):
     assert np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"]) <= 1e-9
 
 
+def test_every_request_of_the_mix_matches_oracle(S):
+    """Per-request error against the oracle: the Poisson and elasticity requests of the mix
+    (Q1/Q2, lognormal coefficients, mixed precision to 1e-10), served concurrently, each within
+    1e-8 of the oracle's FP64 solution of the same request (rtol 1e-13)."""
+    reqs = _mix()
+    srv = S.Server(nworkers=4)
+    tickets = [srv.submit(**rq) for rq in reqs]
+    sols = []
+    for t in tickets:
+        r = srv.wait(t)
+        assert r["status"] == 0
+        sols.append(srv.take(t, r["num_free"]))
+    srv.close()
+    for rq, x in zip(reqs, sols):
+        if rq["kind"] == S.ELASTICITY:
+            P = O.Problem(rq["n"], order=rq["order"], kind=O.ELASTICITY, dirichlet_ids=S.CLAMP_X0_IDS,
+                          cell_coef=rq["cell_coef"], nu=0.3, source_fn=O.FN_CONST, fn_param=[0.0, 0.0, -1.0])
+        else:
+            P = O.Problem(rq["n"], order=rq["order"], cell_coef=rq["cell_coef"], source_fn=O.FN_CONST, fn_param=[1.0])
+        ref = P.cg(precond=1, rtol=1e-13, maxit=100000)
+        err = np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"])
+        assert err <= 1e-8, (rq["kind"], rq["n"], rq["order"], err)
+
+
 def test_budget_refuses_oversized_request(S):
     from fempar_gb300 import FGError
     srv = S.Server(hbm_budget_bytes=64 << 20, nworkers=1)
