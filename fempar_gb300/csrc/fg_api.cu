@@ -572,7 +572,8 @@ fg_status fg_space_get_qp_coords(fg_space* sp, double* xyz, int on_device) {
 static void system_free(fg_system* sys) {
   fg_ctx* ctx = sys->space->mesh->ctx;
   void* ptrs[] = {sys->d_val, sys->d_val32, sys->d_rhs, sys->d_gvals, sys->d_elmat, sys->d_elvec, sys->d_coef,
-                  sys->d_qpsrc, sys->d_sval, sys->d_sval32, sys->d_tval, sys->d_tval32, sys->d_idiag, sys->d_idiag32, sys->d_work, sys->d_work32, sys->d_red, sys->d_ticket};
+                  sys->d_qpsrc, sys->d_sval, sys->d_sval32, sys->d_tval, sys->d_tval32, sys->d_idiag, sys->d_idiag32, sys->d_work, sys->d_work32, sys->d_red, sys->d_ticket,
+                  sys->d_val32s, sys->d_sdiag};
   for (void* p : ptrs) dev_free(ctx, p);
   delete sys;
 }
@@ -608,6 +609,7 @@ static fg_status numeric_phase(fg_system* sys, const fg_integrand* g) {
     FG_TRY(system_interpolate_dirichlet(sys, g->boundary_fn, g->fn_param));
   }
   FG_TRY(system_assemble(sys));
+  sys->scaled_valid = false;
   if (sys->lean) {
     // element matrices are scratch of the scatter: release them before the solver layout
     dev_free(ctx, sys->d_elmat);

@@ -455,8 +455,10 @@ __global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
       }
     EV[c * ND + a] = ev;
   }
+  // Dirichlet columns are spent on the lifting above: stored as zeros, so the row gathers add
+  // nothing there without looking the columns up
   double* Ec = E + (size_t)c * ND * ND;
-  for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = el[idx];
+  for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = gid[idx % ND] < 0 ? 0.0 : el[idx];
 }
 
 // warp per free row; CAP = power-of-two box capacity
@@ -539,7 +541,9 @@ __global__ void __launch_bounds__(W * 32)
 // most 8 cells, visited in increasing cell index, and every position sums its contributions
 // in that order -- the reference's duplicate-summation order, so the values equal
 // k_scatter_rows' CSR values bit for bit.  A lane loads its column of every cell first
-// (latdof + element-matrix entry), then the sums run cell by cell.  The slice's 32 x Bp
+// (streaming loads: each element-matrix entry is read once), then the sums run cell by cell.
+// Dirichlet columns of the element matrices are stored as zeros by the integration kernels,
+// so they add exact zeros to positions that stay zero.  The slice's 32 x Bp
 // block is then written out with consecutive threads on consecutive addresses, FP64 and
 // FP32, padding included: no clearing pass and no CSR in between.
 template <int P, int NC, int W>
@@ -601,11 +605,9 @@ __global__ void __launch_bounds__(W * 32)
             const int bnode = b % NN, bcomp = b / NN;
             const int bi = bnode % NP1, bj = (bnode / NP1) % NP1, bk = bnode / (NP1 * NP1);
             const int Mi = P * ci + bi, Mj = P * cj + bj, Mk = P * ck + bk;
-            const int64_t M = (int64_t)Mi + (int64_t)g.Ln[0] * (Mj + (int64_t)g.Ln[1] * Mk);
-            if (latdof[M * ncomp + bcomp] > 0) {
-              pos[q][h] = bcomp + ncomp * ((Mi - I - C.lo[0]) + C.w[0] * ((Mj - J - C.lo[1]) + C.w[1] * (Mk - K - C.lo[2])));
-              v[q][h] = Erow[b];
-            }
+            // Dirichlet columns hold zeros (the integration stores them so): no lookup needed
+            pos[q][h] = bcomp + ncomp * ((Mi - I - C.lo[0]) + C.w[0] * ((Mj - J - C.lo[1]) + C.w[1] * (Mk - K - C.lo[2])));
+            v[q][h] = __ldcs(Erow + b);
           }
         }
         if (lane == 0) ev[q] = EV[c * ND + a];
@@ -965,8 +967,14 @@ __global__ void __launch_bounds__(ElastShape<P>::WARPS * 32)
       }
     EV[c * ND + i] = ev;
   }
-  if (!S::EL_GLOBAL)
-    for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = el[idx];
+  // Dirichlet columns are spent on the lifting above: stored as zeros (see k_integrate_poisson)
+  if (!S::EL_GLOBAL) {
+    for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = gid[idx % ND] < 0 ? 0.0 : el[idx];
+  } else if (any_dir) {
+    __syncwarp();
+    for (int idx = lane; idx < ND * ND; idx += 32)
+      if (gid[idx % ND] < 0) Ec[idx] = 0.0;
+  }
 }
 
 template <int P>

@@ -186,6 +186,10 @@ struct fg_system {
   float* d_tval32 = nullptr;      // st_nvals FP32 values (lattice-implicit SELL layout)
   double* d_idiag = nullptr;      // nfree inverse diagonal (FP64, slot order)
   float* d_idiag32 = nullptr;     // nfree inverse diagonal (FP32, slot order)
+  // mixed solves with Jacobi: FP32 copy of D^-1/2 A D^-1/2 in the solver layout and D^-1/2
+  float* d_val32s = nullptr;      // st_nvals (lattice-implicit) or sell_nnz (SELL) values
+  double* d_sdiag = nullptr;      // nvec
+  bool scaled_valid = false;      // d_val32s matches the current values
   // solver work vectors (allocated on first solve)
   double* d_work = nullptr;       // FP64 work area
   float* d_work32 = nullptr;      // FP32 work area

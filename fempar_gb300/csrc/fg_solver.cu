@@ -11,14 +11,16 @@
 // the device; kernels of iterations after the stop return at once, so the host polls
 // only every few iterations, replaying a CUDA graph of a fixed chunk of iterations.
 //
-// Mixed path: CG on the FP32 copy of the matrix with FP32 vectors and FP32 Jacobi, with
-// "reliable updates" in FP64: whenever the recursive FP32 residual has dropped by a factor
-// delta (default 0.1) since the last update, or its estimate reaches the tolerance, the
+// Mixed path: CG on an FP32 copy of the matrix with FP32 vectors, with "reliable updates"
+// in FP64: whenever the recursive FP32 residual has dropped by a factor delta (default 0.1)
+// since the last update, or the estimate of the true residual reaches the tolerance, the
 // FP32 correction is folded into the FP64 solution, the true residual r = b - A x is
-// recomputed with the FP64 matrix, the FP32 residual is replaced by it (rescaled to unit
-// norm) and the search direction is kept (rescaled).  The solve stops on the FP64 true
-// residual.  Keeping the direction keeps the iteration count close to the FP64 CG's, where
-// restarting an inner solve per refinement step would lose the Krylov space each time.
+// recomputed with the FP64 matrix, the FP32 residual is replaced by it (rescaled) and the
+// search direction is kept (rescaled).  The solve stops on the FP64 true residual.  Keeping
+// the direction keeps the iteration count close to the FP64 CG's, where restarting an inner
+// solve per refinement step would lose the Krylov space each time.  With Jacobi the FP32
+// segments run CG on D^-1/2 A D^-1/2 (the same iterates in exact arithmetic, no diagonal
+// read per iteration) in two kernels per iteration (see k_update32s).
 //
 // Inner products.  GB300 runs FP64 FMA and FP32<->FP64 conversion at about 0.5 Tera-op/s,
 // some 70x below FP32.  FP64-path dots accumulate in FP64.  FP32-path dots form each
@@ -38,8 +40,10 @@ namespace fg {
 static constexpr int RB = 256;  // threads per block of the vector / SpMV kernels
 
 enum { S_RZ = 0, S_ALPHA, S_BETA, S_ERR, S_TOL, S_APP, S_RNRMM, S_BNRM, S_R0NRM, S_SIGMA, S_RMAX, S_DELTA, S_RNSCALED,
-       S_COUNT = 16 };
-enum { I_ITER = 0, I_DONE, I_CONV, I_MAXIT, I_FLAG, I_COUNT = 8 };
+       S_RRH, S_COUNT = 16 };
+// I_PEND: a segment end decided by the last x/r/p update, taken at the next iteration;
+// I_SKIPP: this iteration's update keeps p (the segment ends after it)
+enum { I_ITER = 0, I_DONE, I_CONV, I_MAXIT, I_FLAG, I_PEND, I_SKIPP, I_COUNT = 8 };
 // FLAG_BREAK: the FP32 recurrence broke down (non-finite or non-positive r_z, residual grown
 // 1e4-fold): the segment's correction is dropped and the solve finishes in FP64
 enum { FLAG_NONE = 0, FLAG_UPDATE = 1, FLAG_CHECK = 2, FLAG_MAXIT = 3, FLAG_BREAK = 4 };
@@ -139,6 +143,221 @@ __device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
 }
 
 // ---------------------------------------------------------------------------
+// Mixed path, FP32 segments on the scaled system A^ = S A S, S = D^-1/2 (D = diag A): Jacobi
+// PCG on A is CG on A^ with x = S x^ and r = S^-1 r^, so no diagonal is streamed per
+// iteration.  Two kernels per iteration:
+//   SpMV (MODE 3): q = A^ p, <p,q>, <q,q>; then alpha = |r|^2/<p,q> and, by the recurrence
+//     |r - alpha q|^2 = alpha^2 |q|^2 - |r|^2 (as <r,q> = <p,q> in CG), beta = |r_new|^2/|r|^2;
+//   update: x += alpha p; r -= alpha q; p = r + beta p; the exact |r_new|^2 for the next alpha,
+//     and on every fourth iteration sum r^2 D (the unscaled residual, for the stop estimate).
+// A segment end (reliable update, stop check, breakdown, iteration limit) found by an update
+// is taken one iteration later: that iteration's update keeps p, so the host can fold x and
+// restart the recursion from the true residual with the direction kept.
+__device__ __forceinline__ void mixed_alpha_beta(double pap, double qq, double* S, int* I) {
+  const double rr = S[S_RRH];
+  int skip = I[I_PEND] != FLAG_NONE;
+  double a = 0.0, b = 0.0;
+  if (!(pap > 0.0 && pap <= 1e300) || !(qq <= 1e300)) {
+    I[I_PEND] = FLAG_BREAK;  // alpha = 0: the update leaves x and r as they are
+    skip = 1;
+  } else {
+    a = rr / pap;
+    const double rrn = a * a * qq - rr;
+    b = rrn / rr;
+    if (!(rrn > 0.0)) {  // the recurrence lost its digits: end the segment here
+      skip = 1;
+      if (I[I_PEND] == FLAG_NONE) I[I_PEND] = FLAG_UPDATE;
+    }
+  }
+  S[S_ALPHA] = a;
+  S[S_BETA] = b;
+  I[I_SKIPP] = skip;
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(RB)
+    k_update32s(int64_t n, float* __restrict__ x, float* __restrict__ r, float* __restrict__ p,
+                const float* __restrict__ q, const float* __restrict__ idiag, RedBuf rb, double* S, int* I) {
+  if (I[I_DONE]) return;
+  const float a = (float)S[S_ALPHA], b = (float)S[S_BETA];
+  const bool keep_p = I[I_SKIPP] != 0;
+  Acc<float> rr, rt;
+  const int64_t t0 = blockIdx.x * (int64_t)RB + threadIdx.x, stride = (int64_t)gridDim.x * RB;
+  const int64_t n4 = n >> 2;
+  {
+    float4* x4 = reinterpret_cast<float4*>(x);
+    float4* r4 = reinterpret_cast<float4*>(r);
+    float4* p4 = reinterpret_cast<float4*>(p);
+    const float4* q4 = reinterpret_cast<const float4*>(q);
+    const float4* d4 = reinterpret_cast<const float4*>(idiag);
+    for (int64_t i = t0; i < n4; i += stride) {
+      float4 xi = x4[i], ri = r4[i], pi = p4[i];
+      const float4 qi = q4[i];
+      xi.x = fmaf(a, pi.x, xi.x);
+      xi.y = fmaf(a, pi.y, xi.y);
+      xi.z = fmaf(a, pi.z, xi.z);
+      xi.w = fmaf(a, pi.w, xi.w);
+      ri.x = fmaf(-a, qi.x, ri.x);
+      ri.y = fmaf(-a, qi.y, ri.y);
+      ri.z = fmaf(-a, qi.z, ri.z);
+      ri.w = fmaf(-a, qi.w, ri.w);
+      x4[i] = xi;
+      r4[i] = ri;
+      if (!keep_p) {
+        pi.x = fmaf(b, pi.x, ri.x);
+        pi.y = fmaf(b, pi.y, ri.y);
+        pi.z = fmaf(b, pi.z, ri.z);
+        pi.w = fmaf(b, pi.w, ri.w);
+        p4[i] = pi;
+      }
+      rr.add(ri.x, ri.x);
+      rr.add(ri.y, ri.y);
+      rr.add(ri.z, ri.z);
+      rr.add(ri.w, ri.w);
+      if (EXACT) {
+        const float4 di = idiag ? d4[i] : make_float4(1.f, 1.f, 1.f, 1.f);
+        // unscaled residual entry r^ sqrt(d): r^2 d = r^2 / (1/d); slots that are not free
+        // dofs hold r = 0 and 1/d = 0: skipped
+        rt.add(ri.x, di.x != 0.f ? ri.x / di.x : 0.f);
+        rt.add(ri.y, di.y != 0.f ? ri.y / di.y : 0.f);
+        rt.add(ri.z, di.z != 0.f ? ri.z / di.z : 0.f);
+        rt.add(ri.w, di.w != 0.f ? ri.w / di.w : 0.f);
+      }
+    }
+  }
+  for (int64_t i = (n4 << 2) + t0; i < n; i += stride) {
+    x[i] = fmaf(a, p[i], x[i]);
+    const float ri = fmaf(-a, q[i], r[i]);
+    r[i] = ri;
+    if (!keep_p) p[i] = fmaf(b, p[i], ri);
+    rr.add(ri, ri);
+    if (EXACT) {
+      const float di = idiag ? idiag[i] : 1.f;
+      rt.add(ri, di != 0.f ? ri / di : 0.f);
+    }
+  }
+  double v[2] = {rr.value(), rt.value()}, tot[2];
+  if (block_reduce_last<2>(v, rb, tot) && threadIdx.x == 0) {
+    const int it = I[I_ITER] + 1;
+    I[I_ITER] = it;
+    if (keep_p) {
+      // the segment ends: |r|^2 of the new residual for the record; the old one stays in
+      // S_RRH for the direction the host keeps
+      S[S_APP] = tot[0];
+      I[I_FLAG] = I[I_PEND] != FLAG_NONE ? I[I_PEND] : FLAG_UPDATE;
+      I[I_DONE] = 1;
+      return;
+    }
+    S[S_RRH] = tot[0];
+    const double rn = sqrt(tot[0]);
+    int pend = FLAG_NONE;
+    if (!(rn <= 1e4 * S[S_RMAX])) pend = FLAG_BREAK;  // NaN fails too
+    else if (EXACT && sqrt(tot[1]) * S[S_SIGMA] <= S[S_TOL]) pend = FLAG_CHECK;
+    else if (rn < S[S_DELTA] * S[S_RMAX]) pend = FLAG_UPDATE;
+    else if (it + 1 >= I[I_MAXIT]) pend = FLAG_MAXIT;
+    if (rn > S[S_RMAX]) S[S_RMAX] = rn;
+    S[S_RNSCALED] = rn;
+    I[I_PEND] = pend;
+  }
+}
+
+// x64 += sigma * s x^32; x^32 = 0 (s = D^-1/2 per slot; null: 1)
+__global__ void k_fold_scaled(int64_t n, double sigma, const double* __restrict__ sd, float* __restrict__ x32,
+                              double* __restrict__ x64) {
+  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+    const double si = sd ? sd[i] : 1.0;
+    x64[i] = fma(sigma * si, (double)x32[i], x64[i]);
+    x32[i] = 0.f;
+  }
+}
+
+// r^32 = s r64 / sigma_new; |r^|^2; beta for keeping the direction (first: p = r^).
+__global__ void __launch_bounds__(RB)
+    k_refresh_scaled(int64_t n, const double* __restrict__ r64, const double* __restrict__ sd, float* __restrict__ r32,
+                     int first, RedBuf rb, double* S, int* I) {
+  const double inv = 1.0 / S[S_ERR];  // S_ERR = ||b - A x64|| from the FP64 residual SpMV
+  Acc<float> rr;
+  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+    const float ri = (float)(r64[i] * inv * (sd ? sd[i] : 1.0));
+    r32[i] = ri;
+    rr.add(ri, ri);
+  }
+  double v[1] = {rr.value()}, tot[1];
+  if (block_reduce_last<1>(v, rb, tot) && threadIdx.x == 0) {
+    const double sig_old = S[S_SIGMA], sig_new = S[S_ERR];
+    if (first) {
+      S[S_BETA] = 0.0;
+    } else {
+      // old |r^|^2 and direction in the new scale: rr*(s_old/s_new)^2, p*(s_old/s_new)
+      const double q = sig_old / sig_new;
+      S[S_BETA] = tot[0] / (S[S_RRH] * q * q) * q;
+    }
+    S[S_RRH] = tot[0];
+    S[S_SIGMA] = sig_new;
+    S[S_RMAX] = sqrt(tot[0]);
+    I[I_DONE] = 0;
+    I[I_FLAG] = FLAG_NONE;
+    I[I_PEND] = FLAG_NONE;
+    I[I_SKIPP] = 0;
+  }
+}
+
+// s = sqrt(1/d) per solver slot (0 where 1/d is 0: slots that are not free dofs)
+__global__ void k_sqrt_idiag(int64_t n, const double* __restrict__ idiag, double* __restrict__ sd) {
+  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+    const double v = idiag[i];
+    sd[i] = v > 0.0 ? sqrt(v) : 0.0;
+  }
+}
+
+// FP32 copy of A^ = S A S in the lattice-implicit layout, from the FP64 values
+__global__ void __launch_bounds__(RB)
+    k_scale_stencil32(int64_t nslices, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
+                      const int32_t* __restrict__ soff, const int32_t* __restrict__ st_row,
+                      const double* __restrict__ tval, const double* __restrict__ sd, int ncomp, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * RB + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
+  for (int64_t s = warp; s < nslices; s += nwarps) {
+    const int k = scls[s];
+    const int64_t sbase = cls[k].sbase, vbase = cls[k].vbase;
+    const int Bp = cls[k].Bp, offbase = cls[k].offbase;
+    const int32_t st = st_row[s * 32 + lane];
+    const int32_t base = ncomp == 1 ? st : st - st % ncomp;
+    const double srow = sd[st + cls[k].ownoff];
+    const int64_t v0 = vbase + (s - sbase) * 32 * (int64_t)Bp + 4 * lane;
+    for (int j = 0; j < (Bp >> 2); ++j) {
+      const int4 o = __ldg(reinterpret_cast<const int4*>(soff + offbase) + j);
+      const int64_t e = v0 + (int64_t)j * 128;
+      out[e + 0] = (float)(tval[e + 0] * srow * sd[base + o.x]);
+      out[e + 1] = (float)(tval[e + 1] * srow * sd[base + o.y]);
+      out[e + 2] = (float)(tval[e + 2] * srow * sd[base + o.z]);
+      out[e + 3] = (float)(tval[e + 3] * srow * sd[base + o.w]);
+    }
+  }
+}
+
+// the same in the explicit-column SELL layout
+__global__ void __launch_bounds__(RB)
+    k_scale_sell32(int64_t nslices, int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+                   const double* __restrict__ sval, const double* __restrict__ sd, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * RB + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
+  for (int64_t s = warp; s < nslices; s += nwarps) {
+    const int64_t base = sptr[s];
+    const int w4 = (int)((sptr[s + 1] - base) >> 7);
+    const int64_t slot = s * 32 + lane;
+    const double srow = slot < n ? sd[slot] : 0.0;
+    for (int j = 0; j < w4; ++j) {
+      const int64_t e = base + 4 * lane + (int64_t)j * 128;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) out[e + t] = (float)(sval[e + t] * srow * sd[scol[e + t]]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // SELL SpMV, warp per slice, lane per row, slices strided over a fixed grid.
 // MODE 0: y = A x.  MODE 1: y = A x, <y,x> reduced, alpha = r_z/<Ap,p>.
 // MODE 2: y = b - A x (b FP64), <y,y> reduced into S_ERR as a norm.
@@ -147,11 +366,11 @@ __global__ void __launch_bounds__(RB)
     k_sell_spmv(int64_t nslices, int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
                 const T* __restrict__ sval, const T* __restrict__ x, T* __restrict__ y, const double* __restrict__ b,
                 RedBuf rb, double* S, const int* I) {
-  if (MODE == 1 && I[I_DONE]) return;
+  if ((MODE == 1 || MODE == 3) && I[I_DONE]) return;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * RB + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
-  Acc<T> dot;
+  Acc<T> dot, dot2;
   for (int64_t s = warp; s < nslices; s += nwarps) {
     const int64_t base = sptr[s];
     const int w4 = (int)((sptr[s + 1] - base) >> 7);  // groups of 4 entries per lane
@@ -179,11 +398,17 @@ __global__ void __launch_bounds__(RB)
         dot.add(rr, rr);
       } else {
         y[slot] = acc;
-        if (MODE == 1) dot.add(acc, x[slot]);
+        if (MODE == 1 || MODE == 3) dot.add(acc, x[slot]);
+        if (MODE == 3) dot2.add(acc, acc);
       }
     }
   }
   if (MODE == 0) return;
+  if (MODE == 3) {
+    double v2[2] = {dot.value(), dot2.value()}, tot2[2];
+    if (block_reduce_last<2>(v2, rb, tot2) && threadIdx.x == 0) mixed_alpha_beta(tot2[0], tot2[1], S, const_cast<int*>(I));
+    return;
+  }
   double v[1] = {dot.value()}, tot[1];
   if (block_reduce_last<1>(v, rb, tot) && threadIdx.x == 0) {
     if (MODE == 1) {
@@ -319,121 +544,6 @@ __global__ void __launch_bounds__(RB)
   }
 }
 
-// Mixed path, FP32 iteration: x += alpha p; r -= alpha Ap; reliable-update / stop decision.
-template <bool PRECOND>
-__global__ void __launch_bounds__(RB)
-    k_update32(int64_t n, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
-               const float* __restrict__ Ap, const float* __restrict__ idiag, RedBuf rb, double* S, int* I) {
-  if (I[I_DONE]) return;
-  const float a = (float)S[S_ALPHA];
-  Acc<float> rr, rz;
-  // four entries per thread and load (the vectors are 16-byte aligned), then the tail
-  const int64_t t0 = blockIdx.x * (int64_t)RB + threadIdx.x, stride = (int64_t)gridDim.x * RB;
-  const int64_t n4 = n >> 2;
-  {
-    float4* x4 = reinterpret_cast<float4*>(x);
-    float4* r4 = reinterpret_cast<float4*>(r);
-    const float4* p4 = reinterpret_cast<const float4*>(p);
-    const float4* a4 = reinterpret_cast<const float4*>(Ap);
-    const float4* d4 = reinterpret_cast<const float4*>(idiag);
-    for (int64_t i = t0; i < n4; i += stride) {
-      float4 xi = x4[i], ri = r4[i];
-      const float4 pi = p4[i], api = a4[i];
-      float4 di = make_float4(1.f, 1.f, 1.f, 1.f);
-      if (PRECOND) di = d4[i];
-      xi.x = fmaf(a, pi.x, xi.x);
-      xi.y = fmaf(a, pi.y, xi.y);
-      xi.z = fmaf(a, pi.z, xi.z);
-      xi.w = fmaf(a, pi.w, xi.w);
-      ri.x = fmaf(-a, api.x, ri.x);
-      ri.y = fmaf(-a, api.y, ri.y);
-      ri.z = fmaf(-a, api.z, ri.z);
-      ri.w = fmaf(-a, api.w, ri.w);
-      x4[i] = xi;
-      r4[i] = ri;
-      rr.add(ri.x, ri.x);
-      rr.add(ri.y, ri.y);
-      rr.add(ri.z, ri.z);
-      rr.add(ri.w, ri.w);
-      if (PRECOND) {
-        rz.add(ri.x, di.x * ri.x);
-        rz.add(ri.y, di.y * ri.y);
-        rz.add(ri.z, di.z * ri.z);
-        rz.add(ri.w, di.w * ri.w);
-      }
-    }
-  }
-  for (int64_t i = (n4 << 2) + t0; i < n; i += stride) {
-    x[i] = fmaf(a, p[i], x[i]);
-    const float ri = fmaf(-a, Ap[i], r[i]);
-    r[i] = ri;
-    rr.add(ri, ri);
-    if (PRECOND) rz.add(ri, idiag[i] * ri);
-  }
-  double v[2] = {rr.value(), PRECOND ? rz.value() : rr.value()}, tot[2];
-  if (block_reduce_last<2>(v, rb, tot) && threadIdx.x == 0) {
-    const int it = I[I_ITER] + 1;
-    I[I_ITER] = it;
-    const double rn = sqrt(tot[0]);  // residual norm in the current scale
-    S[S_RNSCALED] = rn;
-    const double est = rn * S[S_SIGMA];
-    int flag = FLAG_NONE;
-    if (!(rn <= 1e4 * S[S_RMAX]) || !(tot[1] > 0.0 && tot[1] <= 1e300)) flag = FLAG_BREAK;  // NaN fails both
-    else if (est <= S[S_TOL]) flag = FLAG_CHECK;
-    else if (rn < S[S_DELTA] * S[S_RMAX]) flag = FLAG_UPDATE;
-    else if (it >= I[I_MAXIT]) flag = FLAG_MAXIT;
-    if (rn > S[S_RMAX]) S[S_RMAX] = rn;
-    S[S_APP] = tot[1];  // r_z of the new residual (used by the reliable update for beta)
-    if (flag != FLAG_NONE) {
-      I[I_FLAG] = flag;
-      I[I_DONE] = 1;
-    } else {
-      const double beta = tot[1] / S[S_RZ];
-      S[S_RZ] = tot[1];
-      S[S_BETA] = beta;
-    }
-  }
-}
-
-// x64 += sigma * x32; x32 = 0
-__global__ void k_fold(int64_t n, double sigma, float* __restrict__ x32, double* __restrict__ x64) {
-  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
-    x64[i] = fma(sigma, (double)x32[i], x64[i]);
-    x32[i] = 0.f;
-  }
-}
-
-// r32 = r64/sigma_new; r_z of it; beta for keeping the direction (first: p = z).
-template <bool PRECOND>
-__global__ void __launch_bounds__(RB)
-    k_refresh(int64_t n, const double* __restrict__ r64, float* __restrict__ r32, const float* __restrict__ idiag,
-              int first, RedBuf rb, double* S, int* I) {
-  const double inv = 1.0 / S[S_ERR];  // S_ERR = ||b - A x64|| from the FP64 residual SpMV
-  Acc<float> rz;
-  for (int64_t i = blockIdx.x * (int64_t)RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
-    const float ri = (float)(r64[i] * inv);
-    r32[i] = ri;
-    rz.add(ri, PRECOND ? idiag[i] * ri : ri);
-  }
-  double v[1] = {rz.value()}, tot[1];
-  if (block_reduce_last<1>(v, rb, tot) && threadIdx.x == 0) {
-    const double sig_old = S[S_SIGMA], sig_new = S[S_ERR];
-    if (first) {
-      S[S_BETA] = 0.0;
-    } else {
-      // old r_z and direction expressed in the new scale: rz*(s_old/s_new)^2, p*(s_old/s_new)
-      const double q = sig_old / sig_new;
-      const double beta = tot[0] / (S[S_RZ] * q * q);
-      S[S_BETA] = beta * q;
-    }
-    S[S_RZ] = tot[0];
-    S[S_SIGMA] = sig_new;
-    S[S_RMAX] = 1.0;
-    I[I_DONE] = 0;
-    I[I_FLAG] = FLAG_NONE;
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Lattice-implicit SELL SpMV: warp per slice, lane per row, 4 values per lane per load;
 // the column of box position k is the row's node plus the class offset k.
@@ -454,11 +564,11 @@ __global__ void __launch_bounds__(RB)
                    const int32_t* __restrict__ soff, const int32_t* __restrict__ st_row, const T* __restrict__ tval,
                    int ncomp, const T* __restrict__ x, T* __restrict__ y, const double* __restrict__ b, RedBuf rb,
                    double* S, const int* I) {
-  if (MODE == 1 && I[I_DONE]) return;
+  if ((MODE == 1 || MODE == 3) && I[I_DONE]) return;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * RB + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
-  Acc<T> dot;
+  Acc<T> dot, dot2;
   for (int64_t s = warp; s < nslices; s += nwarps) {
     const int k = scls[s];
     const int64_t sbase = cls[k].sbase, nrows = cls[k].nrows, vbase = cls[k].vbase;
@@ -497,11 +607,17 @@ __global__ void __launch_bounds__(RB)
         dot.add(rr, rr);
       } else {
         y[vec] = acc;
-        if (MODE == 1) dot.add(acc, x[vec]);
+        if (MODE == 1 || MODE == 3) dot.add(acc, x[vec]);
+        if (MODE == 3) dot2.add(acc, acc);
       }
     }
   }
   if (MODE == 0) return;
+  if (MODE == 3) {
+    double v2[2] = {dot.value(), dot2.value()}, tot2[2];
+    if (block_reduce_last<2>(v2, rb, tot2) && threadIdx.x == 0) mixed_alpha_beta(tot2[0], tot2[1], S, const_cast<int*>(I));
+    return;
+  }
   double v[1] = {dot.value()}, tot[1];
   if (block_reduce_last<1>(v, rb, tot) && threadIdx.x == 0) {
     if (MODE == 1) {
@@ -661,6 +777,47 @@ FG_SPMV_IMPL(float, 0, d_sval32, d_tval32)
 FG_SPMV_IMPL(float, 1, d_sval32, d_tval32)
 #undef FG_SPMV_IMPL
 
+// FP32 SpMV of the fused mixed iteration on the given values (the scaled copy with Jacobi,
+// the plain FP32 copy without a preconditioner)
+static void spmv_fused32(fg_system* sys, const Work& w, const float* vals, const float* x, float* y, cudaStream_t st) {
+  fg_space* sp = sys->space;
+  if (sp->layout == FG_LAYOUT_STENCIL)
+    launch_k(k_stencil_spmv<float, 3>, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls,
+             (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row, vals,
+             sp->ncomp, x, y, (const double*)nullptr, w.rb, w.S, (const int*)w.I);
+  else
+    launch_k(k_sell_spmv<float, 3>, w, st, sp->nslices, sp->nfree, (const int64_t*)sp->d_sptr,
+             (const int32_t*)sp->d_scol, vals, x, y, (const double*)nullptr, w.rb, w.S, (const int*)w.I);
+  sp->mesh->ctx->launches += 1;
+}
+
+// D^-1/2 and the FP32 copy of D^-1/2 A D^-1/2 (once per numeric assembly)
+static fg_status ensure_scaled(fg_system* sys, const Work& w) {
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  if (sys->scaled_valid) return FG_OK;
+  const bool stencil = sp->layout == FG_LAYOUT_STENCIL;
+  const int64_t nvals = stencil ? sp->st_nvals : sp->sell_nnz;
+  const double* v64 = stencil ? sys->d_tval : sys->d_sval;
+  if (!v64) { set_error("the FP64 solver-layout values are not available"); return FG_ERR_UNSUPPORTED; }
+  const int64_t nv = sp->nvec > 0 ? sp->nvec : 1;
+  if (!sys->d_sdiag) FG_TRY(dev_alloc(ctx, (void**)&sys->d_sdiag, sizeof(double) * nv));
+  if (!sys->d_val32s) FG_TRY(dev_alloc(ctx, (void**)&sys->d_val32s, sizeof(float) * (nvals > 0 ? nvals : 1)));
+  cudaStream_t st = ctx->stream;
+  launch_k(k_sqrt_idiag, w, st, nv, (const double*)sys->d_idiag, sys->d_sdiag);
+  if (stencil)
+    launch_k(k_scale_stencil32, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls, (const StencilClass*)sp->d_st_cls,
+             (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row, v64, (const double*)sys->d_sdiag, sp->ncomp,
+             sys->d_val32s);
+  else
+    launch_k(k_scale_sell32, w, st, sp->nslices, sp->nfree, (const int64_t*)sp->d_sptr, (const int32_t*)sp->d_scol, v64,
+             (const double*)sys->d_sdiag, sys->d_val32s);
+  ctx->launches += 2;
+  FG_CUDA_TRY(cudaGetLastError());
+  sys->scaled_valid = true;
+  return FG_OK;
+}
+
 // y = A x in row order (device pointers): into the solver layout, SpMV, back.
 fg_status system_spmv(fg_system* sys, int precision, const void* x, void* y, cudaStream_t st) {
   fg_space* sp = sys->space;
@@ -727,18 +884,13 @@ static void iter64(fg_system* sys, const Work& w, int precond, bool need_pp, int
   else launch_k(k_pupdate<double, false>, w, st, n, w.p, (const double*)w.r, (const double*)sys->d_idiag, (const double*)w.S, (const int*)w.I);
 }
 
-// Launch one FP32 CG iteration of the mixed path (3 kernels).
-static void iter32(fg_system* sys, const Work& w, int precond, cudaStream_t st) {
-  fg_space* sp = sys->space;
-  const int64_t n = sp->nvec;
-  spmv_k<float, 1>(sys, w, w.p32, w.Ap32, nullptr, st);
-  if (precond) {
-    launch_k(k_update32<true>, w, st, n, w.x32, w.r32, (const float*)w.p32, (const float*)w.Ap32, (const float*)sys->d_idiag32, w.rb, w.S, w.I);
-    launch_k(k_pupdate<float, true>, w, st, n, w.p32, (const float*)w.r32, (const float*)sys->d_idiag32, (const double*)w.S, (const int*)w.I);
-  } else {
-    launch_k(k_update32<false>, w, st, n, w.x32, w.r32, (const float*)w.p32, (const float*)w.Ap32, (const float*)sys->d_idiag32, w.rb, w.S, w.I);
-    launch_k(k_pupdate<float, false>, w, st, n, w.p32, (const float*)w.r32, (const float*)sys->d_idiag32, (const double*)w.S, (const int*)w.I);
-  }
+// Launch one fused FP32 iteration of the mixed path (2 kernels); `exact`: this update also
+// sums the unscaled residual norm for the stop estimate.
+static void iter32s(fg_system* sys, const Work& w, const float* vals, const float* idiag32, bool exact, cudaStream_t st) {
+  const int64_t n = sys->space->nvec;
+  spmv_fused32(sys, w, vals, w.p32, w.Ap32, st);
+  if (exact) launch_k(k_update32s<true>, w, st, n, w.x32, w.r32, w.p32, (const float*)w.Ap32, idiag32, w.rb, w.S, w.I);
+  else launch_k(k_update32s<false>, w, st, n, w.x32, w.r32, w.p32, (const float*)w.Ap32, idiag32, w.rb, w.S, w.I);
 }
 
 // Capture `chunk` iterations into a graph and replay it until the device done flag is set.
@@ -861,11 +1013,20 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
       int hI0[I_COUNT] = {0};
       hI0[I_MAXIT] = prm->max_iters;
       FG_CUDA_TRY(cudaMemcpyAsync(w.I, hI0, sizeof(hI0), cudaMemcpyHostToDevice, st));
+      // FP32 segments on D^-1/2 A D^-1/2 (Jacobi) or A (no preconditioner), fused iterations
+      const double* sd = nullptr;
+      const float* vals32 = sp->layout == FG_LAYOUT_STENCIL ? sys->d_tval32 : sys->d_sval32;
+      const float* id32 = nullptr;
+      if (precond) {
+        FG_TRY(ensure_scaled(sys, w));
+        sd = sys->d_sdiag;
+        vals32 = sys->d_val32s;
+        id32 = sys->d_idiag32;
+      }
       auto refresh = [&](int first) {
-        if (precond) launch_k(k_refresh<true>, w, st, nv, (const double*)w.r, w.r32, (const float*)sys->d_idiag32, first, w.rb, w.S, w.I);
-        else launch_k(k_refresh<false>, w, st, nv, (const double*)w.r, w.r32, (const float*)sys->d_idiag32, first, w.rb, w.S, w.I);
-        if (precond) launch_k(k_pupdate<float, true>, w, st, nv, w.p32, (const float*)w.r32, (const float*)sys->d_idiag32, (const double*)w.S, (const int*)w.I);
-        else launch_k(k_pupdate<float, false>, w, st, nv, w.p32, (const float*)w.r32, (const float*)sys->d_idiag32, (const double*)w.S, (const int*)w.I);
+        launch_k(k_refresh_scaled, w, st, nv, (const double*)w.r, sd, w.r32, first, w.rb, w.S, w.I);
+        launch_k(k_pupdate<float, false>, w, st, nv, w.p32, (const float*)w.r32, (const float*)nullptr,
+                 (const double*)w.S, (const int*)w.I);
         ctx->launches += 2;
       };
       refresh(1);
@@ -874,7 +1035,7 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
       cudaGraph_t graph = nullptr;
       cudaGraphExec_t exec = nullptr;
       FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < chunk; ++k) iter32(sys, w, precond, st);
+      for (int k = 0; k < chunk; ++k) iter32s(sys, w, vals32, id32, (k & 3) == 3, st);
       cudaError_t e = cudaStreamEndCapture(st, &graph);
       if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
       if (e != cudaSuccess) {
@@ -895,7 +1056,7 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
         FG_CUDA_TRY(cudaStreamSynchronize(st));
         const bool broke = h_I[I_FLAG] == FLAG_BREAK;
         if (broke) k_fill<float><<<nblk(nv, RB), RB, 0, st>>>(nv, w.x32, 0.0f);
-        else launch_k(k_fold, w, st, nv, h_S[S_SIGMA], w.x32, w.x);
+        else launch_k(k_fold_scaled, w, st, nv, h_S[S_SIGMA], sd, w.x32, w.x);
         ctx->launches += 1;
         spmv_k<double, 2>(sys, w, w.x, w.r, w.b, st);
         ++outer;
@@ -918,7 +1079,7 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
       cudaGraphDestroy(graph);
       FG_CUDA_TRY(cudaMemcpyAsync(h_I, w.I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, st));
       FG_CUDA_TRY(cudaStreamSynchronize(st));
-      ctx->launches += graph_launches * 3 * chunk;
+      ctx->launches += graph_launches * 2 * chunk;
       if (polish && status == FG_OK) {
         // FP64 PCG from x64 to the same absolute tolerance, with the iterations left
         const int mixed_its = h_I[I_ITER];
