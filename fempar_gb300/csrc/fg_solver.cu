@@ -78,6 +78,25 @@ struct Acc<float> {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// plain FP32 per-thread sum (products rounded): for sums whose terms are all positive
+struct AccPlain {
+  float s = 0.f;
+  __device__ __forceinline__ void add(float a, float b) { s = fmaf(a, b, s); }
+  __device__ __forceinline__ double value() const { return (double)s; }
+};
+
+// <q,q> of the fused mixed SpMV: compensated (1) or plain per-thread FP32 sums (0).  Measured
+// on GB300 at 128^3 Q2: plain sums 1097 iterations and 0.853 ms per iteration, compensated
+// 1106 and 0.863 ms (a thread sums ~80 positive terms; the grid total is formed in FP64).
+#ifndef FG_MIXED_QQ_COMPENSATED
+#define FG_MIXED_QQ_COMPENSATED 0
+#endif
+// the fused update sums the unscaled residual norm (the stop estimate) every
+// FG_MIXED_EXACT_EVERY iterations (a divisor of the graph chunk); 8 vs 4: -2 us per iteration
+#ifndef FG_MIXED_EXACT_EVERY
+#define FG_MIXED_EXACT_EVERY 8
+#endif
+
 template <int NV>
 __device__ __forceinline__ bool block_reduce_last(double (&v)[NV], const RedBuf& rb, double (&tot)[NV]) {
   __shared__ double sw[NV][RB / 32];
@@ -370,7 +389,12 @@ __global__ void __launch_bounds__(RB)
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * RB + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
-  Acc<T> dot, dot2;
+  Acc<T> dot;
+#if FG_MIXED_QQ_COMPENSATED
+  Acc<T> dot2;
+#else
+  AccPlain dot2;
+#endif
   for (int64_t s = warp; s < nslices; s += nwarps) {
     const int64_t base = sptr[s];
     const int w4 = (int)((sptr[s + 1] - base) >> 7);  // groups of 4 entries per lane
@@ -560,7 +584,8 @@ static constexpr int kPrefetch = FG_SPMV_PREFETCH;  // value groups (of 4 entrie
 static constexpr int kUnroll = FG_SPMV_UNROLL;      // value groups per unrolled step
 template <typename T, int MODE>
 __global__ void __launch_bounds__(RB)
-    k_stencil_spmv(int64_t nslices, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
+    k_stencil_spmv(int64_t nslices, const int32_t* __restrict__ sorder, const uint8_t* __restrict__ scls,
+                   const StencilClass* __restrict__ cls,
                    const int32_t* __restrict__ soff, const int32_t* __restrict__ st_row, const T* __restrict__ tval,
                    int ncomp, const T* __restrict__ x, T* __restrict__ y, const double* __restrict__ b, RedBuf rb,
                    double* S, const int* I) {
@@ -568,8 +593,14 @@ __global__ void __launch_bounds__(RB)
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * RB + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
-  Acc<T> dot, dot2;
-  for (int64_t s = warp; s < nslices; s += nwarps) {
+  Acc<T> dot;
+#if FG_MIXED_QQ_COMPENSATED
+  Acc<T> dot2;
+#else
+  AccPlain dot2;
+#endif
+  for (int64_t t = warp; t < nslices; t += nwarps) {
+    const int64_t s = sorder[t];
     const int k = scls[s];
     const int64_t sbase = cls[k].sbase, nrows = cls[k].nrows, vbase = cls[k].vbase;
     const int Bp = cls[k].Bp, offbase = cls[k].offbase;
@@ -762,7 +793,8 @@ static void spmv_k(fg_system* sys, const Work& w, const T* x, T* y, const double
   void spmv_k<T, MODE>(fg_system * sys, const Work& w, const T* x, T* y, const double* b, cudaStream_t st) {       \
     fg_space* sp = sys->space;                                                                                      \
     if (sp->layout == FG_LAYOUT_STENCIL)                                                                            \
-      launch_k(k_stencil_spmv<T, MODE>, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls,                       \
+      launch_k(k_stencil_spmv<T, MODE>, w, st, sp->st_nslices, (const int32_t*)sp->d_st_order,                     \
+               (const uint8_t*)sp->d_st_scls,                                                                       \
                (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row,       \
                (const T*)sys->TVALS, sp->ncomp, x, y, b, w.rb, w.S, (const int*)w.I);                               \
     else                                                                                                            \
@@ -782,7 +814,8 @@ FG_SPMV_IMPL(float, 1, d_sval32, d_tval32)
 static void spmv_fused32(fg_system* sys, const Work& w, const float* vals, const float* x, float* y, cudaStream_t st) {
   fg_space* sp = sys->space;
   if (sp->layout == FG_LAYOUT_STENCIL)
-    launch_k(k_stencil_spmv<float, 3>, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls,
+    launch_k(k_stencil_spmv<float, 3>, w, st, sp->st_nslices, (const int32_t*)sp->d_st_order,
+             (const uint8_t*)sp->d_st_scls,
              (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row, vals,
              sp->ncomp, x, y, (const double*)nullptr, w.rb, w.S, (const int*)w.I);
   else
@@ -1035,7 +1068,8 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
       cudaGraph_t graph = nullptr;
       cudaGraphExec_t exec = nullptr;
       FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < chunk; ++k) iter32s(sys, w, vals32, id32, (k & 3) == 3, st);
+      for (int k = 0; k < chunk; ++k)
+        iter32s(sys, w, vals32, id32, k % FG_MIXED_EXACT_EVERY == FG_MIXED_EXACT_EVERY - 1, st);
       cudaError_t e = cudaStreamEndCapture(st, &graph);
       if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
       if (e != cudaSuccess) {
