@@ -150,7 +150,6 @@ struct fg_space {
   fg::StencilClass* d_st_cls = nullptr;
   int32_t* d_st_off = nullptr;    // box offsets per class
   uint8_t* d_st_scls = nullptr;   // class of each slice
-  int32_t* d_st_order = nullptr;  // st_nslices: order in which the SpMV visits the slices
   int32_t* d_st_row = nullptr;    // 32*st_nslices: solver vector index of each row slot
   int32_t* d_row2st = nullptr;    // free row -> row slot
   int32_t* d_st_slot2row = nullptr;  // 32*st_nslices: free row of each row slot (-1: padding)

@@ -584,8 +584,7 @@ static constexpr int kPrefetch = FG_SPMV_PREFETCH;  // value groups (of 4 entrie
 static constexpr int kUnroll = FG_SPMV_UNROLL;      // value groups per unrolled step
 template <typename T, int MODE>
 __global__ void __launch_bounds__(RB)
-    k_stencil_spmv(int64_t nslices, const int32_t* __restrict__ sorder, const uint8_t* __restrict__ scls,
-                   const StencilClass* __restrict__ cls,
+    k_stencil_spmv(int64_t nslices, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
                    const int32_t* __restrict__ soff, const int32_t* __restrict__ st_row, const T* __restrict__ tval,
                    int ncomp, const T* __restrict__ x, T* __restrict__ y, const double* __restrict__ b, RedBuf rb,
                    double* S, const int* I) {
@@ -599,8 +598,7 @@ __global__ void __launch_bounds__(RB)
 #else
   AccPlain dot2;
 #endif
-  for (int64_t t = warp; t < nslices; t += nwarps) {
-    const int64_t s = sorder[t];
+  for (int64_t s = warp; s < nslices; s += nwarps) {
     const int k = scls[s];
     const int64_t sbase = cls[k].sbase, nrows = cls[k].nrows, vbase = cls[k].vbase;
     const int Bp = cls[k].Bp, offbase = cls[k].offbase;
@@ -793,8 +791,7 @@ static void spmv_k(fg_system* sys, const Work& w, const T* x, T* y, const double
   void spmv_k<T, MODE>(fg_system * sys, const Work& w, const T* x, T* y, const double* b, cudaStream_t st) {       \
     fg_space* sp = sys->space;                                                                                      \
     if (sp->layout == FG_LAYOUT_STENCIL)                                                                            \
-      launch_k(k_stencil_spmv<T, MODE>, w, st, sp->st_nslices, (const int32_t*)sp->d_st_order,                     \
-               (const uint8_t*)sp->d_st_scls,                                                                       \
+      launch_k(k_stencil_spmv<T, MODE>, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls,                       \
                (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row,       \
                (const T*)sys->TVALS, sp->ncomp, x, y, b, w.rb, w.S, (const int*)w.I);                               \
     else                                                                                                            \
@@ -814,8 +811,7 @@ FG_SPMV_IMPL(float, 1, d_sval32, d_tval32)
 static void spmv_fused32(fg_system* sys, const Work& w, const float* vals, const float* x, float* y, cudaStream_t st) {
   fg_space* sp = sys->space;
   if (sp->layout == FG_LAYOUT_STENCIL)
-    launch_k(k_stencil_spmv<float, 3>, w, st, sp->st_nslices, (const int32_t*)sp->d_st_order,
-             (const uint8_t*)sp->d_st_scls,
+    launch_k(k_stencil_spmv<float, 3>, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls,
              (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row, vals,
              sp->ncomp, x, y, (const double*)nullptr, w.rb, w.S, (const int*)w.I);
   else
@@ -1068,8 +1064,8 @@ fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double
       cudaGraph_t graph = nullptr;
       cudaGraphExec_t exec = nullptr;
       FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < chunk; ++k)
-        iter32s(sys, w, vals32, id32, k % FG_MIXED_EXACT_EVERY == FG_MIXED_EXACT_EVERY - 1, st);
+      for (int k = 0; k < chunk; ++k)  // at least the last iteration of a chunk sums the stop estimate
+        iter32s(sys, w, vals32, id32, k % FG_MIXED_EXACT_EVERY == FG_MIXED_EXACT_EVERY - 1 || k == chunk - 1, st);
       cudaError_t e = cudaStreamEndCapture(st, &graph);
       if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
       if (e != cudaSuccess) {

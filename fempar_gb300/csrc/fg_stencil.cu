@@ -15,9 +15,6 @@
 // halo and padding nodes stay zero.  Box positions outside the domain or on Dirichlet
 // nodes hold value 0.  For Q2 Poisson at 128^3 the FP32 matrix is 4 B per stored entry
 // instead of 8 B with explicit int32 columns.
-#include <algorithm>
-#include <utility>
-
 #include <cub/cub.cuh>
 
 #include "fg_internal.h"
@@ -192,29 +189,11 @@ fg_status space_build_stencil(fg_space* sp) {
   std::vector<uint8_t> hscls(nsl > 0 ? nsl : 1);
   for (int k = 0; k < ncls; ++k)
     for (int64_t s = 0; s < (cls[k].nrows + 31) / 32; ++s) hscls[cls[k].sbase + s] = (uint8_t)k;
-  // SpMV visiting order: the classes interleaved by position.  A class's slices run through
-  // its sub-lattice in lattice order, so slice j of class k lies near the fraction
-  // (j + 1/2)/nslices_k of the domain; visiting all classes' slices in that order keeps the
-  // x entries their boxes gather (the neighbouring nodes of every class) in a moving band
-  // that stays in L2, where a class-by-class sweep gathers all of x once per class.
-  std::vector<int32_t> horder(nsl > 0 ? nsl : 1, 0);
-  {
-    std::vector<std::pair<double, int32_t>> key;
-    key.reserve(nsl);
-    for (int k = 0; k < ncls; ++k) {
-      const int64_t ns = (cls[k].nrows + 31) / 32;
-      for (int64_t j = 0; j < ns; ++j) key.emplace_back((j + 0.5) / (double)ns, (int32_t)(cls[k].sbase + j));
-    }
-    std::stable_sort(key.begin(), key.end(),
-                     [](const std::pair<double, int32_t>& a, const std::pair<double, int32_t>& b) { return a.first < b.first; });
-    for (int64_t t = 0; t < nsl; ++t) horder[t] = key[t].second;
-  }
   int64_t* d_cstart = nullptr;
   int* d_dims = nullptr;
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_cls, sizeof(StencilClass) * ncls));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_off, sizeof(int32_t) * offs.size()));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_scls, hscls.size()));
-  FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_order, sizeof(int32_t) * horder.size()));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_row, sizeof(int32_t) * (nsl > 0 ? nsl * 32 : 1)));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_row2st, sizeof(int32_t) * (sp->nfree > 0 ? sp->nfree : 1)));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_slot2row, sizeof(int32_t) * (nsl > 0 ? nsl * 32 : 1)));
@@ -226,8 +205,6 @@ fg_status space_build_stencil(fg_space* sp) {
   FG_CUDA_TRY(cudaMemcpyAsync(sp->d_st_cls, cls.data(), sizeof(StencilClass) * ncls, cudaMemcpyHostToDevice, ctx->stream));
   FG_CUDA_TRY(cudaMemcpyAsync(sp->d_st_off, offs.data(), sizeof(int32_t) * offs.size(), cudaMemcpyHostToDevice, ctx->stream));
   FG_CUDA_TRY(cudaMemcpyAsync(sp->d_st_scls, hscls.data(), hscls.size(), cudaMemcpyHostToDevice, ctx->stream));
-  FG_CUDA_TRY(cudaMemcpyAsync(sp->d_st_order, horder.data(), sizeof(int32_t) * horder.size(), cudaMemcpyHostToDevice,
-                              ctx->stream));
   FG_CUDA_TRY(cudaMemcpyAsync(d_cstart, cstart.data(), sizeof(int64_t) * (ncls + 1), cudaMemcpyHostToDevice, ctx->stream));
   FG_CUDA_TRY(cudaMemcpyAsync(d_dims, hdims, sizeof(hdims), cudaMemcpyHostToDevice, ctx->stream));
   if (sp->nfree > 0) {
