@@ -247,9 +247,10 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-# DRAM bytes per stored byte of the FP32 SpMV launch, from one ncu capture at 64^3
-# (dram__bytes_read.sum + dram__bytes_write.sum = 555.2 MB + 4.8 MB for 556.9 MB stored)
-DRAM_PER_STORED_BYTE_FP32 = 560.0 / 556.93
+# DRAM bytes per stored byte of the FP32 SpMV launch at 128^3 Q2, one ncu capture of the
+# full-size launch (dram__bytes_read.sum + dram__bytes_write.sum = 4990 MB + 65 MB for 4508.9 MB
+# stored): the values once, the x vector about 7 times (once per node class)
+DRAM_PER_STORED_BYTE_FP32 = 5055.0 / 4508.9
 
 
 def replica_aggregate(dist, times_ms, units, device="cpu"):
@@ -531,12 +532,13 @@ def main():
         "mixed_vs_fp64": value / v64,
         "e2e": {"value": ve2e, "unit": "DOF/s", "h2d_bytes_per_step": int(coef.nbytes),
                 "d2h_bytes_per_step": int(nfree * 8), "ms_per_step": ms_e2e},
-        "roofline": {"bound": "hbm", "kernel": f"{kname}<float,0> (FP32 SpMV, {layout})",
+        "roofline": {"bound": "hbm", "kernel": f"{kname}<float,0> (FP32 SpMV, {layout}; the iteration runs MODE 3, the same "
+                               "bytes plus two dot products)",
                      "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
                      "peak_source": "of measured" if pk else "of fallback",
                      "traffic": DRAM_PER_STORED_BYTE_FP32 * fmt32,
-                     "traffic_source": "ncu dram__bytes_read+write of this kernel at 64^3 (560.0 MB = 1.005 x its "
-                                       "stored bytes), scaled to this launch by the stored bytes",
+                     "traffic_source": "ncu dram__bytes_read+write of this kernel at 128^3 Q2 (5055 MB = 1.121 x its "
+                                       "stored bytes: values once, x re-read per node class), scaled by the stored bytes",
                      "bytes_per_launch": b32, "ms_per_launch": ms32,
                      "bytes_def": "4*nnz + 8*n (values once, x once, y once)",
                      "format_bytes_per_launch": fmt32, "format_frac": fmt32 / (ms32 * 1e-3) / 1e9 / hbm,
