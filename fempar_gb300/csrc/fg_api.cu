@@ -368,6 +368,7 @@ static void space_free(fg_space* sp) {
   dev_free(ctx, sp->d_st_cls);
   dev_free(ctx, sp->d_st_off);
   dev_free(ctx, sp->d_st_scls);
+  dev_free(ctx, sp->d_st_voff);
   dev_free(ctx, sp->d_st_row);
   dev_free(ctx, sp->d_row2st);
   dev_free(ctx, sp->d_st_slot2row);

@@ -548,7 +548,8 @@ __global__ void __launch_bounds__(W * 32)
 // FP32, padding included: no clearing pass and no CSR in between.
 template <int P, int NC, int W>
 __global__ void __launch_bounds__(W * 32)
-    k_scatter_stencil(AsmGeom g, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
+    k_scatter_stencil(AsmGeom g, const uint8_t* __restrict__ scls, const int64_t* __restrict__ voff,
+                      const StencilClass* __restrict__ cls,
                       const int32_t* __restrict__ slot2row, const int32_t* __restrict__ free2lat,
                       const int32_t* __restrict__ latdof, const double* __restrict__ E, const double* __restrict__ EV,
                       double* __restrict__ tval, float* __restrict__ tval32, double* __restrict__ rhs) {
@@ -628,7 +629,7 @@ __global__ void __launch_bounds__(W * 32)
     if (lane == 0) rhs[r] = rsum;
   }
   __syncthreads();
-  const int64_t vb = C.vbase + (sl - C.sbase) * 32 * (int64_t)Bp;
+  const int64_t vb = voff[sl];
   for (int k = threadIdx.x; k < 32 * Bp; k += W * 32) {
     const int grp = k >> 7, w = k & 127;
     const double x = s_slice[(w >> 2) * stride + grp * 4 + (w & 3)];
@@ -656,7 +657,7 @@ static fg_status launch_scatter_stencil(fg_system* sys, const AsmGeom& g) {
   if (sp->st_nslices > 0) {
     ctx->launches += 1;
     k_scatter_stencil<P, NC, W><<<(unsigned)sp->st_nslices, W * 32, smem, ctx->stream>>>(
-        g, sp->d_st_scls, sp->d_st_cls, sp->d_st_slot2row, sp->d_free2lat, sp->d_latdof, sys->d_elmat, sys->d_elvec,
+        g, sp->d_st_scls, sp->d_st_voff, sp->d_st_cls, sp->d_st_slot2row, sp->d_free2lat, sp->d_latdof, sys->d_elmat, sys->d_elvec,
         sys->d_tval, sys->d_tval32, sys->d_rhs);
     FG_CUDA_TRY(cudaGetLastError());
   }

@@ -56,8 +56,8 @@ struct RefTables {
 
 // One row class of the lattice-implicit SELL layout (fg_stencil.cu).
 struct StencilClass {
-  int64_t vbase;   // first value of the class
-  int64_t sbase;   // first slice of the class
+  int64_t vbase;   // first value of the class in class-by-class storage (set-up only)
+  int64_t sbase;   // first slice of the class in class-by-class numbering (set-up only)
   int64_t nrows;   // rows of the class
   int lo[3], w[3]; // box start (relative to the row's node) and width per direction
   int B, Bp;       // box entries (all components) and the 4-padded count
@@ -150,6 +150,7 @@ struct fg_space {
   fg::StencilClass* d_st_cls = nullptr;
   int32_t* d_st_off = nullptr;    // box offsets per class
   uint8_t* d_st_scls = nullptr;   // class of each slice
+  int64_t* d_st_voff = nullptr;   // first value of each slice (slices are stored interleaved)
   int32_t* d_st_row = nullptr;    // 32*st_nslices: solver vector index of each row slot
   int32_t* d_row2st = nullptr;    // free row -> row slot
   int32_t* d_st_slot2row = nullptr;  // 32*st_nslices: free row of each row slot (-1: padding)

@@ -331,7 +331,8 @@ __global__ void k_sqrt_idiag(int64_t n, const double* __restrict__ idiag, double
 
 // FP32 copy of A^ = S A S in the lattice-implicit layout, from the FP64 values
 __global__ void __launch_bounds__(RB)
-    k_scale_stencil32(int64_t nslices, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
+    k_scale_stencil32(int64_t nslices, const uint8_t* __restrict__ scls, const int64_t* __restrict__ voff,
+                      const StencilClass* __restrict__ cls,
                       const int32_t* __restrict__ soff, const int32_t* __restrict__ st_row,
                       const double* __restrict__ tval, const double* __restrict__ sd, int ncomp, float* __restrict__ out) {
   const int lane = threadIdx.x & 31;
@@ -339,12 +340,12 @@ __global__ void __launch_bounds__(RB)
   const int64_t nwarps = ((int64_t)gridDim.x * RB) >> 5;
   for (int64_t s = warp; s < nslices; s += nwarps) {
     const int k = scls[s];
-    const int64_t sbase = cls[k].sbase, vbase = cls[k].vbase;
     const int Bp = cls[k].Bp, offbase = cls[k].offbase;
-    const int32_t st = st_row[s * 32 + lane];
+    int32_t st = st_row[s * 32 + lane];
+    if (st < 0) st = ~st;  // padding lane: the slice's first row (its values are 0)
     const int32_t base = ncomp == 1 ? st : st - st % ncomp;
     const double srow = sd[st + cls[k].ownoff];
-    const int64_t v0 = vbase + (s - sbase) * 32 * (int64_t)Bp + 4 * lane;
+    const int64_t v0 = voff[s] + 4 * lane;
     for (int j = 0; j < (Bp >> 2); ++j) {
       const int4 o = __ldg(reinterpret_cast<const int4*>(soff + offbase) + j);
       const int64_t e = v0 + (int64_t)j * 128;
@@ -584,8 +585,9 @@ static constexpr int kPrefetch = FG_SPMV_PREFETCH;  // value groups (of 4 entrie
 static constexpr int kUnroll = FG_SPMV_UNROLL;      // value groups per unrolled step
 template <typename T, int MODE>
 __global__ void __launch_bounds__(RB)
-    k_stencil_spmv(int64_t nslices, const uint8_t* __restrict__ scls, const StencilClass* __restrict__ cls,
-                   const int32_t* __restrict__ soff, const int32_t* __restrict__ st_row, const T* __restrict__ tval,
+    k_stencil_spmv(int64_t nslices, const uint8_t* __restrict__ scls, const int64_t* __restrict__ voff,
+                   const StencilClass* __restrict__ cls, const int32_t* __restrict__ soff,
+                   const int32_t* __restrict__ st_row, const T* __restrict__ tval,
                    int ncomp, const T* __restrict__ x, T* __restrict__ y, const double* __restrict__ b, RedBuf rb,
                    double* S, const int* I) {
   if ((MODE == 1 || MODE == 3) && I[I_DONE]) return;
@@ -600,15 +602,17 @@ __global__ void __launch_bounds__(RB)
 #endif
   for (int64_t s = warp; s < nslices; s += nwarps) {
     const int k = scls[s];
-    const int64_t sbase = cls[k].sbase, nrows = cls[k].nrows, vbase = cls[k].vbase;
+    const int64_t vb = voff[s];
     const int Bp = cls[k].Bp, offbase = cls[k].offbase;
-    const int64_t rowid = (s - sbase) * 32 + lane;
     // st = node index in the class sub-lattice * ncomp + component; the row's own entry is
-    // in the class's sub-lattice, its box columns are base + table offsets
-    const int32_t st = st_row[s * 32 + lane];
+    // in the class's sub-lattice, its box columns are base + table offsets.  Padding lanes
+    // hold the complement of the slice's first row (valid addresses, values 0, no store).
+    int32_t st = st_row[s * 32 + lane];
+    const bool valid = st >= 0;
+    if (!valid) st = ~st;
     const int32_t base = ncomp == 1 ? st : st - st % ncomp;
     const int64_t vec = st + cls[k].ownoff;
-    const T* vp = tval + vbase + (s - sbase) * 32 * (int64_t)Bp + 4 * lane;
+    const T* vp = tval + vb + 4 * lane;
     const int4* op = reinterpret_cast<const int4*>(soff + offbase);
     const T* xb = x + base;
     T acc = 0;
@@ -629,7 +633,7 @@ __global__ void __launch_bounds__(RB)
       acc = fmaT(v[3], x3, acc);
       vp += 128;
     }
-    if (rowid < nrows) {
+    if (valid) {
       if (MODE == 2) {
         const T rr = (T)(b[vec] - (double)acc);
         y[vec] = rr;
@@ -792,7 +796,7 @@ static void spmv_k(fg_system* sys, const Work& w, const T* x, T* y, const double
     fg_space* sp = sys->space;                                                                                      \
     if (sp->layout == FG_LAYOUT_STENCIL)                                                                            \
       launch_k(k_stencil_spmv<T, MODE>, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls,                       \
-               (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row,       \
+               (const int64_t*)sp->d_st_voff, (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row,       \
                (const T*)sys->TVALS, sp->ncomp, x, y, b, w.rb, w.S, (const int*)w.I);                               \
     else                                                                                                            \
       launch_k(k_sell_spmv<T, MODE>, w, st, sp->nslices, sp->nfree, (const int64_t*)sp->d_sptr,                     \
@@ -812,7 +816,7 @@ static void spmv_fused32(fg_system* sys, const Work& w, const float* vals, const
   fg_space* sp = sys->space;
   if (sp->layout == FG_LAYOUT_STENCIL)
     launch_k(k_stencil_spmv<float, 3>, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls,
-             (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row, vals,
+             (const int64_t*)sp->d_st_voff, (const StencilClass*)sp->d_st_cls, (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row, vals,
              sp->ncomp, x, y, (const double*)nullptr, w.rb, w.S, (const int*)w.I);
   else
     launch_k(k_sell_spmv<float, 3>, w, st, sp->nslices, sp->nfree, (const int64_t*)sp->d_sptr,
@@ -835,7 +839,8 @@ static fg_status ensure_scaled(fg_system* sys, const Work& w) {
   cudaStream_t st = ctx->stream;
   launch_k(k_sqrt_idiag, w, st, nv, (const double*)sys->d_idiag, sys->d_sdiag);
   if (stencil)
-    launch_k(k_scale_stencil32, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls, (const StencilClass*)sp->d_st_cls,
+    launch_k(k_scale_stencil32, w, st, sp->st_nslices, (const uint8_t*)sp->d_st_scls, (const int64_t*)sp->d_st_voff,
+             (const StencilClass*)sp->d_st_cls,
              (const int32_t*)sp->d_st_off, (const int32_t*)sp->d_st_row, v64, (const double*)sys->d_sdiag, sp->ncomp,
              sys->d_val32s);
   else

@@ -15,11 +15,19 @@
 // halo and padding nodes stay zero.  Box positions outside the domain or on Dirichlet
 // nodes hold value 0.  For Q2 Poisson at 128^3 the FP32 matrix is 4 B per stored entry
 // instead of 8 B with explicit int32 columns.
+#include <algorithm>
+
 #include <cub/cub.cuh>
 
 #include "fg_internal.h"
 
 namespace fg {
+
+// Slices are stored in runs of FG_STENCIL_RUN consecutive slices of one class, the runs of
+// all classes in the order of their position in the domain (0: class by class).
+#ifndef FG_STENCIL_RUN
+#define FG_STENCIL_RUN 0
+#endif
 
 static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -38,8 +46,8 @@ __global__ void k_class_keys(int64_t nslots, int ncomp, int p, int Ln0, int Ln1,
 
 __global__ void k_stencil_rows(int64_t nfree, int ncomp, int p, const int Ln[3], int halo, const int Pn[3],
                                const uint8_t* skeys, const int32_t* svals, const int64_t* cls_start,
-                               const StencilClass* cls, const int32_t* latdof, int32_t* st_row, int32_t* row2st,
-                               int32_t* row2vec, int32_t* slot2row) {
+                               const StencilClass* cls, const int32_t* latdof, const int32_t* slice_perm,
+                               int32_t* st_row, int32_t* row2st, int32_t* row2vec, int32_t* slot2row) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nfree) return;
   const int k = skeys[i];
@@ -51,7 +59,9 @@ __global__ void k_stencil_rows(int64_t nfree, int ncomp, int p, const int Ln[3],
   const int S0 = Pn[0] / p, S1 = Pn[1] / p;
   const int64_t sub = (int64_t)((I + halo) / p) + (int64_t)S0 * (((J + halo) / p) + (int64_t)S1 * ((K + halo) / p));
   const int64_t st = sub * ncomp + c;
-  const int64_t slot = (int64_t)cls[k].sbase * 32 + (i - cls_start[k]);
+  // the row's slot in class-by-class numbering, moved to its slice's stored position
+  const int64_t slot_c = (int64_t)cls[k].sbase * 32 + (i - cls_start[k]);
+  const int64_t slot = (int64_t)slice_perm[slot_c >> 5] * 32 + (slot_c & 31);
   const int32_t r = latdof[s] - 1;
   st_row[slot] = (int32_t)st;
   slot2row[slot] = r;
@@ -59,20 +69,20 @@ __global__ void k_stencil_rows(int64_t nfree, int ncomp, int p, const int Ln[3],
   row2vec[r] = (int32_t)(st + cls[k].ownoff);
 }
 
-// padding lanes of a class's last slice: point at the slice's first row (values are 0)
-__global__ void k_stencil_pad(int64_t nslices, const uint8_t* scls, const StencilClass* cls, int32_t* st_row) {
+// padding lanes of a class's last slice (no row): the bitwise complement of the slice's first
+// row, so a kernel reads a valid address there (values are 0) and knows not to store
+__global__ void k_stencil_pad(int64_t nslices, const int32_t* slot2row, int32_t* st_row) {
   int64_t sl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (sl >= nslices) return;
-  const StencilClass& C = cls[scls[sl]];
-  const int64_t first_row = (sl - C.sbase) * 32;
-  for (int l = 0; l < 32; ++l)
-    if (first_row + l >= C.nrows) st_row[sl * 32 + l] = st_row[sl * 32];
+  for (int l = 1; l < 32; ++l)
+    if (slot2row[sl * 32 + l] < 0) st_row[sl * 32 + l] = ~st_row[sl * 32];
 }
 
 // values: CSR (row order) -> stencil layout, FP64 and FP32 copies (arrays cleared before)
 __global__ void k_stencil_vals(int64_t nfree, int ncomp, int p, int Ln0, int Ln1, const int64_t* rowptr,
                                const int32_t* col, const double* val, const int32_t* free2lat, const int32_t* row2st,
-                               const uint8_t* scls, const StencilClass* cls, double* sval, float* sval32) {
+                               const uint8_t* scls, const StencilClass* cls, const int64_t* voff, double* sval,
+                               float* sval32) {
   const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= nfree) return;
@@ -80,7 +90,7 @@ __global__ void k_stencil_vals(int64_t nfree, int ncomp, int p, int Ln0, int Ln1
   const int64_t sl = slot >> 5;
   const int rl = slot & 31;
   const StencilClass& C = cls[scls[sl]];
-  const int64_t vb = C.vbase + (sl - C.sbase) * 32 * (int64_t)C.Bp + 4 * rl;
+  const int64_t vb = voff[sl] + 4 * rl;
   const int64_t L = free2lat[r] / ncomp;
   const int I = (int)(L % Ln0), J = (int)((L / Ln0) % Ln1), K = (int)(L / ((int64_t)Ln0 * Ln1));
   const int lox = I + C.lo[0], loy = J + C.lo[1], loz = K + C.lo[2];
@@ -186,14 +196,45 @@ fg_status space_build_stencil(fg_space* sp) {
   sp->st_nslices = nsl;
   sp->st_nvals = nv;
   sp->st_ncls = ncls;
+  // Stored slice order.  A class's slices run through its sub-lattice in lattice order, so
+  // slice j of class k lies near the fraction (j + 1/2)/nslices_k of the domain.  Class by
+  // class, the SpMV gathers all of x once per class (at 128^3 Q2 that re-reads the 71 MB x
+  // vector from DRAM ~7 times per launch); with runs of every class interleaved by position
+  // the gathered x stays in a moving band, and the sweep still reads one value stream.
+  int64_t run = FG_STENCIL_RUN;
+  if (const char* e = getenv("FG_STENCIL_RUN")) run = std::max<int64_t>(0, atoll(e));
   std::vector<uint8_t> hscls(nsl > 0 ? nsl : 1);
-  for (int k = 0; k < ncls; ++k)
-    for (int64_t s = 0; s < (cls[k].nrows + 31) / 32; ++s) hscls[cls[k].sbase + s] = (uint8_t)k;
+  std::vector<int64_t> hvoff(nsl > 0 ? nsl : 1, 0);
+  std::vector<int32_t> hperm(nsl > 0 ? nsl : 1, 0);  // class-by-class slice id -> stored id
+  {
+    struct Run { double key; int k; int64_t j0, len; };
+    std::vector<Run> runs;
+    for (int k = 0; k < ncls; ++k) {
+      const int64_t ns = (cls[k].nrows + 31) / 32;
+      const int64_t c = run > 0 ? run : std::max<int64_t>(ns, 1);
+      for (int64_t j = 0; j < ns; j += c) {
+        const int64_t len = std::min(c, ns - j);
+        runs.push_back({run > 0 ? (j + 0.5 * len) / (double)ns : (double)k, k, j, len});
+      }
+    }
+    std::stable_sort(runs.begin(), runs.end(), [](const Run& a, const Run& b) { return a.key < b.key; });
+    int64_t t = 0, v = 0;
+    for (const Run& ru : runs)
+      for (int64_t q = 0; q < ru.len; ++q, ++t) {
+        hperm[cls[ru.k].sbase + ru.j0 + q] = (int32_t)t;
+        hscls[t] = (uint8_t)ru.k;
+        hvoff[t] = v;
+        v += 32 * (int64_t)cls[ru.k].Bp;
+      }
+  }
+  int32_t* d_perm = nullptr;
   int64_t* d_cstart = nullptr;
   int* d_dims = nullptr;
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_cls, sizeof(StencilClass) * ncls));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_off, sizeof(int32_t) * offs.size()));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_scls, hscls.size()));
+  FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_voff, sizeof(int64_t) * hvoff.size()));
+  FG_TRY(dev_alloc(ctx, (void**)&d_perm, sizeof(int32_t) * hperm.size()));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_row, sizeof(int32_t) * (nsl > 0 ? nsl * 32 : 1)));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_row2st, sizeof(int32_t) * (sp->nfree > 0 ? sp->nfree : 1)));
   FG_TRY(dev_alloc(ctx, (void**)&sp->d_st_slot2row, sizeof(int32_t) * (nsl > 0 ? nsl * 32 : 1)));
@@ -205,15 +246,18 @@ fg_status space_build_stencil(fg_space* sp) {
   FG_CUDA_TRY(cudaMemcpyAsync(sp->d_st_cls, cls.data(), sizeof(StencilClass) * ncls, cudaMemcpyHostToDevice, ctx->stream));
   FG_CUDA_TRY(cudaMemcpyAsync(sp->d_st_off, offs.data(), sizeof(int32_t) * offs.size(), cudaMemcpyHostToDevice, ctx->stream));
   FG_CUDA_TRY(cudaMemcpyAsync(sp->d_st_scls, hscls.data(), hscls.size(), cudaMemcpyHostToDevice, ctx->stream));
+  FG_CUDA_TRY(cudaMemcpyAsync(sp->d_st_voff, hvoff.data(), sizeof(int64_t) * hvoff.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+  FG_CUDA_TRY(cudaMemcpyAsync(d_perm, hperm.data(), sizeof(int32_t) * hperm.size(), cudaMemcpyHostToDevice, ctx->stream));
   FG_CUDA_TRY(cudaMemcpyAsync(d_cstart, cstart.data(), sizeof(int64_t) * (ncls + 1), cudaMemcpyHostToDevice, ctx->stream));
   FG_CUDA_TRY(cudaMemcpyAsync(d_dims, hdims, sizeof(hdims), cudaMemcpyHostToDevice, ctx->stream));
   if (sp->nfree > 0) {
     k_stencil_rows<<<nblk(sp->nfree, 256), 256, 0, ctx->stream>>>(sp->nfree, ncomp, p, d_dims, p, d_dims + 3, skeys,
-                                                                   svals, d_cstart, sp->d_st_cls, sp->d_latdof,
+                                                                   svals, d_cstart, sp->d_st_cls, sp->d_latdof, d_perm,
                                                                    sp->d_st_row, sp->d_row2st, sp->d_row2vec,
                                                                    sp->d_st_slot2row);
     FG_CUDA_TRY(cudaGetLastError());
-    k_stencil_pad<<<nblk(nsl, 256), 256, 0, ctx->stream>>>(nsl, sp->d_st_scls, sp->d_st_cls, sp->d_st_row);
+    k_stencil_pad<<<nblk(nsl, 256), 256, 0, ctx->stream>>>(nsl, sp->d_st_slot2row, sp->d_st_row);
     FG_CUDA_TRY(cudaGetLastError());
     ctx->launches += 2;
   }
@@ -229,6 +273,7 @@ fg_status space_build_stencil(fg_space* sp) {
   dev_free(ctx, tmp);
   dev_free(ctx, d_cstart);
   dev_free(ctx, d_dims);
+  dev_free(ctx, d_perm);
   return FG_OK;
 }
 
@@ -240,7 +285,7 @@ fg_status system_fill_stencil(fg_system* sys) {
   FG_CUDA_TRY(cudaMemsetAsync(sys->d_tval32, 0, sizeof(float) * sp->st_nvals, ctx->stream));
   k_stencil_vals<<<nblk(sp->nfree * 32, 256), 256, 0, ctx->stream>>>(
       sp->nfree, sp->ncomp, sp->order, sp->Ln[0], sp->Ln[1], sp->d_rowptr, sp->d_col, sys->d_val, sp->d_free2lat,
-      sp->d_row2st, sp->d_st_scls, sp->d_st_cls, sys->d_tval, sys->d_tval32);
+      sp->d_row2st, sp->d_st_scls, sp->d_st_cls, sp->d_st_voff, sys->d_tval, sys->d_tval32);
   FG_CUDA_TRY(cudaGetLastError());
   ctx->launches += 1;
   return FG_OK;
@@ -249,7 +294,8 @@ fg_status system_fill_stencil(fg_system* sys) {
 // CSR values from the lattice-implicit FP64 values (the inverse of k_stencil_vals)
 __global__ void k_stencil_to_csr(int64_t nfree, int ncomp, int Ln0, int Ln1, const int64_t* rowptr,
                                  const int32_t* col, const double* sval, const int32_t* free2lat,
-                                 const int32_t* row2st, const uint8_t* scls, const StencilClass* cls, double* val) {
+                                 const int32_t* row2st, const uint8_t* scls, const StencilClass* cls,
+                                 const int64_t* voff, double* val) {
   const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= nfree) return;
@@ -257,7 +303,7 @@ __global__ void k_stencil_to_csr(int64_t nfree, int ncomp, int Ln0, int Ln1, con
   const int64_t sl = slot >> 5;
   const int rl = slot & 31;
   const StencilClass& C = cls[scls[sl]];
-  const int64_t vb = C.vbase + (sl - C.sbase) * 32 * (int64_t)C.Bp + 4 * rl;
+  const int64_t vb = voff[sl] + 4 * rl;
   const int64_t L = free2lat[r] / ncomp;
   const int I = (int)(L % Ln0), J = (int)((L / Ln0) % Ln1), K = (int)(L / ((int64_t)Ln0 * Ln1));
   const int lox = I + C.lo[0], loy = J + C.lo[1], loz = K + C.lo[2];
@@ -285,7 +331,7 @@ fg_status system_ensure_csr(fg_system* sys) {
   if (sp->nfree > 0) {
     k_stencil_to_csr<<<nblk(sp->nfree * 32, 256), 256, 0, ctx->stream>>>(
         sp->nfree, sp->ncomp, sp->Ln[0], sp->Ln[1], sp->d_rowptr, sp->d_col, sys->d_tval, sp->d_free2lat,
-        sp->d_row2st, sp->d_st_scls, sp->d_st_cls, sys->d_val);
+        sp->d_row2st, sp->d_st_scls, sp->d_st_cls, sp->d_st_voff, sys->d_val);
     FG_CUDA_TRY(cudaGetLastError());
     ctx->launches += 1;
   }
@@ -297,7 +343,7 @@ fg_status system_ensure_csr(fg_system* sys) {
 // itself, component = the row's); entries of non-free vector slots stay 0
 __global__ void k_inv_diag_stencil(int64_t nfree, int ncomp, const int32_t* free2lat, const int32_t* row2st,
                                    const int32_t* row2vec, const uint8_t* scls, const StencilClass* cls,
-                                   const double* sval, double* d64, float* d32) {
+                                   const int64_t* voff, const double* sval, double* d64, float* d32) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= nfree) return;
   const int32_t slot = row2st[r];
@@ -306,7 +352,7 @@ __global__ void k_inv_diag_stencil(int64_t nfree, int ncomp, const int32_t* free
   const StencilClass& C = cls[scls[sl]];
   const int c = free2lat[r] % ncomp;
   const int pos = c + ncomp * (-C.lo[0] + C.w[0] * (-C.lo[1] + C.w[1] * (-C.lo[2])));
-  const double d = sval[C.vbase + (sl - C.sbase) * 32 * (int64_t)C.Bp + 4 * rl + (int64_t)(pos >> 2) * 128 + (pos & 3)];
+  const double d = sval[voff[sl] + 4 * rl + (int64_t)(pos >> 2) * 128 + (pos & 3)];
   const double inv = 1.0 / d;
   d64[row2vec[r]] = inv;
   d32[row2vec[r]] = (float)inv;
@@ -318,7 +364,8 @@ fg_status system_inv_diag_stencil(fg_system* sys) {
   if (sp->nfree == 0) return FG_OK;
   k_inv_diag_stencil<<<nblk(sp->nfree, 256), 256, 0, ctx->stream>>>(sp->nfree, sp->ncomp, sp->d_free2lat, sp->d_row2st,
                                                                     sp->d_row2vec, sp->d_st_scls, sp->d_st_cls,
-                                                                    sys->d_tval, sys->d_idiag, sys->d_idiag32);
+                                                                    sp->d_st_voff, sys->d_tval, sys->d_idiag,
+                                                                    sys->d_idiag32);
   FG_CUDA_TRY(cudaGetLastError());
   ctx->launches += 1;
   return FG_OK;
