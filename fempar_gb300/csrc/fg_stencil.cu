@@ -23,12 +23,6 @@
 
 namespace fg {
 
-// Slices are stored in runs of FG_STENCIL_RUN consecutive slices of one class, the runs of
-// all classes in the order of their position in the domain (0: class by class).
-#ifndef FG_STENCIL_RUN
-#define FG_STENCIL_RUN 0
-#endif
-
 static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 __global__ void k_class_keys(int64_t nslots, int ncomp, int p, int Ln0, int Ln1, int ncls, const int32_t* latdof,
@@ -196,35 +190,22 @@ fg_status space_build_stencil(fg_space* sp) {
   sp->st_nslices = nsl;
   sp->st_nvals = nv;
   sp->st_ncls = ncls;
-  // Stored slice order.  A class's slices run through its sub-lattice in lattice order, so
-  // slice j of class k lies near the fraction (j + 1/2)/nslices_k of the domain.  Class by
-  // class, the SpMV gathers all of x once per class (at 128^3 Q2 that re-reads the 71 MB x
-  // vector from DRAM ~7 times per launch); with runs of every class interleaved by position
-  // the gathered x stays in a moving band, and the sweep still reads one value stream.
-  int64_t run = FG_STENCIL_RUN;
-  if (const char* e = getenv("FG_STENCIL_RUN")) run = std::max<int64_t>(0, atoll(e));
+  // Slices are stored class by class (a class's slices in lattice order).  The SpMV's warps
+  // take slices at a stride of the warp count, so neighbouring warps work on neighbouring rows
+  // of one class and share the x entries they gather in L1/L2.  Interleaving the classes by
+  // position (runs of 8-4096 slices) read fewer DRAM bytes (x once instead of ~once per
+  // class) but ran 7-17 % slower on GB300; the per-slice value offsets keep that choice here.
   std::vector<uint8_t> hscls(nsl > 0 ? nsl : 1);
   std::vector<int64_t> hvoff(nsl > 0 ? nsl : 1, 0);
   std::vector<int32_t> hperm(nsl > 0 ? nsl : 1, 0);  // class-by-class slice id -> stored id
   {
-    struct Run { double key; int k; int64_t j0, len; };
-    std::vector<Run> runs;
-    for (int k = 0; k < ncls; ++k) {
-      const int64_t ns = (cls[k].nrows + 31) / 32;
-      const int64_t c = run > 0 ? run : std::max<int64_t>(ns, 1);
-      for (int64_t j = 0; j < ns; j += c) {
-        const int64_t len = std::min(c, ns - j);
-        runs.push_back({run > 0 ? (j + 0.5 * len) / (double)ns : (double)k, k, j, len});
-      }
-    }
-    std::stable_sort(runs.begin(), runs.end(), [](const Run& a, const Run& b) { return a.key < b.key; });
     int64_t t = 0, v = 0;
-    for (const Run& ru : runs)
-      for (int64_t q = 0; q < ru.len; ++q, ++t) {
-        hperm[cls[ru.k].sbase + ru.j0 + q] = (int32_t)t;
-        hscls[t] = (uint8_t)ru.k;
+    for (int k = 0; k < ncls; ++k)
+      for (int64_t j = 0; j < (cls[k].nrows + 31) / 32; ++j, ++t) {
+        hperm[cls[k].sbase + j] = (int32_t)t;
+        hscls[t] = (uint8_t)k;
         hvoff[t] = v;
-        v += 32 * (int64_t)cls[ru.k].Bp;
+        v += 32 * (int64_t)cls[k].Bp;
       }
   }
   int32_t* d_perm = nullptr;
