@@ -179,6 +179,7 @@ class BatchInfo(C.Structure):
         ("predicted_balance", C.c_double),
         ("run_ms", C.c_double),
         ("autotune_ms", C.c_double),
+        ("team_share", C.c_double),
     ]
 
 

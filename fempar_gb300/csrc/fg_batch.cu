@@ -754,6 +754,8 @@ struct fg_batch {
   std::vector<double*> user_x;            // caller's output pointers
   std::vector<int64_t> nf, nx;            // source / output lengths
   int threads = 0, ctas = 0, max_team = 0, teams_gt1 = 0;
+  // team sizing: a problem gets ceil(work / (team_share * per-CTA share)) CTAs
+  double team_share = 0.5;
   double predicted_balance = 0.0, autotune_ms = 0.0, run_ms = 0.0;
   int64_t total_dofs = 0;
   fg::BatchProb* d_probs = nullptr;
@@ -810,7 +812,7 @@ static void batch_schedule(fg_batch* B, int G, std::vector<int>& job_ptr, std::v
   for (int i : order) {
     BatchProb& P = B->probs[i];
     const int64_t F3 = (int64_t)P.F * P.F * P.F;
-    int t = (int)std::ceil(w[i] / (0.5 * target));
+    int t = (int)std::ceil(w[i] / (B->team_share * target));
     t = std::max(1, std::min(t, G));
     t = (int)std::min<int64_t>(t, std::max<int64_t>(1, F3 / (4 * B->threads)));
     P.team = t;
@@ -1066,7 +1068,8 @@ fg_status fg_batch_create(fg_ctx* ctx, int32_t nprob, const fg_batch_problem* pr
     batch_free(B);
     return FG_ERR_CUDA;
   }
-  // block size: given, or the fastest of 128/256/512 on this batch (inputs must be valid);
+  // block size and team sizing: given block size (team sizing 0.5), or the fastest of
+  // 128/256/512 threads x team sizing 0.25/0.5/1/2 on this batch (inputs must be valid);
   // large batches are timed on a stratified sample of at most 256 problems
   if (threads == 0 && nprob > 256) {
     std::vector<int> order(nprob);
@@ -1085,6 +1088,7 @@ fg_status fg_batch_create(fg_ctx* ctx, int32_t nprob, const fg_batch_problem* pr
       return s;
     }
     threads = S->threads;
+    B->team_share = S->team_share;
     batch_free(S);
     B->autotune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
@@ -1097,19 +1101,28 @@ fg_status fg_batch_create(fg_ctx* ctx, int32_t nprob, const fg_batch_problem* pr
         if (e != cudaSuccess) break;
       }
     }
+    // block size x team sizing (how large a problem must be, in per-CTA shares of the
+    // batch's work, before it is split over a team of CTAs)
     float best = 0.f;
     int best_t = 256;
+    double best_share = 0.5;
     for (int t : {128, 256, 512}) {
-      s = batch_plan(B, t);
       if (s != FG_OK) break;
-      float ms = 0.f;
-      s = batch_time(B, &ms);
-      if (s != FG_OK) break;
-      if (best == 0.f || ms < best) {
-        best = ms;
-        best_t = t;
+      for (double share : {0.25, 0.5, 1.0, 2.0}) {
+        B->team_share = share;
+        s = batch_plan(B, t);
+        if (s != FG_OK) break;
+        float ms = 0.f;
+        s = batch_time(B, &ms);
+        if (s != FG_OK) break;
+        if (best == 0.f || ms < best) {
+          best = ms;
+          best_t = t;
+          best_share = share;
+        }
       }
     }
+    B->team_share = best_share;
     B->autotune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     threads = best_t;
     if (s != FG_OK) {
@@ -1209,6 +1222,7 @@ fg_status fg_batch_get_info(fg_batch* B, fg_batch_info* info) {
   info->predicted_balance = B->predicted_balance;
   info->run_ms = B->run_ms;
   info->autotune_ms = B->autotune_ms;
+  info->team_share = B->team_share;
   return FG_OK;
 }
 

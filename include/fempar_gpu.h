@@ -466,6 +466,8 @@ typedef struct {
   double predicted_balance;  /* planner's estimate: mean CTA load / the longest            */
   double run_ms;             /* last fg_batch_run (device events, copies included)         */
   double autotune_ms;
+  double team_share;         /* team sizing chosen (with threads) by the autotuner: a problem
+                                gets ceil(work / (team_share x a CTA's share)) CTAs         */
 } fg_batch_info;
 /* flags: FG_INPUTS_ON_DEVICE = qp_source and x are device pointers (read / written in place
  * at every run); otherwise host pointers, copied in and out by every run.  params: rtol,
