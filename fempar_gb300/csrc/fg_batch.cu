@@ -755,6 +755,7 @@ struct fg_batch {
   std::vector<int64_t> nf, nx;            // source / output lengths
   int threads = 0, ctas = 0, max_team = 0, teams_gt1 = 0;
   // team sizing: a problem gets ceil(work / (team_share * per-CTA share)) CTAs
+  // (0.5, or FG_BATCH_TEAM_SHARE when set > 0)
   double team_share = 0.5;
   double predicted_balance = 0.0, autotune_ms = 0.0, run_ms = 0.0;
   int64_t total_dofs = 0;
@@ -981,6 +982,8 @@ fg_status fg_batch_create(fg_ctx* ctx, int32_t nprob, const fg_batch_problem* pr
   FG_CUDA_TRY(cudaSetDevice(ctx->device));
   fg_batch* B = new fg_batch();
   B->ctx = ctx;
+  if (const char* env = std::getenv("FG_BATCH_TEAM_SHARE"))
+    if (std::atof(env) > 0.0) B->team_share = std::atof(env);
   B->nprob = nprob;
   B->flags = flags;
   B->prm = *params;
@@ -1068,9 +1071,10 @@ fg_status fg_batch_create(fg_ctx* ctx, int32_t nprob, const fg_batch_problem* pr
     batch_free(B);
     return FG_ERR_CUDA;
   }
-  // block size and team sizing: given block size (team sizing 0.5), or the fastest of
-  // 128/256/512 threads x team sizing 0.25/0.5/1/2 on this batch (inputs must be valid);
-  // large batches are timed on a stratified sample of at most 256 problems
+  // block size: given, or the fastest of 128/256/512 on this batch (inputs must be valid);
+  // large batches are timed on a stratified sample of at most 256 problems.  Team sizing is
+  // not timed (a sample run with the full plan's team sizes lasts as long as its largest
+  // problem, about half a full run): 0.5, or FG_BATCH_TEAM_SHARE
   if (threads == 0 && nprob > 256) {
     std::vector<int> order(nprob);
     std::iota(order.begin(), order.end(), 0);
@@ -1088,7 +1092,6 @@ fg_status fg_batch_create(fg_ctx* ctx, int32_t nprob, const fg_batch_problem* pr
       return s;
     }
     threads = S->threads;
-    B->team_share = S->team_share;
     batch_free(S);
     B->autotune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
@@ -1101,28 +1104,19 @@ fg_status fg_batch_create(fg_ctx* ctx, int32_t nprob, const fg_batch_problem* pr
         if (e != cudaSuccess) break;
       }
     }
-    // block size x team sizing (how large a problem must be, in per-CTA shares of the
-    // batch's work, before it is split over a team of CTAs)
     float best = 0.f;
     int best_t = 256;
-    double best_share = 0.5;
     for (int t : {128, 256, 512}) {
+      s = batch_plan(B, t);
       if (s != FG_OK) break;
-      for (double share : {0.25, 0.5, 1.0, 2.0}) {
-        B->team_share = share;
-        s = batch_plan(B, t);
-        if (s != FG_OK) break;
-        float ms = 0.f;
-        s = batch_time(B, &ms);
-        if (s != FG_OK) break;
-        if (best == 0.f || ms < best) {
-          best = ms;
-          best_t = t;
-          best_share = share;
-        }
+      float ms = 0.f;
+      s = batch_time(B, &ms);
+      if (s != FG_OK) break;
+      if (best == 0.f || ms < best) {
+        best = ms;
+        best_t = t;
       }
     }
-    B->team_share = best_share;
     B->autotune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     threads = best_t;
     if (s != FG_OK) {

@@ -131,16 +131,19 @@ def test_batch_reports_non_convergence_and_bad_input(fg, ctx):
         BatchSolver(ctx, bad)
 
 
-def test_batch_autotune_picks_a_block_size_and_team_sizing(fg, ctx):
+def test_batch_autotune_picks_a_block_size(fg, ctx, monkeypatch):
     from fempar_gb300.batch import BatchSolver
     probs = small_set(seed=11)
     B = BatchSolver(ctx, probs, rtol=1e-8, threads=0)
     info = B.info()
-    assert info["threads"] in (128, 256, 512) and info["autotune_ms"] > 0
-    assert info["team_share"] in (0.25, 0.5, 1.0, 2.0)
-    assert BatchSolver(ctx, probs, rtol=1e-8, threads=256).info()["team_share"] == 0.5
+    assert info["threads"] in (128, 256, 512) and info["autotune_ms"] > 0 and info["team_share"] == 0.5
     res = B.run()
     assert all(r["status"] == 0 for r in res)
+    # team sizing from the environment: more and larger teams at 0.25, same convergence
+    monkeypatch.setenv("FG_BATCH_TEAM_SHARE", "0.25")
+    B2 = BatchSolver(ctx, probs, rtol=1e-8, threads=256)
+    assert B2.info()["team_share"] == 0.25
+    assert all(r["status"] == 0 for r in B2.run())
 
 
 def test_batch_bounded_team_wait_runs_out_and_context_survives(fg, ctx, monkeypatch):
