@@ -23,6 +23,7 @@ FG_PREC_NONE, FG_PREC_JACOBI, FG_PREC_BDDC = 0, 1, 2
 FG_BDDC_WEIGHT_MULTIPLICITY, FG_BDDC_WEIGHT_STIFFNESS = 0, 1
 FG_BDDC_HANDLER_STANDARD, FG_BDDC_HANDLER_ELASTICITY = 0, 1
 FG_FP64, FG_MIXED = 0, 1
+FG_DENSE_LOWER = 1
 FG_RES_RES, FG_RES_RHS, FG_DELTA_RHS, FG_DELTA_DELTA, FG_RES_NRMGIVEN_RHS_NRMGIVEN, FG_RES_NRMGIVEN_RES_NRMGIVEN = range(6)
 
 # every symbol include/fempar_gpu.h declares
@@ -44,7 +45,7 @@ EXPORTS = [
     "fg_partition_create", "fg_partition_destroy", "fg_partition_get_info", "fg_partition_get_dof_import_sizes",
     "fg_partition_get_dof_import", "fg_partition_assemble", "fg_partition_comm_device", "fg_partition_solve",
     "fg_request_footprint", "fg_server_create", "fg_server_submit", "fg_server_wait", "fg_server_take_solution",
-    "fg_server_stats", "fg_server_destroy",
+    "fg_server_stats", "fg_server_destroy", "fg_dense_gemm_nt",
 ]
 
 
@@ -278,6 +279,8 @@ def lib():
         "fg_system_export_rhs": (i32, [vp, vp]),
         "fg_system_export_dirichlet_values": (i32, [vp, vp]),
         "fg_system_spmv_device": (i32, [vp, i32, vp, vp]),
+        "fg_dense_gemm_nt": (i32, [vp, C.c_int64, C.c_int64, C.c_int64, C.c_double, vp, C.c_int64, C.c_int64, vp,
+                                   C.c_int64, C.c_int64, C.c_double, vp, C.c_int64, C.c_int64, i32]),
         "fg_system_spmv_solver_layout_device": (i32, [vp, i32, vp, vp, i32]),
         "fg_system_spmv_device_noalloc": (i32, [vp, i32, vp, vp]),
         "fg_solve": (i32, [vp, C.POINTER(SolverParams), vp, vp, vp, C.POINTER(SolveInfo)]),

@@ -103,6 +103,7 @@ struct fg_bddc {
   int32_t* dBox = nullptr;
   int32_t* dOrder = nullptr;  // subdomains by decreasing factorisation work
   bool stepped = false;        // factorise panel step by panel step over all subdomains
+  bool coarse_emulated = false; // coarse trailing updates on the tensor cores (last setup)
   int64_t* dIptr = nullptr;
   int64_t* dIsrc = nullptr;
   int32_t* dIvec = nullptr;
@@ -198,8 +199,10 @@ __device__ __forceinline__ void chol_trsm_row(double* A, int64_t lda, int j0, in
 }
 
 // Trailing tile (ti, tj) of 64 x 64 at rows/cols starting t0: A[r, c] -= sum_k A[r, j0+k] A[c, j0+k]
-// for r >= c, r, c < N.
-__device__ void chol_syrk_tile(double* A, int64_t lda, int N, int j0, int nb, int t0, int ti, int tj, CholSmem& sm) {
+// for r >= c, r < N, c < cN (cN < 0: N).
+__device__ void chol_syrk_tile(double* A, int64_t lda, int N, int j0, int nb, int t0, int ti, int tj, CholSmem& sm,
+                               int cN = -1) {
+  const int cn = cN < 0 ? N : cN;
   const int tid = threadIdx.x;
   const int r0 = t0 + ti * 64, q0 = t0 + tj * 64;
   for (int t = tid; t < 32 * 64; t += blockDim.x) {
@@ -231,7 +234,7 @@ __device__ void chol_syrk_tile(double* A, int64_t lda, int N, int j0, int nb, in
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int r = r0 + tr + 16 * u;
-      if (r < N && c < N && r >= c) A[r + (int64_t)c * lda] -= acc[u][v];
+      if (r < N && c < cn && r >= c) A[r + (int64_t)c * lda] -= acc[u][v];
     }
   }
   __syncthreads();
@@ -533,6 +536,15 @@ __global__ void __launch_bounds__(256) k_chol_syrk1(double* A, int64_t lda, int 
   int tj = (int)(b - (int64_t)ti * (ti + 1) / 2);
   if (ti >= nt) return;
   chol_syrk_tile(A, lda, N, j0, nb, j0 + nb, ti, tj, sm);
+}
+
+// The same update restricted to the columns [j0 + nb, cN) of a wider panel: tiles (ti, tj) =
+// blockIdx (x, y), ti >= tj.
+__global__ void __launch_bounds__(256) k_chol_syrk_panel(double* A, int64_t lda, int N, int j0, int nb, int cN) {
+  __shared__ CholSmem sm;
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (ti < tj) return;
+  chol_syrk_tile(A, lda, N, j0, nb, j0 + nb, ti, tj, sm, cN);
 }
 
 __global__ void k_coarse_extract(int64_t nC, const double* __restrict__ Kc, double* __restrict__ Kinv,
@@ -1457,20 +1469,51 @@ static fg_status check_err(fg_bddc* B, const char* what) {
 // it, as in [[K, I], [I, 0]]): such a row's panel entries stay zero until the panel reaches
 // column i, so at panel j0 the rows from zrow + j0 + nb on are skipped by the solve and the
 // trailing update (exactly: their contributions are zero).  zrow = N: no unit block.
-static fg_status chol_partial_grid(fg_ctx* ctx, double* A, int64_t lda, int N, int ncols, int zrow, int* err) {
+// With work (ozaki_workspace_bytes(N, N, 128, true) bytes + an int), the factorisation is
+// blocked by 128 columns: each 128-column panel is factored by 32-column steps whose
+// updates stay inside the panel, and the trailing matrix gets one rank-128 update on the
+// tensor cores (FP64 emulated by digit slicing, fg_ozaki.cu) instead of four rank-32
+// updates on the FP64 pipe.
+static fg_status chol_partial_grid(fg_ctx* ctx, double* A, int64_t lda, int N, int ncols, int zrow, int* err,
+                                   void* work = nullptr) {
   cudaStream_t st = ctx->stream;
-  for (int j0 = 0; j0 < ncols; j0 += 32) {
-    const int nb = std::min(32, ncols - j0);
-    k_chol_diag1<<<1, 32, 0, st>>>(A, lda, j0, nb, err);
-    const int Neff = (int)std::min<int64_t>(N, (int64_t)zrow + j0 + nb);
-    const int rows = Neff - j0 - nb;
-    if (rows > 0) {
-      k_chol_trsm1<<<nblk(rows, 256), 256, 0, st>>>(A, lda, Neff, j0, nb);
-      const int nt = (rows + 63) / 64;
-      k_chol_syrk1<<<(unsigned)((int64_t)nt * (nt + 1) / 2), 256, 0, st>>>(A, lda, Neff, j0, nb, nt);
-      ctx->launches += 2;
+  const int NB = work ? 128 : ncols;
+  for (int J0 = 0; J0 < ncols; J0 += NB) {
+    const int J1 = std::min(J0 + NB, ncols);
+    for (int j0 = J0; j0 < J1; j0 += 32) {
+      const int nb = std::min(32, J1 - j0);
+      k_chol_diag1<<<1, 32, 0, st>>>(A, lda, j0, nb, err);
+      const int Neff = (int)std::min<int64_t>(N, (int64_t)zrow + j0 + nb);
+      const int rows = Neff - j0 - nb;
+      if (rows > 0) {
+        k_chol_trsm1<<<nblk(rows, 256), 256, 0, st>>>(A, lda, Neff, j0, nb);
+        const int nt = (rows + 63) / 64;
+        if (work) {
+          const int ntc = (J1 - (j0 + nb) + 63) / 64;  // columns left inside the panel
+          if (ntc > 0) {
+            k_chol_syrk_panel<<<dim3((unsigned)nt, (unsigned)ntc), 256, 0, st>>>(A, lda, Neff, j0, nb, J1);
+            ctx->launches += 1;
+          }
+        } else {
+          k_chol_syrk1<<<(unsigned)((int64_t)nt * (nt + 1) / 2), 256, 0, st>>>(A, lda, Neff, j0, nb, nt);
+          ctx->launches += 1;
+        }
+        ctx->launches += 1;
+      }
+      ctx->launches += 1;
     }
-    ctx->launches += 1;
+    if (work) {
+      // A[J1:Ne, J1:Ne] -= P P^T (lower), P = A[J1:Ne, J0:J1]
+      const int Ne = (int)std::min<int64_t>(N, (int64_t)zrow + J1);
+      const int rows = Ne - J1;
+      if (rows > 0) {
+        double* P = A + J1 + (int64_t)J0 * lda;
+        double* Ct = A + J1 + (int64_t)J1 * lda;
+        int* oz_err = (int*)((uint8_t*)work + ozaki_workspace_bytes(N, N, 128, true));
+        FG_TRY(ozaki_gemm_nt(ctx, st, rows, rows, J1 - J0, -1.0, P, 1, lda, nullptr, 0, 0, 1.0, Ct, 1, lda, true,
+                             work, oz_err));
+      }
+    }
   }
   FG_CUDA_TRY(cudaGetLastError());
   return FG_OK;
@@ -1532,7 +1575,29 @@ static fg_status bddc_numeric(fg_bddc* B) {
     k_seg_sum<<<nblk(B->nKpair, 256), 256, 0, st>>>(B->nKpair, B->dKptr, B->dKsrc, B->dKdst, B->dKp, B->dKc);
     k_coarse_identity<<<nblk(nC, 256), 256, 0, st>>>(nC, B->dKc);
     ctx->launches += 2;
-    FG_TRY(chol_partial_grid(ctx, B->dKc, 2 * nC, (int)(2 * nC), (int)nC, (int)nC, B->dErr));
+    // coarse matrices of 1024 dofs and more: trailing updates on the tensor cores (FP64
+    // emulated), unless FG_BDDC_EMULATED_FP64=0
+    void* work = nullptr;
+    const char* ee = std::getenv("FG_BDDC_EMULATED_FP64");
+    const size_t wbytes = ozaki_workspace_bytes(2 * nC, 2 * nC, 128, true);
+    if (nC >= 1024 && !(ee && ee[0] == '0')) {
+      FG_TRY(dev_alloc(ctx, &work, wbytes + sizeof(int)));
+      FG_CUDA_TRY(cudaMemsetAsync((uint8_t*)work + wbytes, 0, sizeof(int), st));
+    }
+    fg_status cs = chol_partial_grid(ctx, B->dKc, 2 * nC, (int)(2 * nC), (int)nC, (int)nC, B->dErr, work);
+    int oz_err = 0;
+    if (cs == FG_OK && work) {
+      cudaError_t ce = cudaMemcpyAsync(&oz_err, (uint8_t*)work + wbytes, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+      if (ce != cudaSuccess) cs = FG_ERR_CUDA;
+    }
+    B->coarse_emulated = work != nullptr;
+    if (work) dev_free(ctx, work);
+    FG_TRY(cs);
+    if (oz_err) {
+      set_error("BDDC: a bounded tensor-core wait ran out in the coarse factorisation");
+      return (fg_status)oz_err;
+    }
     FG_TRY(check_err(B, "the coarse matrix"));
     k_coarse_extract<<<nblk(nC * nC, 256), 256, 0, st>>>(nC, B->dKc, B->dKinv, B->dKinv32);
     ctx->launches += 1;

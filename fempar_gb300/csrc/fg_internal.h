@@ -275,4 +275,12 @@ fg_status system_spmv_layout_noalloc(fg_system* sys, int precision, const void* 
 fg_status system_solve(fg_system* sys, const fg_solver_params* prm, const double* d_b, const double* d_x0,
                        double* d_x, fg_solve_info* info);
 
+// Dense FP64 product on the bf16 tensor cores (fg_ozaki.cu): C = alpha A B^T + beta C,
+// B == nullptr means B = A; work holds ozaki_workspace_bytes(m, n, k, B == nullptr) bytes;
+// d_err receives FG_ERR_TIMEOUT if a bounded device wait ran out.
+size_t ozaki_workspace_bytes(int64_t m, int64_t n, int64_t k, bool same);
+fg_status ozaki_gemm_nt(fg_ctx* ctx, cudaStream_t st, int64_t m, int64_t n, int64_t k, double alpha,
+                        const double* A, int64_t a_rs, int64_t a_cs, const double* B, int64_t b_rs, int64_t b_cs,
+                        double beta, double* C, int64_t c_rs, int64_t c_cs, bool lower, void* work, int* d_err);
+
 }  // namespace fg

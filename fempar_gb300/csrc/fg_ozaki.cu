@@ -1,0 +1,584 @@
+// fg_ozaki.cu -- FP64 matrix products on the bf16 tensor cores (tcgen05) by digit slicing.
+//
+// GB300 runs FP64 at ~1 TFLOP/s (DFMA and the FP64 MMA alike) and bf16 MMAs at ~1.9
+// PFLOP/s.  The dense FP64 products of the BDDC set-up are moved onto the tensor cores with
+// the Ozaki scheme (K. Ozaki, T. Ogita, S. Oishi, S. M. Rump, "Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication and its
+// applications", Numer. Algorithms 59, 2012), in its fixed-point digit form (H. Ootomo,
+// K. Ozaki, R. Yokota, "DGEMM on integer matrix multiplication unit", IJHPCA 2024), with
+// bf16 digits instead of int8 ones because this part's int8 MMA rate is low:
+//
+//   * every row i of an operand gets a power of two 2^e_i with |x_il| 2^-e_i < 1/2 and is cut
+//     into S = 7 signed digits, x_il = 2^e_i sum_s d_s 2^(-8(s+1)) (+ a tail below
+//     2^(e_i-57)), |d_s| <= 128, so every digit is an exact bf16.  The cut is integer
+//     arithmetic on the FP64 bit pattern (56 fraction bits, digits rounded to nearest);
+//   * the digit matrices are multiplied by tcgen05.mma kind::f16 (bf16 x bf16 -> FP32).  A
+//     digit product is at most 2^14, and an accumulator sums at most 7 pairs over K <= 128:
+//     every FP32 partial sum is an integer below 2^24, i.e. exact;
+//   * the products of weight 2^(-8k), k = s + t = 0..6 (28 digit pairs), go to 7 FP32
+//     accumulators in tensor memory; pairs with s + t >= 7 are dropped (|error| <~ K 2^-51
+//     max_l |x_il| max_l |y_jl|, inside the FP64 dot-product bound);
+//   * the epilogue sums the 7 accumulators in float-float (error-free FP32 two-sums), adds the
+//     K chunks of 128 in float-float, and applies alpha 2^(e_i + f_j - 16) in FP64 once per
+//     output element (5 FP64 operations per element instead of K).
+//
+// Digit layout in HBM: per operand, blocks of 128 rows x 16 columns (one MMA K step) per
+// digit, 4 KB each, ordered [row tile][K step][digit]; inside a block the rows are in the
+// canonical K-major, non-swizzled UMMA layout: core matrices of 8 rows x 16 bytes, the two
+// 8-column halves 128 B apart (LBO), row groups 256 B apart (SBO).  An operand B tile of 64
+// rows is half a block (2 KB).  A CTA computes one 128 x 64 output tile: warp 0's lane 0
+// streams the digit blocks into shared memory with cp.async.bulk (5 stages, mbarrier
+// transaction counts) and issues the MMAs; warps 1-8 read the accumulators (tcgen05.ld, two
+// warps per TMEM lane quarter, 32 columns each) and write C.  CTAs are persistent (one per SM, tiles round robin):
+// the epilogue releases the accumulators before its FP64 writes, which then overlap the next
+// tile's MMAs, and the stages of the next tile are loaded meanwhile.  Every wait is bounded: after ~1 s the CTA records
+// FG_ERR_TIMEOUT, stops, frees its tensor memory and returns.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "fg_internal.h"
+
+namespace fg {
+
+namespace {
+
+constexpr int OZ_S = 7;                       // digits per value
+constexpr int OZ_NACC = 7;                    // accumulators: digit weights k = s + t = 0..6
+constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 16;
+constexpr int OZ_CHUNK = 8;                   // K steps per exact accumulation (K <= 128)
+constexpr int OZ_NBUF = 5;                    // shared-memory stages
+constexpr uint32_t OZ_BLOCK = OZ_BM * OZ_BK * 2;           // one digit block: 4096 B
+constexpr uint32_t OZ_A_BYTES = OZ_S * OZ_BLOCK;           // 28672 B per K step
+constexpr uint32_t OZ_B_BYTES = OZ_S * OZ_BLOCK / 2;       // 14336 B per K step
+constexpr uint32_t OZ_STAGE = OZ_A_BYTES + OZ_B_BYTES;     // 43008 B
+constexpr uint32_t OZ_SMEM = OZ_NBUF * OZ_STAGE;           // 215040 B: one CTA per SM
+constexpr uint32_t OZ_TMEM_COLS = 512;                     // 7 x 64 used
+constexpr long long OZ_WAIT_CYCLES = 1ll << 31;            // ~1 s at 2 GHz
+constexpr int OZ_EPI_COLS = 32;                            // columns per epilogue thread
+constexpr int OZ_THREADS = 32 + 4 * 32 * (OZ_BN / OZ_EPI_COLS);  // MMA warp + 8 epilogue warps
+
+// ---- PTX wrappers -------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+// global -> own shared memory, completion counted in bytes on the mbarrier
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// D[tmem] (+)= A[smem] * B[smem]^T, 128 x 64 x 16, bf16 -> FP32
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// arrive on the mbarrier once every tcgen05 operation issued so far by this thread is done
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr)
+               : "memory");
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major, no swizzle; LBO = 128 B (the two 8-column
+// halves of a 16-column step), SBO = 256 B (consecutive 8-row groups); version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(256u >> 4) << 32) |
+         (1ull << 46);
+}
+// Instruction descriptor, kind::f16: FP32 accumulator, bf16 A and B, both K-major, N = 64, M = 128.
+constexpr uint32_t OZ_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
+                              ((uint32_t)(OZ_BM >> 4) << 24);
+
+// bounded wait; false (and the CTA's abort flag and the error status set) when it runs out
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err) {
+  const long long t0 = clock64();
+  int spins = 0;
+  while (!mbar_try(a, parity)) {
+    if (*abort_flag) return false;
+    if (++spins > 64) __nanosleep(64);
+    if (clock64() - t0 > OZ_WAIT_CYCLES) {
+      *abort_flag = 1;
+      atomicExch(err, (int)FG_ERR_TIMEOUT);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+}  // namespace
+
+// Row exponents: e_r with max_l |x_rl| < 2^(e_r - 1), from the largest biased exponent of
+// the row (an all-zero row gets 0).  Thread per row.
+__global__ void k_oz_rowexp(int64_t rows, int64_t k, const double* __restrict__ x, int64_t rs, int64_t cs,
+                            int32_t* __restrict__ e) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  unsigned long long mx = 0;
+  for (int64_t l = 0; l < k; ++l) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x[r * rs + l * cs]) & 0x7FFFFFFFFFFFFFFFull;
+    mx = b > mx ? b : mx;
+  }
+  const int E = (int)(mx >> 52);            // biased exponent of the largest |x| (0: zero/subnormal)
+  e[r] = mx == 0 ? 0 : (E == 0 ? 1 : E) - 1021;
+}
+
+// Digits: block (row tile, K step), thread per row; 16 values, 7 digits each, written as the
+// 7 digit blocks' 32-byte rows.  Rows >= rows and columns >= k are zero.
+__global__ void __launch_bounds__(OZ_BM) k_oz_split(int64_t rows, int64_t k, const double* __restrict__ x,
+                                                    int64_t rs, int64_t cs, const int32_t* __restrict__ e,
+                                                    int ksteps, uint4* __restrict__ out) {
+  const int tid = threadIdx.x;
+  const int64_t r = (int64_t)blockIdx.x * OZ_BM + tid;
+  const int ks = blockIdx.y;
+  uint32_t w[OZ_S][8];
+  const int er = r < rows ? e[r] : 0;
+#pragma unroll
+  for (int c = 0; c < OZ_BK; c += 2) {
+    int32_t d[2][OZ_S];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t l = (int64_t)ks * OZ_BK + c + h;
+      const double v = (r < rows && l < k) ? x[r * rs + l * cs] : 0.0;
+      const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+      const int E = (int)((b >> 52) & 0x7FF);
+      const long long mant = (long long)(b & 0xFFFFFFFFFFFFFull) | (E ? (1ll << 52) : 0ll);
+      // F = |v| 2^(56 - e_r) as an integer: v = mant 2^(max(E,1) - 1075)
+      const int sh = (E ? E : 1) - 1019 - er;  // <= 2 by the choice of e_r
+      long long F = sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> -sh) : 0ll);
+      if (b >> 63) F = -F;
+#pragma unroll
+      for (int s = 0; s < OZ_S - 1; ++s) {
+        const int q = 48 - 8 * s;
+        const long long dg = (F + (1ll << (q - 1))) >> q;  // nearest digit, in [-128, 128]
+        F -= dg << q;
+        d[h][s] = (int32_t)dg;
+      }
+      d[h][OZ_S - 1] = (int32_t)F;  // |F| <= 128 after six digits
+    }
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) {
+      // small integers are exact in bf16: the upper half of their FP32 pattern
+      const uint32_t lo = __float_as_uint((float)d[0][s]) >> 16;
+      const uint32_t hi = __float_as_uint((float)d[1][s]) >> 16;
+      w[s][c / 2] = lo | (hi << 16);
+    }
+  }
+  const size_t blk = ((size_t)blockIdx.x * ksteps + ks) * OZ_S;
+  const int g = tid >> 3, r8 = tid & 7;
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s) {
+    uint4* p = out + (blk + s) * (OZ_BLOCK / 16);
+    p[g * 16 + r8] = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);      // columns 0-7
+    p[g * 16 + 8 + r8] = make_uint4(w[s][4], w[s][5], w[s][6], w[s][7]);  // columns 8-15
+  }
+}
+
+struct OzGemmArgs {
+  const uint8_t* a;      // digit blocks of A
+  const uint8_t* b;      // digit blocks of B
+  const int32_t* ea;     // row exponents of A
+  const int32_t* eb;     // row exponents of B
+  int m, n, ksteps;
+  int tiles_m, tiles_n;  // 128-row and 64-column tiles
+  double alpha, beta;
+  double* c;
+  int64_t c_rs, c_cs;
+  int lower;             // write only i >= j
+  int* err;
+};
+
+// 2^off (h + l) as two FP64 values, by exponent arithmetic (no FP64 operation).  h and l are
+// normal or zero (every partial sum is a multiple of 2^-48); false if the result would leave
+// the normal FP64 range.
+__device__ __forceinline__ bool ff_to_f64(float f, int off, double& d) {
+  const uint32_t u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
+  if (a == 0) {
+    d = 0.0;
+    return true;
+  }
+  const int e = (int)(a >> 23) + (1023 - 127) + off;
+  if (e < 1 || e > 2046) return false;
+  d = __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | ((unsigned long long)e << 52) |
+                                       ((unsigned long long)(a & 0x7FFFFFu) << 29)));
+  return true;
+}
+
+// out-of-range fallback of ff_to_f64 (kept out of line: it costs FP64 operations)
+__device__ __noinline__ void scale_slow(float h, float l, int off, double& xh, double& xl) {
+  xh = ldexp((double)h, off);
+  xl = ldexp((double)l, off);
+}
+
+// Persistent: CTA b takes the tiles b, b + gridDim.x, ... (upper tiles skipped when lower).
+// The accumulators are released as soon as the epilogue has read them, so the next tile's
+// MMAs run while the epilogue writes C.
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
+  extern __shared__ __align__(1024) uint8_t oz_smem[];
+  __shared__ __align__(8) uint64_t bar_full[OZ_NBUF], bar_empty[OZ_NBUF], bar_acc_full, bar_acc_empty;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = g.tiles_m * g.tiles_n;
+  auto valid = [&](int t) { return !g.lower || (t % g.tiles_n) * OZ_BN <= (t / g.tiles_n) * OZ_BM + OZ_BM - 1; };
+  auto next_tile = [&](int t) {
+    for (t += gridDim.x; t < ntiles && !valid(t); t += gridDim.x) {
+    }
+    return t;
+  };
+  const int first = valid(blockIdx.x) ? (int)blockIdx.x : next_tile(blockIdx.x);
+  if (first >= ntiles) return;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(OZ_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    if (lane == 0) {
+      for (int i = 0; i < OZ_NBUF; ++i) {
+        mbar_init(smem_u32(&bar_full[i]), 1);
+        mbar_init(smem_u32(&bar_empty[i]), 1);
+      }
+      mbar_init(smem_u32(&bar_acc_full), 1);
+      mbar_init(smem_u32(&bar_acc_empty), OZ_THREADS - 32);
+      abort_flag = 0;
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int KS = g.ksteps;
+  const int nchunks = (KS + OZ_CHUNK - 1) / OZ_CHUNK;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const uint32_t sbase = smem_u32(oz_smem);
+      // producer cursor: tile pt, K step pks, global stage counter pgs
+      int pt = first, pks = 0, pgs = 0;
+      auto produce = [&]() -> bool {
+        if (pt >= ntiles) return true;
+        const int buf = pgs % OZ_NBUF;
+        if (pgs >= OZ_NBUF && !mbar_wait(smem_u32(&bar_empty[buf]), ((pgs / OZ_NBUF) - 1) & 1, &abort_flag, g.err))
+          return false;
+        const int rt = pt / g.tiles_n, ct = pt % g.tiles_n;
+        const uint8_t* asrc = g.a + ((size_t)rt * KS + pks) * OZ_A_BYTES;
+        const uint8_t* bsrc = g.b + ((size_t)(ct >> 1) * KS + pks) * OZ_A_BYTES + (size_t)(ct & 1) * (OZ_BLOCK / 2);
+        const uint32_t full = smem_u32(&bar_full[buf]);
+        const uint32_t dst = sbase + buf * OZ_STAGE;
+        mbar_expect_tx(full, OZ_STAGE);
+        bulk_g2s(dst, asrc, OZ_A_BYTES, full);
+        for (int t = 0; t < OZ_S; ++t)
+          bulk_g2s(dst + OZ_A_BYTES + t * (OZ_BLOCK / 2), bsrc + (size_t)t * OZ_BLOCK, OZ_BLOCK / 2, full);
+        ++pgs;
+        if (++pks == KS) {
+          pks = 0;
+          pt = next_tile(pt);
+        }
+        return true;
+      };
+      bool ok = true;
+      for (int p = 0; p < OZ_NBUF - 1 && ok; ++p) ok = produce();
+      int gs = 0, gc = 0;
+      for (int t = first; t < ntiles && ok; t = next_tile(t)) {
+        for (int ks = 0; ks < KS && ok; ++ks) {
+          const int kin = ks % OZ_CHUNK;
+          const int buf = gs % OZ_NBUF;
+          if (kin == 0 && gc > 0 && !mbar_wait(smem_u32(&bar_acc_empty), (gc - 1) & 1, &abort_flag, g.err)) {
+            ok = false;
+            break;
+          }
+          if (!mbar_wait(smem_u32(&bar_full[buf]), (gs / OZ_NBUF) & 1, &abort_flag, g.err)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = sbase + buf * OZ_STAGE, sb = sa + OZ_A_BYTES;
+          const uint64_t da = smem_desc(sa), db = smem_desc(sb);
+#pragma unroll
+          for (int kk = 0; kk < OZ_NACC; ++kk)
+#pragma unroll
+            for (int s = 0; s <= kk; ++s)  // start-address field in 16-byte units
+              tc_mma(tmem + kk * OZ_BN, da + (uint64_t)(s * (OZ_BLOCK >> 4)),
+                     db + (uint64_t)((kk - s) * (OZ_BLOCK >> 5)), OZ_IDESC, (kin > 0 || s > 0) ? 1u : 0u);
+          tc_commit(smem_u32(&bar_empty[buf]));
+          if (kin == OZ_CHUNK - 1 || ks == KS - 1) {
+            tc_commit(smem_u32(&bar_acc_full));
+            ++gc;
+          }
+          ++gs;
+          ok = produce();
+        }
+      }
+    }
+    __syncwarp();
+  } else {
+    // epilogue: warps 1-8; warp w reads TMEM lanes 32 (w % 4) .. +31 (tile rows), columns
+    // 32 h .. 32 h + 31 with h = (w - 1) / 4
+    const int quarter = warp & 3, half = (warp - 1) >> 2;
+    const int row = quarter * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + half * OZ_EPI_COLS;
+    // alpha, beta cases as integers, decided once (an FP64 compare per element would cost as
+    // much as the element's arithmetic)
+    const int amode = g.alpha == -1.0 ? 0 : (g.alpha == 1.0 ? 1 : 2);
+    const int bmode = g.beta == 0.0 ? 0 : (g.beta == 1.0 ? 1 : 2);
+    int gc = 0;
+    for (int t = first; t < ntiles; t = next_tile(t)) {
+      float acc_h[OZ_EPI_COLS], acc_l[OZ_EPI_COLS];
+#pragma unroll
+      for (int j = 0; j < OZ_EPI_COLS; ++j) acc_h[j] = acc_l[j] = 0.f;
+      bool ok = true;
+      for (int chunk = 0; chunk < nchunks; ++chunk, ++gc) {
+        if (!mbar_wait(smem_u32(&bar_acc_full), gc & 1, &abort_flag, g.err)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int cb = 0; cb < OZ_EPI_COLS / 8; ++cb) {
+          uint32_t v[OZ_NACC][8];
+#pragma unroll
+          for (int kk = 0; kk < OZ_NACC; ++kk) tc_ld8(trow + kk * OZ_BN + cb * 8, v[kk]);
+          tc_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            // sum_k v_k 2^(-8k), smallest weight first, in float-float (every term is exact)
+            float h = __uint_as_float(v[OZ_NACC - 1][j]) * 0x1p-48f, l = 0.f;
+#pragma unroll
+            for (int kk = OZ_NACC - 2; kk >= 0; --kk) {
+              const float tv = __uint_as_float(v[kk][j]) * __int_as_float((127 - 8 * kk) << 23);
+              float s, e;
+              two_sum(tv, h, s, e);
+              h = s;
+              l += e;
+            }
+            float s, e;
+            two_sum(acc_h[cb * 8 + j], h, s, e);
+            acc_h[cb * 8 + j] = s;
+            acc_l[cb * 8 + j] += e + l;
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(smem_u32(&bar_acc_empty));  // accumulators free: the next MMAs may start
+      }
+      if (!ok) break;
+      const int rt = t / g.tiles_n, ct = t % g.tiles_n;
+      const int i = rt * OZ_BM + row;
+      if (i >= g.m) continue;
+      const int ei = g.ea[i] - 16;
+      const int c0 = ct * OZ_BN + half * OZ_EPI_COLS;
+      double* crow = g.c + (int64_t)i * g.c_rs;
+#pragma unroll
+      for (int j0 = 0; j0 < OZ_EPI_COLS; j0 += 8) {
+        // eight columns at a time: their exponents and C values are loaded before any store
+        int off[8];
+        double cv[8];
+        bool w[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int col = c0 + j0 + j;
+          w[j] = col < g.n && !(g.lower && col > i);
+          off[j] = w[j] ? ei + g.eb[col] : 0;
+          cv[j] = (w[j] && bmode != 0) ? crow[(int64_t)col * g.c_cs] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (!w[j]) continue;
+          double xh, xl;
+          if (!ff_to_f64(acc_h[j0 + j], off[j], xh) || !ff_to_f64(acc_l[j0 + j], off[j], xl))
+            scale_slow(acc_h[j0 + j], acc_l[j0 + j], off[j], xh, xl);
+          double r;
+          if (bmode == 0) {
+            const double x = xh + xl;
+            r = amode == 0 ? -x : (amode == 1 ? x : g.alpha * x);
+          } else {
+            const double base = bmode == 1 ? cv[j] : g.beta * cv[j];
+            r = amode == 0 ? (base - xl) - xh : (amode == 1 ? (base + xl) + xh : fma(g.alpha, xh, fma(g.alpha, xl, base)));
+          }
+          crow[(int64_t)(c0 + j0 + j) * g.c_cs] = r;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS) : "memory");
+  }
+}
+
+// k = 0: C = beta C (the product is empty).
+__global__ void k_oz_scale(int64_t m, int64_t n, double beta, double* c, int64_t c_rs, int64_t c_cs, int lower) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= m * n) return;
+  const int64_t i = idx % m, j = idx / m;
+  if (lower && j > i) return;
+  double* cp = c + i * c_rs + j * c_cs;
+  *cp = beta == 0.0 ? 0.0 : beta * *cp;
+}
+
+// Digit blocks of one operand (rows x k): bytes of the workspace.
+static size_t oz_digits_bytes(int64_t rows, int64_t k) {
+  const int64_t rtiles = (rows + OZ_BM - 1) / OZ_BM, ksteps = (k + OZ_BK - 1) / OZ_BK;
+  return (size_t)rtiles * ksteps * OZ_A_BYTES;
+}
+
+size_t ozaki_workspace_bytes(int64_t m, int64_t n, int64_t k, bool same) {
+  const size_t ex = (size_t)(((m + 63) / 64) * 64 + ((n + 63) / 64) * 64) * sizeof(int32_t) + 256;
+  return oz_digits_bytes(m, k) + (same ? 0 : oz_digits_bytes(n, k)) + ex;
+}
+
+// C = alpha A B^T + beta C (lower: only i >= j).  B == nullptr: B = A (same strides).
+fg_status ozaki_gemm_nt(fg_ctx* ctx, cudaStream_t st, int64_t m, int64_t n, int64_t k, double alpha,
+                        const double* A, int64_t a_rs, int64_t a_cs, const double* B, int64_t b_rs, int64_t b_cs,
+                        double beta, double* C, int64_t c_rs, int64_t c_cs, bool lower, void* work, int* d_err) {
+  if (m <= 0 || n <= 0) return FG_OK;
+  if (k <= 0) {
+    if (beta != 1.0) {
+      k_oz_scale<<<(unsigned)((m * n + 255) / 256), 256, 0, st>>>(m, n, beta, C, c_rs, c_cs, lower ? 1 : 0);
+      ctx->launches += 1;
+      FG_CUDA_TRY(cudaGetLastError());
+    }
+    return FG_OK;
+  }
+  const bool same = B == nullptr;
+  if (same) {
+    b_rs = a_rs;
+    b_cs = a_cs;
+  }
+  const int64_t ksteps = k > 0 ? (k + OZ_BK - 1) / OZ_BK : 1;
+  const int64_t rta = (m + OZ_BM - 1) / OZ_BM, rtb = (n + OZ_BM - 1) / OZ_BM;
+  const int64_t tiles_n = (n + OZ_BN - 1) / OZ_BN;
+  if (rta * tiles_n > (1ll << 31) - 1 || ksteps > 65535) {
+    set_error("ozaki_gemm_nt: %lld x %lld x %lld is too large", (long long)m, (long long)n, (long long)k);
+    return FG_ERR_UNSUPPORTED;
+  }
+  uint8_t* wa = (uint8_t*)work;
+  uint8_t* wb = same ? wa : wa + oz_digits_bytes(m, k);
+  int32_t* ea = (int32_t*)(wb + (same ? oz_digits_bytes(m, k) : oz_digits_bytes(n, k)));
+  int32_t* eb = same ? ea : ea + ((m + 63) / 64) * 64;
+  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM));
+  const int64_t kk = k > 0 ? k : 0;
+  k_oz_rowexp<<<(unsigned)((m + 127) / 128), 128, 0, st>>>(m, kk, A, a_rs, a_cs, ea);
+  k_oz_split<<<dim3((unsigned)rta, (unsigned)ksteps), OZ_BM, 0, st>>>(m, kk, A, a_rs, a_cs, ea, (int)ksteps,
+                                                                     (uint4*)wa);
+  ctx->launches += 2;
+  if (!same) {
+    k_oz_rowexp<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, kk, B, b_rs, b_cs, eb);
+    k_oz_split<<<dim3((unsigned)rtb, (unsigned)ksteps), OZ_BM, 0, st>>>(n, kk, B, b_rs, b_cs, eb, (int)ksteps,
+                                                                       (uint4*)wb);
+    ctx->launches += 2;
+  }
+  OzGemmArgs g;
+  g.a = wa;
+  g.b = wb;
+  g.ea = ea;
+  g.eb = eb;
+  g.m = (int)m;
+  g.n = (int)n;
+  g.ksteps = (int)ksteps;
+  g.tiles_m = (int)rta;
+  g.tiles_n = (int)tiles_n;
+  g.alpha = alpha;
+  g.beta = beta;
+  g.c = C;
+  g.c_rs = c_rs;
+  g.c_cs = c_cs;
+  g.lower = lower ? 1 : 0;
+  g.err = d_err;
+  // persistent: one CTA per SM (the shared memory allows no second), at most one per tile
+  const int64_t tiles = lower ? std::min(rta * tiles_n, rta * (rta * 2 + 1)) : rta * tiles_n;
+  k_oz_gemm<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, ctx->sm_count)), OZ_THREADS, OZ_SMEM, st>>>(g);
+  ctx->launches += 1;
+  FG_CUDA_TRY(cudaGetLastError());
+  return FG_OK;
+}
+
+}  // namespace fg
+
+using namespace fg;
+
+extern "C" {
+
+fg_status fg_dense_gemm_nt(fg_ctx* ctx, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                           int64_t a_rs, int64_t a_cs, const double* B, int64_t b_rs, int64_t b_cs, double beta,
+                           double* C, int64_t c_rs, int64_t c_cs, int32_t flags) {
+  if (!ctx || (!A && k > 0) || !C || m < 0 || n < 0 || k < 0 || (flags & ~FG_DENSE_LOWER) ||
+      (!B && n != m && k > 0)) {
+    set_error("bad argument: ctx/A/C/m/n/k/flags (B = NULL needs n = m)");
+    return FG_ERR_BADARG;
+  }
+  if (m > (1ll << 31) - 1 || n > (1ll << 31) - 1) {
+    set_error("bad argument: m, n < 2^31");
+    return FG_ERR_BADARG;
+  }
+  FG_CUDA_TRY(cudaSetDevice(ctx->device));
+  if (m == 0 || n == 0) return FG_OK;
+  void* work = nullptr;
+  FG_TRY(dev_alloc(ctx, &work, ozaki_workspace_bytes(m, n, k, B == nullptr) + 16));
+  int* d_err = (int*)((uint8_t*)work + ozaki_workspace_bytes(m, n, k, B == nullptr));
+  fg_status s = FG_OK;
+  int h_err = 0;
+  cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream);
+  if (e == cudaSuccess) {
+    s = ozaki_gemm_nt(ctx, ctx->stream, m, n, k, alpha, A, a_rs, a_cs, B, b_rs, b_cs, beta, C, c_rs, c_cs,
+                      (flags & FG_DENSE_LOWER) != 0, work, d_err);
+    if (s == FG_OK) e = cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (s == FG_OK && e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  }
+  dev_free(ctx, work);
+  if (s != FG_OK) return s;
+  if (e != cudaSuccess) {
+    set_error("fg_dense_gemm_nt: %s", cudaGetErrorString(e));
+    return FG_ERR_CUDA;
+  }
+  if (h_err) {
+    set_error("fg_dense_gemm_nt: a bounded tensor-core wait ran out");
+    return (fg_status)h_err;
+  }
+  return FG_OK;
+}
+
+}  // extern "C"

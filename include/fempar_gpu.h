@@ -527,6 +527,20 @@ fg_status fg_server_take_solution(fg_server* srv, uint64_t ticket, double* x);
 fg_status fg_server_stats(fg_server* srv, uint64_t* peak_reserved, int64_t* completed);
 fg_status fg_server_destroy(fg_server* srv);
 
+/* ---------------------------------------------------------------------------------------
+ * Dense FP64 product on the bf16 tensor cores: C = alpha A B^T + beta C with A m x k,
+ * B n x k, C m x n; element (i, l) of A at A[i*a_rs + l*a_cs] (likewise B, C), device
+ * pointers, on the context's stream, synchronous.  B = NULL: B = A (needs n = m).
+ * flags: FG_DENSE_LOWER writes only the elements with i >= j.  FP64 is emulated by 7 signed
+ * 8-bit digits per value and row (Ozaki scheme); the result is within ~k 2^-51
+ * max|A_i.| max|B_j.| of the exact product, like an FP64 dot product.  No counterpart in the
+ * reference (its dense factorisations call MKL / PARDISO); the building block of the BDDC
+ * set-up's factorisations.  Returns FG_ERR_TIMEOUT if a bounded device wait ran out. */
+#define FG_DENSE_LOWER 1
+fg_status fg_dense_gemm_nt(fg_ctx* ctx, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                           int64_t a_rs, int64_t a_cs, const double* B, int64_t b_rs, int64_t b_cs, double beta,
+                           double* C, int64_t c_rs, int64_t c_cs, int32_t flags);
+
 /* Default parameters (reference defaults: CG, res_res, rtol 1e-6, 1000 iterations). */
 void fg_solver_params_default(fg_solver_params* p);
 void fg_integrand_default(fg_integrand* g);
