@@ -104,6 +104,7 @@ struct fg_bddc {
   int32_t* dOrder = nullptr;  // subdomains by decreasing factorisation work
   bool stepped = false;        // factorise panel step by panel step over all subdomains
   bool coarse_emulated = false; // coarse trailing updates on the tensor cores (last setup)
+  bool local_emulated = false;  // subdomain trailing updates on the tensor cores (last setup)
   int64_t* dIptr = nullptr;
   int64_t* dIsrc = nullptr;
   int32_t* dIvec = nullptr;
@@ -369,6 +370,20 @@ __global__ void __launch_bounds__(256) k_bstep_syrk(const BSub* __restrict__ sub
   while ((int64_t)ti * (ti + 1) / 2 > b) --ti;
   const int tj = (int)(b - (int64_t)ti * (ti + 1) / 2);
   chol_syrk_tile(A + S.aoff, S.N, S.N, j0, nb, t0, ti, tj, sm);
+}
+
+// k_bstep_syrk restricted to the columns [j0 + nb, min(cend, nr)) of a wider panel: tiles
+// (ti, tj, subdomain) = blockIdx (x, y, z), ti >= tj.
+__global__ void __launch_bounds__(256) k_bstep_syrk_panel(const BSub* __restrict__ subs, double* __restrict__ A,
+                                                          int j0, int cend) {
+  __shared__ CholSmem sm;
+  const BSub S = subs[blockIdx.z];
+  if (j0 >= S.nr) return;
+  const int nb = min(32, S.nr - j0);
+  const int t0 = j0 + nb, cN = min(cend, S.nr);
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (ti < tj || t0 + tj * 64 >= cN || t0 + ti * 64 >= S.N) return;
+  chol_syrk_tile(A + S.aoff, S.N, S.N, j0, nb, t0, ti, tj, sm, cN);
 }
 
 // Local coarse matrix K_Pi (order [V | e]), S_e^-1 and H = S_e^-1 T from the trailing block.
@@ -1535,7 +1550,68 @@ static fg_status bddc_numeric(fg_bddc* B) {
   cudaEvent_t ev[4];
   for (auto& e : ev) FG_CUDA_TRY(cudaEventCreate(&e));
   FG_CUDA_TRY(cudaEventRecord(ev[0], st));
-  if (B->stepped) {
+  // subdomain trailing updates on the tensor cores (FP64 emulated, fg_ozaki.cu), blocked by
+  // 128 columns, unless FG_BDDC_EMULATED_FP64=0
+  const char* ee = std::getenv("FG_BDDC_EMULATED_FP64");
+  const bool emulate = !(ee && ee[0] == '0');
+  B->local_emulated = false;
+  if (B->stepped && emulate) {
+    auto panel_items = [&](int J0) {
+      std::vector<OzSyrk> items;
+      for (const BSub& S : B->subs) {
+        if (J0 >= S.nr) continue;
+        const int J1 = std::min(J0 + 128, S.nr);
+        if (S.N - J1 <= 0) continue;
+        double* As = B->dA + S.aoff;
+        items.push_back(OzSyrk{As + J1 + (int64_t)J0 * S.N, As + J1 + (int64_t)J1 * S.N, (int64_t)S.N, S.N - J1,
+                               J1 - J0});
+      }
+      return items;
+    };
+    const size_t wbytes = ozaki_syrk_batch_bytes(panel_items(0));
+    void* work = nullptr;
+    FG_TRY(dev_alloc(ctx, &work, wbytes + sizeof(int)));
+    int* oz_err = (int*)((uint8_t*)work + wbytes);
+    fg_status ls = FG_OK;
+    cudaError_t ce = cudaMemsetAsync(oz_err, 0, sizeof(int), st);
+    for (int J0 = 0; J0 < B->maxnr && ls == FG_OK && ce == cudaSuccess; J0 += 128) {
+      for (int j0 = J0; j0 < std::min(J0 + 128, B->maxnr); j0 += 32) {
+        k_bstep_diag<<<ns, 32, 0, st>>>(B->d_subs, B->dA, j0, B->dErr);
+        const int rem = B->maxN - j0 - 1;
+        if (rem > 0) {
+          k_bstep_trsm<<<dim3(nblk(rem, 256), ns), 256, 0, st>>>(B->d_subs, B->dA, j0);
+          const int nt = (rem + 63) / 64;
+          const int ntc = std::max(0, (J0 + 128 - (j0 + 32) + 63) / 64);  // column tiles left in the panel
+          if (ntc > 0) {
+            k_bstep_syrk_panel<<<dim3((unsigned)nt, (unsigned)ntc, ns), 256, 0, st>>>(B->d_subs, B->dA, j0, J0 + 128);
+            ctx->launches += 1;
+          }
+          ctx->launches += 1;
+        }
+        ctx->launches += 1;
+      }
+      ls = ozaki_syrk_batch(ctx, st, panel_items(J0), work, wbytes, oz_err);
+    }
+    int h_oz = 0;
+    if (ls == FG_OK && ce == cudaSuccess) ce = cudaMemcpyAsync(&h_oz, oz_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ls == FG_OK && ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    dev_free(ctx, work);
+    if (ls != FG_OK) {
+      for (auto& e : ev) cudaEventDestroy(e);
+      return ls;
+    }
+    if (ce != cudaSuccess) {
+      for (auto& e : ev) cudaEventDestroy(e);
+      set_error("BDDC factorisation: %s", cudaGetErrorString(ce));
+      return FG_ERR_CUDA;
+    }
+    if (h_oz) {
+      for (auto& e : ev) cudaEventDestroy(e);
+      set_error("BDDC: a bounded tensor-core wait ran out in the subdomain factorisation");
+      return (fg_status)h_oz;
+    }
+    B->local_emulated = true;
+  } else if (B->stepped) {
     for (int j0 = 0; j0 < B->maxnr; j0 += 32) {
       k_bstep_diag<<<ns, 32, 0, st>>>(B->d_subs, B->dA, j0, B->dErr);
       const int rem = B->maxN - j0 - 1;
@@ -1578,9 +1654,8 @@ static fg_status bddc_numeric(fg_bddc* B) {
     // coarse matrices of 1024 dofs and more: trailing updates on the tensor cores (FP64
     // emulated), unless FG_BDDC_EMULATED_FP64=0
     void* work = nullptr;
-    const char* ee = std::getenv("FG_BDDC_EMULATED_FP64");
     const size_t wbytes = ozaki_workspace_bytes(2 * nC, 2 * nC, 128, true);
-    if (nC >= 1024 && !(ee && ee[0] == '0')) {
+    if (nC >= 1024 && emulate) {
       FG_TRY(dev_alloc(ctx, &work, wbytes + sizeof(int)));
       FG_CUDA_TRY(cudaMemsetAsync((uint8_t*)work + wbytes, 0, sizeof(int), st));
     }

@@ -282,5 +282,16 @@ size_t ozaki_workspace_bytes(int64_t m, int64_t n, int64_t k, bool same);
 fg_status ozaki_gemm_nt(fg_ctx* ctx, cudaStream_t st, int64_t m, int64_t n, int64_t k, double alpha,
                         const double* A, int64_t a_rs, int64_t a_cs, const double* B, int64_t b_rs, int64_t b_cs,
                         double beta, double* C, int64_t c_rs, int64_t c_cs, bool lower, void* work, int* d_err);
+// A batch of lower rank-k updates C_b -= P_b P_b^T (k_b <= 128, column-major with leading
+// dimension ld_b), in one launch of each kernel; work holds ozaki_syrk_batch_bytes(b) bytes.
+struct OzSyrk {
+  const double* p;
+  double* c;
+  int64_t ld;
+  int m, k;
+};
+size_t ozaki_syrk_batch_bytes(const std::vector<OzSyrk>& b);
+fg_status ozaki_syrk_batch(fg_ctx* ctx, cudaStream_t st, const std::vector<OzSyrk>& b, void* work, size_t bytes,
+                           int* d_err);
 
 }  // namespace fg

@@ -15,12 +15,16 @@
 //   * the digit matrices are multiplied by tcgen05.mma kind::f16 (bf16 x bf16 -> FP32).  A
 //     digit product is at most 2^14, and an accumulator sums at most 7 pairs over K <= 128:
 //     every FP32 partial sum is an integer below 2^24, i.e. exact;
-//   * the products of weight 2^(-8k), k = s + t = 0..6 (28 digit pairs), go to 7 FP32
-//     accumulators in tensor memory; pairs with s + t >= 7 are dropped (|error| <~ K 2^-51
-//     max_l |x_il| max_l |y_jl|, inside the FP64 dot-product bound);
-//   * the epilogue sums the 7 accumulators in float-float (error-free FP32 two-sums), adds the
-//     K chunks of 128 in float-float, and applies alpha 2^(e_i + f_j - 16) in FP64 once per
-//     output element (5 FP64 operations per element instead of K).
+//   * the products of weight 2^(-8k), k = s + t = 0..7 (34 digit pairs), go to 8 FP32
+//     accumulators in tensor memory (8 x 64 columns: all 512); pairs with s + t >= 8 are
+//     dropped (|error| <~ K 2^-59 max_l |x_il| max_l |y_jl|).  The cut keeps 56 bits below
+//     2^e_i, so a value far below its row's maximum loses its low bits: overall the product
+//     is within ~K 2^-53 max|x_i.| max|y_j.| of the exact one (the FP64 dot-product bound);
+//   * the epilogue converts the 8 class sums to integers, combines them exactly in int64,
+//     turns the chunk's sum into FP64 with one rounding (two exact conversions by bit
+//     arithmetic, one addition), adds the K chunks of 128 in FP64, and applies the power of
+//     two 2^(e_i + f_j - 16) through the exponent field: ~2 FP64 operations per output
+//     element and chunk instead of 128.
 //
 // Digit layout in HBM: per operand, blocks of 128 rows x 16 columns (one MMA K step) per
 // digit, 4 KB each, ordered [row tile][K step][digit]; inside a block the rows are in the
@@ -46,7 +50,7 @@ namespace fg {
 namespace {
 
 constexpr int OZ_S = 7;                       // digits per value
-constexpr int OZ_NACC = 7;                    // accumulators: digit weights k = s + t = 0..6
+constexpr int OZ_NACC = 8;                    // accumulators: digit weights k = s + t = 0..7
 constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 16;
 constexpr int OZ_CHUNK = 8;                   // K steps per exact accumulation (K <= 128)
 constexpr int OZ_NBUF = 5;                    // shared-memory stages
@@ -55,7 +59,7 @@ constexpr uint32_t OZ_A_BYTES = OZ_S * OZ_BLOCK;           // 28672 B per K step
 constexpr uint32_t OZ_B_BYTES = OZ_S * OZ_BLOCK / 2;       // 14336 B per K step
 constexpr uint32_t OZ_STAGE = OZ_A_BYTES + OZ_B_BYTES;     // 43008 B
 constexpr uint32_t OZ_SMEM = OZ_NBUF * OZ_STAGE;           // 215040 B: one CTA per SM
-constexpr uint32_t OZ_TMEM_COLS = 512;                     // 7 x 64 used
+constexpr uint32_t OZ_TMEM_COLS = 512;                     // 8 x 64: all of it
 constexpr long long OZ_WAIT_CYCLES = 1ll << 31;            // ~1 s at 2 GHz
 constexpr int OZ_EPI_COLS = 32;                            // columns per epilogue thread
 constexpr int OZ_THREADS = 32 + 4 * 32 * (OZ_BN / OZ_EPI_COLS);  // MMA warp + 8 epilogue warps
@@ -139,46 +143,71 @@ __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile 
   return true;
 }
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
 }  // namespace
 
-// Row exponents: e_r with max_l |x_rl| < 2^(e_r - 1), from the largest biased exponent of
-// the row (an all-zero row gets 0).  Thread per row.
-__global__ void k_oz_rowexp(int64_t rows, int64_t k, const double* __restrict__ x, int64_t rs, int64_t cs,
-                            int32_t* __restrict__ e) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
-  unsigned long long mx = 0;
-  for (int64_t l = 0; l < k; ++l) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x[r * rs + l * cs]) & 0x7FFFFFFFFFFFFFFFull;
-    mx = b > mx ? b : mx;
+// ---- operands: one or more row blocks cut into digits ------------------------------------
+// A split item: rows x k values, element (r, l) at x[r*rs + l*cs], cut into the digit row
+// tiles rtile0 .. rtile0 + ceil(rows/128) - 1 of the workspace (exponents at 128 rtile + r).
+struct OzSplit {
+  const double* x;
+  int64_t rs, cs;
+  int rows, k;
+  int rtile0;
+};
+struct OzSplitArgs {
+  const OzSplit* items;  // device array, or nullptr: one[0 .. none-1]
+  int nitems;
+  OzSplit one[2];
+  int none;
+  int ksteps;
+  int32_t* ex;
+  uint4* dig;
+};
+
+__device__ __forceinline__ OzSplit split_of(const OzSplitArgs& a, int rtile) {
+  if (!a.items) return (a.none > 1 && rtile >= a.one[1].rtile0) ? a.one[1] : a.one[0];
+  int lo = 0, hi = a.nitems - 1;  // last item with rtile0 <= rtile
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (a.items[mid].rtile0 <= rtile) lo = mid;
+    else hi = mid - 1;
   }
-  const int E = (int)(mx >> 52);            // biased exponent of the largest |x| (0: zero/subnormal)
-  e[r] = mx == 0 ? 0 : (E == 0 ? 1 : E) - 1021;
+  return a.items[lo];
 }
 
-// Digits: block (row tile, K step), thread per row; 16 values, 7 digits each, written as the
-// 7 digit blocks' 32-byte rows.  Rows >= rows and columns >= k are zero.
-__global__ void __launch_bounds__(OZ_BM) k_oz_split(int64_t rows, int64_t k, const double* __restrict__ x,
-                                                    int64_t rs, int64_t cs, const int32_t* __restrict__ e,
-                                                    int ksteps, uint4* __restrict__ out) {
+// Row exponents: e_r with max_l |x_rl| < 2^(e_r - 1), from the largest biased exponent of
+// the row (an all-zero or padding row gets 0).  Block per digit row tile, thread per row.
+__global__ void __launch_bounds__(OZ_BM) k_oz_rowexp(OzSplitArgs a) {
+  const int rtile = blockIdx.x;
+  const OzSplit it = split_of(a, rtile);
+  const int64_t r = (int64_t)(rtile - it.rtile0) * OZ_BM + threadIdx.x;
+  unsigned long long mx = 0;
+  if (r < it.rows)
+    for (int64_t l = 0; l < it.k; ++l) {
+      const unsigned long long b =
+          (unsigned long long)__double_as_longlong(it.x[r * it.rs + l * it.cs]) & 0x7FFFFFFFFFFFFFFFull;
+      mx = b > mx ? b : mx;
+    }
+  const int E = (int)(mx >> 52);            // biased exponent of the largest |x| (0: zero/subnormal)
+  a.ex[(int64_t)rtile * OZ_BM + threadIdx.x] = mx == 0 ? 0 : (E == 0 ? 1 : E) - 1021;
+}
+
+// Digits: block (digit row tile, K step), thread per row; 16 values, 7 digits each, written as
+// the 7 digit blocks' 32-byte rows.  Rows past the item and columns >= k are zero.
+__global__ void __launch_bounds__(OZ_BM) k_oz_split(OzSplitArgs a) {
   const int tid = threadIdx.x;
-  const int64_t r = (int64_t)blockIdx.x * OZ_BM + tid;
-  const int ks = blockIdx.y;
+  const int rtile = blockIdx.x, ks = blockIdx.y;
+  const OzSplit it = split_of(a, rtile);
+  const int64_t r = (int64_t)(rtile - it.rtile0) * OZ_BM + tid;
+  const int er = a.ex[(int64_t)rtile * OZ_BM + tid];
   uint32_t w[OZ_S][8];
-  const int er = r < rows ? e[r] : 0;
 #pragma unroll
   for (int c = 0; c < OZ_BK; c += 2) {
     int32_t d[2][OZ_S];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int64_t l = (int64_t)ks * OZ_BK + c + h;
-      const double v = (r < rows && l < k) ? x[r * rs + l * cs] : 0.0;
+      const double v = (r < it.rows && l < it.k) ? it.x[r * it.rs + l * it.cs] : 0.0;
       const unsigned long long b = (unsigned long long)__double_as_longlong(v);
       const int E = (int)((b >> 52) & 0x7FF);
       const long long mant = (long long)(b & 0xFFFFFFFFFFFFFull) | (E ? (1ll << 52) : 0ll);
@@ -203,55 +232,89 @@ __global__ void __launch_bounds__(OZ_BM) k_oz_split(int64_t rows, int64_t k, con
       w[s][c / 2] = lo | (hi << 16);
     }
   }
-  const size_t blk = ((size_t)blockIdx.x * ksteps + ks) * OZ_S;
+  const size_t blk = ((size_t)rtile * a.ksteps + ks) * OZ_S;
   const int g = tid >> 3, r8 = tid & 7;
 #pragma unroll
   for (int s = 0; s < OZ_S; ++s) {
-    uint4* p = out + (blk + s) * (OZ_BLOCK / 16);
+    uint4* p = a.dig + (blk + s) * (OZ_BLOCK / 16);
     p[g * 16 + r8] = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);      // columns 0-7
     p[g * 16 + 8 + r8] = make_uint4(w[s][4], w[s][5], w[s][6], w[s][7]);  // columns 8-15
   }
 }
 
-struct OzGemmArgs {
-  const uint8_t* a;      // digit blocks of A
-  const uint8_t* b;      // digit blocks of B
-  const int32_t* ea;     // row exponents of A
-  const int32_t* eb;     // row exponents of B
-  int m, n, ksteps;
-  int tiles_m, tiles_n;  // 128-row and 64-column tiles
-  double alpha, beta;
+// ---- products --------------------------------------------------------------------------
+// One product of a launch: C (m x n; (i, j) at c[i*c_rs + j*c_cs]) from the digit row tiles
+// arow0.. (A) and brow0.. (B); its output tiles are tile0 .. tile0 + ceil(m/128) tiles_n - 1.
+struct OzItem {
   double* c;
   int64_t c_rs, c_cs;
+  int m, n;
+  int arow0, brow0;
+  int tiles_n;
+  int tile0;
+};
+
+struct OzGemmArgs {
+  const uint8_t* dig;    // digit blocks [row tile][K step][digit]
+  const int32_t* ex;     // row exponents [row tile][128]
+  const OzItem* items;   // device array, or nullptr: `one`
+  int nitems;
+  OzItem one;
+  int ntiles;            // output tiles of all items
+  int ksteps;
+  double alpha, beta;
   int lower;             // write only i >= j
   int* err;
 };
 
-// 2^off (h + l) as two FP64 values, by exponent arithmetic (no FP64 operation).  h and l are
-// normal or zero (every partial sum is a multiple of 2^-48); false if the result would leave
-// the normal FP64 range.
-__device__ __forceinline__ bool ff_to_f64(float f, int off, double& d) {
-  const uint32_t u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
-  if (a == 0) {
+__device__ __forceinline__ OzItem item_of(const OzGemmArgs& g, int t) {
+  if (!g.items) return g.one;
+  int lo = 0, hi = g.nitems - 1;  // last item with tile0 <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (g.items[mid].tile0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return g.items[lo];
+}
+
+// x 2^off as FP64, for |x| < 2^53 (exact), by integer operations on the bit pattern (no
+// FP64 operation); false if the result would leave the normal FP64 range.
+__device__ __forceinline__ bool i64_to_f64(long long x, int off, double& d) {
+  if (x == 0) {
     d = 0.0;
     return true;
   }
-  const int e = (int)(a >> 23) + (1023 - 127) + off;
-  if (e < 1 || e > 2046) return false;
-  d = __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | ((unsigned long long)e << 52) |
-                                       ((unsigned long long)(a & 0x7FFFFFu) << 29)));
+  const unsigned long long sgn = x < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long a = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+  const int lz = __clzll((long long)a);
+  const int be = (63 - lz) + 1023 + off;
+  if (be < 1 || be > 2046) return false;
+  const unsigned long long mant = (a << (lz + 1)) >> 12;  // the bits after the leading one
+  d = __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | mant));
   return true;
 }
 
-// out-of-range fallback of ff_to_f64 (kept out of line: it costs FP64 operations)
-__device__ __noinline__ void scale_slow(float h, float l, int off, double& xh, double& xl) {
-  xh = ldexp((double)h, off);
-  xl = ldexp((double)l, off);
+// d 2^off by adding off to the exponent field; false if d or the result is not a normal
+// FP64 number (zero passes).
+__device__ __forceinline__ bool scale_f64(double d, int off, double& r) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if ((b << 1) == 0) {
+    r = d;
+    return true;
+  }
+  if (e == 0 || e == 0x7FF || e + off < 1 || e + off > 2046) return false;
+  r = __longlong_as_double((long long)(b + ((unsigned long long)(long long)off << 52)));
+  return true;
 }
 
-// Persistent: CTA b takes the tiles b, b + gridDim.x, ... (upper tiles skipped when lower).
-// The accumulators are released as soon as the epilogue has read them, so the next tile's
-// MMAs run while the epilogue writes C.
+// out-of-range fallback of scale_f64 (kept out of line: it costs FP64 operations)
+__device__ __noinline__ double scale_slow(double d, int off) { return ldexp(d, off); }
+
+// Persistent: CTA b takes the output tiles b, b + gridDim.x, ... of all items (tiles above
+// the diagonal skipped when lower).  The accumulators are released as soon as the epilogue
+// has read them, so the next tile's MMAs run while the epilogue writes C.
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
   extern __shared__ __align__(1024) uint8_t oz_smem[];
   __shared__ __align__(8) uint64_t bar_full[OZ_NBUF], bar_empty[OZ_NBUF], bar_acc_full, bar_acc_empty;
@@ -259,8 +322,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
   __shared__ volatile int abort_flag;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = g.tiles_m * g.tiles_n;
-  auto valid = [&](int t) { return !g.lower || (t % g.tiles_n) * OZ_BN <= (t / g.tiles_n) * OZ_BM + OZ_BM - 1; };
+  const int ntiles = g.ntiles;
+  // tile t of item it: local tile lt = t - tile0, row tile lt / tiles_n, column tile lt % tiles_n
+  auto valid = [&](int t) {
+    if (!g.lower) return true;
+    const OzItem it = item_of(g, t);
+    const int lt = t - it.tile0;
+    return (lt % it.tiles_n) * OZ_BN <= (lt / it.tiles_n) * OZ_BM + OZ_BM - 1;
+  };
   auto next_tile = [&](int t) {
     for (t += gridDim.x; t < ntiles && !valid(t); t += gridDim.x) {
     }
@@ -295,26 +364,34 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
   if (warp == 0) {
     if (lane == 0) {
       const uint32_t sbase = smem_u32(oz_smem);
-      // producer cursor: tile pt, K step pks, global stage counter pgs
+      // producer cursor: tile pt (its digit rows pa, pb and half), K step pks, stage counter pgs
       int pt = first, pks = 0, pgs = 0;
+      const uint8_t *pa = nullptr, *pb = nullptr;
+      auto locate = [&]() {
+        if (pt >= ntiles) return;
+        const OzItem it = item_of(g, pt);
+        const int lt = pt - it.tile0, rt = lt / it.tiles_n, ct = lt % it.tiles_n;
+        pa = g.dig + (size_t)(it.arow0 + rt) * KS * OZ_A_BYTES;
+        pb = g.dig + (size_t)(it.brow0 + (ct >> 1)) * KS * OZ_A_BYTES + (size_t)(ct & 1) * (OZ_BLOCK / 2);
+      };
+      locate();
       auto produce = [&]() -> bool {
         if (pt >= ntiles) return true;
         const int buf = pgs % OZ_NBUF;
         if (pgs >= OZ_NBUF && !mbar_wait(smem_u32(&bar_empty[buf]), ((pgs / OZ_NBUF) - 1) & 1, &abort_flag, g.err))
           return false;
-        const int rt = pt / g.tiles_n, ct = pt % g.tiles_n;
-        const uint8_t* asrc = g.a + ((size_t)rt * KS + pks) * OZ_A_BYTES;
-        const uint8_t* bsrc = g.b + ((size_t)(ct >> 1) * KS + pks) * OZ_A_BYTES + (size_t)(ct & 1) * (OZ_BLOCK / 2);
         const uint32_t full = smem_u32(&bar_full[buf]);
         const uint32_t dst = sbase + buf * OZ_STAGE;
         mbar_expect_tx(full, OZ_STAGE);
-        bulk_g2s(dst, asrc, OZ_A_BYTES, full);
+        bulk_g2s(dst, pa + (size_t)pks * OZ_A_BYTES, OZ_A_BYTES, full);
         for (int t = 0; t < OZ_S; ++t)
-          bulk_g2s(dst + OZ_A_BYTES + t * (OZ_BLOCK / 2), bsrc + (size_t)t * OZ_BLOCK, OZ_BLOCK / 2, full);
+          bulk_g2s(dst + OZ_A_BYTES + t * (OZ_BLOCK / 2), pb + ((size_t)pks * OZ_S + t) * OZ_BLOCK, OZ_BLOCK / 2,
+                   full);
         ++pgs;
         if (++pks == KS) {
           pks = 0;
           pt = next_tile(pt);
+          locate();
         }
         return true;
       };
@@ -339,9 +416,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
 #pragma unroll
           for (int kk = 0; kk < OZ_NACC; ++kk)
 #pragma unroll
-            for (int s = 0; s <= kk; ++s)  // start-address field in 16-byte units
+            for (int s = (kk > OZ_S - 1 ? kk - (OZ_S - 1) : 0); s <= (kk < OZ_S - 1 ? kk : OZ_S - 1); ++s)
+              // start-address field in 16-byte units; the first pair of a class starts the chunk's sum
               tc_mma(tmem + kk * OZ_BN, da + (uint64_t)(s * (OZ_BLOCK >> 4)),
-                     db + (uint64_t)((kk - s) * (OZ_BLOCK >> 5)), OZ_IDESC, (kin > 0 || s > 0) ? 1u : 0u);
+                     db + (uint64_t)((kk - s) * (OZ_BLOCK >> 5)), OZ_IDESC,
+                     (kin > 0 || s > (kk > OZ_S - 1 ? kk - (OZ_S - 1) : 0)) ? 1u : 0u);
           tc_commit(smem_u32(&bar_empty[buf]));
           if (kin == OZ_CHUNK - 1 || ks == KS - 1) {
             tc_commit(smem_u32(&bar_acc_full));
@@ -365,9 +444,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
     const int bmode = g.beta == 0.0 ? 0 : (g.beta == 1.0 ? 1 : 2);
     int gc = 0;
     for (int t = first; t < ntiles; t = next_tile(t)) {
-      float acc_h[OZ_EPI_COLS], acc_l[OZ_EPI_COLS];
+      // per column: sum over K chunks of the chunk's product / 2^(e_i + f_j - 16), in FP64
+      double acc[OZ_EPI_COLS];
 #pragma unroll
-      for (int j = 0; j < OZ_EPI_COLS; ++j) acc_h[j] = acc_l[j] = 0.f;
+      for (int j = 0; j < OZ_EPI_COLS; ++j) acc[j] = 0.0;
       bool ok = true;
       for (int chunk = 0; chunk < nchunks; ++chunk, ++gc) {
         if (!mbar_wait(smem_u32(&bar_acc_full), gc & 1, &abort_flag, g.err)) {
@@ -377,38 +457,52 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
         tc_fence_after();
 #pragma unroll
         for (int cb = 0; cb < OZ_EPI_COLS / 8; ++cb) {
-          uint32_t v[OZ_NACC][8];
+          // sum_k v_k 2^(-8k) exactly: every v_k is an integer below 2^24 held in FP32; hi in
+          // units of 2^-16 (classes 0-2), lo in units of 2^-56 (classes 3-7), loaded four
+          // classes at a time
+          long long hi[8], lo[8];
 #pragma unroll
-          for (int kk = 0; kk < OZ_NACC; ++kk) tc_ld8(trow + kk * OZ_BN + cb * 8, v[kk]);
-          tc_wait_ld();
+          for (int part = 0; part < 2; ++part) {
+            uint32_t v[OZ_NACC / 2][8];
+#pragma unroll
+            for (int q = 0; q < OZ_NACC / 2; ++q) tc_ld8(trow + (part * 4 + q) * OZ_BN + cb * 8, v[q]);
+            tc_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              int a[OZ_NACC / 2];
+#pragma unroll
+              for (int q = 0; q < OZ_NACC / 2; ++q) a[q] = __float2int_rn(__uint_as_float(v[q][j]));
+              if (part == 0) {
+                hi[j] = (long long)a[0] * 65536 + (long long)a[1] * 256 + a[2];
+                lo[j] = (long long)a[3] * 4294967296ll;
+              } else {
+                lo[j] += (long long)a[0] * 16777216 + (long long)a[1] * 65536 + (long long)a[2] * 256 + a[3];
+              }
+            }
+          }
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            // sum_k v_k 2^(-8k), smallest weight first, in float-float (every term is exact)
-            float h = __uint_as_float(v[OZ_NACC - 1][j]) * 0x1p-48f, l = 0.f;
-#pragma unroll
-            for (int kk = OZ_NACC - 2; kk >= 0; --kk) {
-              const float tv = __uint_as_float(v[kk][j]) * __int_as_float((127 - 8 * kk) << 23);
-              float s, e;
-              two_sum(tv, h, s, e);
-              h = s;
-              l += e;
-            }
-            float s, e;
-            two_sum(acc_h[cb * 8 + j], h, s, e);
-            acc_h[cb * 8 + j] = s;
-            acc_l[cb * 8 + j] += e + l;
+            // |hi| < 2^42 and |lo| < 2^57: move lo's bits above 2^40 into hi, then both
+            // convert exactly; one rounding for the chunk
+            const long long carry = lo[j] >> 40;
+            double xh, xl;
+            i64_to_f64(hi[j] + carry, -16, xh);
+            i64_to_f64(lo[j] - carry * 1099511627776ll, -56, xl);
+            acc[cb * 8 + j] += xh + xl;
           }
         }
         tc_fence_before();
         mbar_arrive(smem_u32(&bar_acc_empty));  // accumulators free: the next MMAs may start
       }
       if (!ok) break;
-      const int rt = t / g.tiles_n, ct = t % g.tiles_n;
+      const OzItem it = item_of(g, t);
+      const int lt = t - it.tile0, rt = lt / it.tiles_n, ct = lt % it.tiles_n;
       const int i = rt * OZ_BM + row;
-      if (i >= g.m) continue;
-      const int ei = g.ea[i] - 16;
+      if (i >= it.m) continue;
+      const int ei = g.ex[(int64_t)(it.arow0 + rt) * OZ_BM + row];
       const int c0 = ct * OZ_BN + half * OZ_EPI_COLS;
-      double* crow = g.c + (int64_t)i * g.c_rs;
+      const int32_t* ebp = g.ex + (int64_t)(it.brow0 + (ct >> 1)) * OZ_BM + (ct & 1) * OZ_BN + half * OZ_EPI_COLS;
+      double* crow = it.c + (int64_t)i * it.c_rs;
 #pragma unroll
       for (int j0 = 0; j0 < OZ_EPI_COLS; j0 += 8) {
         // eight columns at a time: their exponents and C values are loaded before any store
@@ -418,25 +512,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int col = c0 + j0 + j;
-          w[j] = col < g.n && !(g.lower && col > i);
-          off[j] = w[j] ? ei + g.eb[col] : 0;
-          cv[j] = (w[j] && bmode != 0) ? crow[(int64_t)col * g.c_cs] : 0.0;
+          w[j] = col < it.n && !(g.lower && col > i);
+          off[j] = w[j] ? ei + ebp[j0 + j] : 0;
+          cv[j] = (w[j] && bmode != 0) ? crow[(int64_t)col * it.c_cs] : 0.0;
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           if (!w[j]) continue;
-          double xh, xl;
-          if (!ff_to_f64(acc_h[j0 + j], off[j], xh) || !ff_to_f64(acc_l[j0 + j], off[j], xl))
-            scale_slow(acc_h[j0 + j], acc_l[j0 + j], off[j], xh, xl);
+          // product = 2^(e_i + f_j - 16) acc: a power of two, applied to the exponent field
+          double x;
+          if (!scale_f64(acc[j0 + j], off[j] - 16, x)) x = scale_slow(acc[j0 + j], off[j] - 16);
           double r;
           if (bmode == 0) {
-            const double x = xh + xl;
             r = amode == 0 ? -x : (amode == 1 ? x : g.alpha * x);
           } else {
             const double base = bmode == 1 ? cv[j] : g.beta * cv[j];
-            r = amode == 0 ? (base - xl) - xh : (amode == 1 ? (base + xl) + xh : fma(g.alpha, xh, fma(g.alpha, xl, base)));
+            r = amode == 0 ? base - x : (amode == 1 ? base + x : fma(g.alpha, x, base));
           }
-          crow[(int64_t)(c0 + j0 + j) * g.c_cs] = r;
+          crow[(int64_t)(c0 + j0 + j) * it.c_cs] = r;
         }
       }
     }
@@ -459,15 +552,24 @@ __global__ void k_oz_scale(int64_t m, int64_t n, double beta, double* c, int64_t
   *cp = beta == 0.0 ? 0.0 : beta * *cp;
 }
 
-// Digit blocks of one operand (rows x k): bytes of the workspace.
-static size_t oz_digits_bytes(int64_t rows, int64_t k) {
-  const int64_t rtiles = (rows + OZ_BM - 1) / OZ_BM, ksteps = (k + OZ_BK - 1) / OZ_BK;
-  return (size_t)rtiles * ksteps * OZ_A_BYTES;
-}
+static int64_t rtiles_of(int64_t rows) { return (rows + OZ_BM - 1) / OZ_BM; }
 
 size_t ozaki_workspace_bytes(int64_t m, int64_t n, int64_t k, bool same) {
-  const size_t ex = (size_t)(((m + 63) / 64) * 64 + ((n + 63) / 64) * 64) * sizeof(int32_t) + 256;
-  return oz_digits_bytes(m, k) + (same ? 0 : oz_digits_bytes(n, k)) + ex;
+  const int64_t rt = rtiles_of(m) + (same ? 0 : rtiles_of(n));
+  const int64_t ks = std::max<int64_t>(1, (k + OZ_BK - 1) / OZ_BK);
+  return (size_t)rt * ks * OZ_A_BYTES + (size_t)rt * OZ_BM * sizeof(int32_t) + 256;
+}
+
+static fg_status oz_launch(fg_ctx* ctx, cudaStream_t st, OzSplitArgs& sa, int64_t rtiles, OzGemmArgs& g,
+                           int64_t ntiles) {
+  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM));
+  k_oz_rowexp<<<(unsigned)rtiles, OZ_BM, 0, st>>>(sa);
+  k_oz_split<<<dim3((unsigned)rtiles, (unsigned)sa.ksteps), OZ_BM, 0, st>>>(sa);
+  // persistent: one CTA per SM (the shared memory allows no second), at most one per tile
+  k_oz_gemm<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, ctx->sm_count)), OZ_THREADS, OZ_SMEM, st>>>(g);
+  ctx->launches += 3;
+  FG_CUDA_TRY(cudaGetLastError());
+  return FG_OK;
 }
 
 // C = alpha A B^T + beta C (lower: only i >= j).  B == nullptr: B = A (same strides).
@@ -484,56 +586,96 @@ fg_status ozaki_gemm_nt(fg_ctx* ctx, cudaStream_t st, int64_t m, int64_t n, int6
     return FG_OK;
   }
   const bool same = B == nullptr;
-  if (same) {
-    b_rs = a_rs;
-    b_cs = a_cs;
-  }
-  const int64_t ksteps = k > 0 ? (k + OZ_BK - 1) / OZ_BK : 1;
-  const int64_t rta = (m + OZ_BM - 1) / OZ_BM, rtb = (n + OZ_BM - 1) / OZ_BM;
+  const int64_t ksteps = (k + OZ_BK - 1) / OZ_BK;
+  const int64_t rta = rtiles_of(m), rtb = same ? 0 : rtiles_of(n);
   const int64_t tiles_n = (n + OZ_BN - 1) / OZ_BN;
-  if (rta * tiles_n > (1ll << 31) - 1 || ksteps > 65535) {
+  if (rta * tiles_n > (1ll << 31) - 1 || rta + rtb > (1ll << 31) - 1 || ksteps > 65535) {
     set_error("ozaki_gemm_nt: %lld x %lld x %lld is too large", (long long)m, (long long)n, (long long)k);
     return FG_ERR_UNSUPPORTED;
   }
-  uint8_t* wa = (uint8_t*)work;
-  uint8_t* wb = same ? wa : wa + oz_digits_bytes(m, k);
-  int32_t* ea = (int32_t*)(wb + (same ? oz_digits_bytes(m, k) : oz_digits_bytes(n, k)));
-  int32_t* eb = same ? ea : ea + ((m + 63) / 64) * 64;
-  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM));
-  const int64_t kk = k > 0 ? k : 0;
-  k_oz_rowexp<<<(unsigned)((m + 127) / 128), 128, 0, st>>>(m, kk, A, a_rs, a_cs, ea);
-  k_oz_split<<<dim3((unsigned)rta, (unsigned)ksteps), OZ_BM, 0, st>>>(m, kk, A, a_rs, a_cs, ea, (int)ksteps,
-                                                                     (uint4*)wa);
-  ctx->launches += 2;
-  if (!same) {
-    k_oz_rowexp<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, kk, B, b_rs, b_cs, eb);
-    k_oz_split<<<dim3((unsigned)rtb, (unsigned)ksteps), OZ_BM, 0, st>>>(n, kk, B, b_rs, b_cs, eb, (int)ksteps,
-                                                                       (uint4*)wb);
-    ctx->launches += 2;
-  }
+  OzSplitArgs sa;
+  sa.items = nullptr;
+  sa.nitems = 0;
+  sa.one[0] = OzSplit{A, a_rs, a_cs, (int)m, (int)k, 0};
+  sa.one[1] = OzSplit{B, b_rs, b_cs, (int)n, (int)k, (int)rta};
+  sa.none = same ? 1 : 2;
+  sa.ksteps = (int)ksteps;
+  sa.dig = (uint4*)work;
+  sa.ex = (int32_t*)((uint8_t*)work + (size_t)(rta + rtb) * ksteps * OZ_A_BYTES);
   OzGemmArgs g;
-  g.a = wa;
-  g.b = wb;
-  g.ea = ea;
-  g.eb = eb;
-  g.m = (int)m;
-  g.n = (int)n;
+  g.dig = (const uint8_t*)work;
+  g.ex = sa.ex;
+  g.items = nullptr;
+  g.nitems = 1;
+  g.one = OzItem{C, c_rs, c_cs, (int)m, (int)n, 0, same ? 0 : (int)rta, (int)tiles_n, 0};
+  g.ntiles = (int)(rta * tiles_n);
   g.ksteps = (int)ksteps;
-  g.tiles_m = (int)rta;
-  g.tiles_n = (int)tiles_n;
   g.alpha = alpha;
   g.beta = beta;
-  g.c = C;
-  g.c_rs = c_rs;
-  g.c_cs = c_cs;
   g.lower = lower ? 1 : 0;
   g.err = d_err;
-  // persistent: one CTA per SM (the shared memory allows no second), at most one per tile
-  const int64_t tiles = lower ? std::min(rta * tiles_n, rta * (rta * 2 + 1)) : rta * tiles_n;
-  k_oz_gemm<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, ctx->sm_count)), OZ_THREADS, OZ_SMEM, st>>>(g);
-  ctx->launches += 1;
-  FG_CUDA_TRY(cudaGetLastError());
-  return FG_OK;
+  return oz_launch(ctx, st, sa, rta + rtb, g, rta * tiles_n);
+}
+
+// Batch of lower updates C_b -= P_b P_b^T, P_b m_b x k_b (k_b <= 128), all column-major.
+size_t ozaki_syrk_batch_bytes(const std::vector<OzSyrk>& b) {
+  int64_t rt = 0;
+  for (const auto& x : b) rt += rtiles_of(x.m);
+  return (size_t)rt * (128 / OZ_BK) * OZ_A_BYTES + (size_t)rt * OZ_BM * sizeof(int32_t) +
+         b.size() * (sizeof(OzSplit) + sizeof(OzItem)) + 512;
+}
+
+fg_status ozaki_syrk_batch(fg_ctx* ctx, cudaStream_t st, const std::vector<OzSyrk>& b, void* work, size_t bytes,
+                           int* d_err) {
+  std::vector<OzSplit> hs;
+  std::vector<OzItem> hi;
+  int64_t rt = 0, tiles = 0;
+  for (const auto& x : b) {
+    if (x.m <= 0 || x.k <= 0) continue;
+    if (x.k > 128) {
+      set_error("ozaki_syrk_batch: k = %d > 128", x.k);
+      return FG_ERR_UNSUPPORTED;
+    }
+    const int64_t tn = (x.m + OZ_BN - 1) / OZ_BN;
+    hs.push_back(OzSplit{x.p, 1, x.ld, x.m, x.k, (int)rt});
+    hi.push_back(OzItem{x.c, 1, x.ld, x.m, x.m, (int)rt, (int)rt, (int)tn, (int)tiles});
+    rt += rtiles_of(x.m);
+    tiles += rtiles_of(x.m) * tn;
+  }
+  if (hs.empty()) return FG_OK;
+  if (tiles > (1ll << 31) - 1 || ozaki_syrk_batch_bytes(b) > bytes) {
+    set_error("ozaki_syrk_batch: workspace too small or too many tiles");
+    return FG_ERR_UNSUPPORTED;
+  }
+  const int ksteps = 128 / OZ_BK;
+  uint8_t* w = (uint8_t*)work;
+  const size_t dig_bytes = (size_t)rt * ksteps * OZ_A_BYTES;
+  int32_t* ex = (int32_t*)(w + dig_bytes);
+  uint8_t* tail = (uint8_t*)ex + (size_t)rt * OZ_BM * sizeof(int32_t);
+  tail = (uint8_t*)(((uintptr_t)tail + 255) & ~(uintptr_t)255);
+  OzSplit* ds = (OzSplit*)tail;
+  OzItem* di = (OzItem*)(tail + ((hs.size() * sizeof(OzSplit) + 255) / 256) * 256);
+  FG_CUDA_TRY(cudaMemcpyAsync(ds, hs.data(), hs.size() * sizeof(OzSplit), cudaMemcpyHostToDevice, st));
+  FG_CUDA_TRY(cudaMemcpyAsync(di, hi.data(), hi.size() * sizeof(OzItem), cudaMemcpyHostToDevice, st));
+  OzSplitArgs sa;
+  sa.items = ds;
+  sa.nitems = (int)hs.size();
+  sa.none = 0;
+  sa.ksteps = ksteps;
+  sa.dig = (uint4*)w;
+  sa.ex = ex;
+  OzGemmArgs g;
+  g.dig = w;
+  g.ex = ex;
+  g.items = di;
+  g.nitems = (int)hi.size();
+  g.ntiles = (int)tiles;
+  g.ksteps = ksteps;
+  g.alpha = -1.0;
+  g.beta = 1.0;
+  g.lower = 1;
+  g.err = d_err;
+  return oz_launch(ctx, st, sa, rt, g, tiles);
 }
 
 }  // namespace fg

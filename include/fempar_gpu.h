@@ -532,8 +532,9 @@ fg_status fg_server_destroy(fg_server* srv);
  * B n x k, C m x n; element (i, l) of A at A[i*a_rs + l*a_cs] (likewise B, C), device
  * pointers, on the context's stream, synchronous.  B = NULL: B = A (needs n = m).
  * flags: FG_DENSE_LOWER writes only the elements with i >= j.  FP64 is emulated by 7 signed
- * 8-bit digits per value and row (Ozaki scheme); the result is within ~k 2^-51
- * max|A_i.| max|B_j.| of the exact product, like an FP64 dot product.  No counterpart in the
+ * 8-bit digits per value and row (Ozaki scheme) with 56 bits below the row's maximum; the
+ * result is within ~k 2^-53 max|A_i.| max|B_j.| of the exact product (the FP64 dot-product
+ * bound), plus the FP64 rounding of the update.  No counterpart in the
  * reference (its dense factorisations call MKL / PARDISO); the building block of the BDDC
  * set-up's factorisations.  Returns FG_ERR_TIMEOUT if a bounded device wait ran out. */
 #define FG_DENSE_LOWER 1
