@@ -31,8 +31,9 @@
 // digit, 4 KB each, ordered [row tile][K step][digit]; inside a block the rows are in the
 // canonical K-major, non-swizzled UMMA layout: core matrices of 8 rows x 16 bytes, the two
 // 8-column halves 128 B apart (LBO), row groups 256 B apart (SBO).  An operand B tile of 64
-// rows is half a block (2 KB).  A CTA computes one 128 x 64 output tile: warp 0's lane 0
-// streams the digit blocks into shared memory with cp.async.bulk (5 stages, mbarrier
+// rows is half a block (2 KB), of 32 rows a quarter.  A CTA computes 128 x 64 (or 128 x 32)
+// output tiles: warp 0's lane 0 streams the digit blocks into shared memory with
+// cp.async.bulk (5 or 6 stages, mbarrier
 // transaction counts) and issues the MMAs; warps 1-8 read the accumulators (tcgen05.ld, two
 // warps per TMEM lane quarter, 32 columns each) and write C.  CTAs are persistent (one per SM, tiles round robin):
 // the epilogue releases the accumulators before its FP64 writes, which then overlap the next
@@ -42,6 +43,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdint>
 
 #include "fg_internal.h"
@@ -52,18 +54,30 @@ namespace {
 
 constexpr int OZ_S = 7;                       // digits per value
 constexpr int OZ_NACC = 8;                    // accumulators: digit weights k = s + t = 0..7
-constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 16;
+constexpr int OZ_BM = 128, OZ_BK = 16;
 constexpr int OZ_CHUNK = 8;                   // K steps per exact accumulation (K <= 128)
-constexpr int OZ_NBUF = 5;                    // shared-memory stages
 constexpr uint32_t OZ_BLOCK = OZ_BM * OZ_BK * 2;           // one digit block: 4096 B
 constexpr uint32_t OZ_A_BYTES = OZ_S * OZ_BLOCK;           // 28672 B per K step
-constexpr uint32_t OZ_B_BYTES = OZ_S * OZ_BLOCK / 2;       // 14336 B per K step
-constexpr uint32_t OZ_STAGE = OZ_A_BYTES + OZ_B_BYTES;     // 43008 B
-constexpr uint32_t OZ_SMEM = OZ_NBUF * OZ_STAGE;           // 215040 B: one CTA per SM
-constexpr uint32_t OZ_TMEM_COLS = 512;                     // 8 x 64: all of it
+constexpr uint32_t OZ_TMEM_COLS = 512;                     // all of it
 constexpr long long OZ_WAIT_CYCLES = 1ll << 31;            // ~1 s at 2 GHz
-constexpr int OZ_EPI_COLS = 32;                            // columns per epilogue thread
-constexpr int OZ_THREADS = 32 + 4 * 32 * (OZ_BN / OZ_EPI_COLS);  // MMA warp + 8 epilogue warps
+constexpr int OZ_THREADS = 32 + 8 * 32;                    // MMA warp + 8 epilogue warps
+
+// Output tiles of 128 x BN.  BN = 64: the 8 accumulators fill the tensor memory (one set);
+// BN = 32: two sets, so one tile's MMAs run while the epilogue reads the previous tile.
+template <int BN>
+struct OzT {
+  static constexpr int NSET = (int)OZ_TMEM_COLS / (OZ_NACC * BN);
+  static constexpr int EPI = BN / 2;                          // columns per epilogue thread
+  static constexpr int QB = OZ_BM / BN;                       // B tiles per 128-row digit block
+  static constexpr uint32_t B_DIGIT = BN * OZ_BK * 2;         // one digit of a B tile per K step
+  static constexpr uint32_t STAGE = OZ_A_BYTES + OZ_S * B_DIGIT;
+  static constexpr int NBUF = BN == 64 ? 5 : 6;               // stages: 215040 B either way
+  static constexpr uint32_t SMEM = NBUF * STAGE;
+  // kind::f16: FP32 accumulator, bf16 A and B, both K-major, N = BN, M = 128
+  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                    ((uint32_t)(OZ_BM >> 4) << 24);
+};
+constexpr int OZ_MAXBUF = 6;
 
 // ---- PTX wrappers -------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -124,9 +138,6 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(256u >> 4) << 32) |
          (1ull << 46);
 }
-// Instruction descriptor, kind::f16: FP32 accumulator, bf16 A and B, both K-major, N = 64, M = 128.
-constexpr uint32_t OZ_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
-                              ((uint32_t)(OZ_BM >> 4) << 24);
 
 // bounded wait; false (and the CTA's abort flag and the error status set) when it runs out
 __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err) {
@@ -336,9 +347,12 @@ __device__ __noinline__ double scale_slow(double d, int off) { return ldexp(d, o
 // Persistent: CTA b takes the output tiles b, b + gridDim.x, ... of all items (tiles above
 // the diagonal skipped when lower).  The accumulators are released as soon as the epilogue
 // has read them, so the next tile's MMAs run while the epilogue writes C.
+template <int BN>
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
+  using T = OzT<BN>;
+  constexpr int OZ_NBUF = T::NBUF;
   extern __shared__ __align__(1024) uint8_t oz_smem[];
-  __shared__ __align__(8) uint64_t bar_full[OZ_NBUF], bar_empty[OZ_NBUF], bar_acc_full, bar_acc_empty;
+  __shared__ __align__(8) uint64_t bar_full[OZ_MAXBUF], bar_empty[OZ_MAXBUF], bar_acc_full[2], bar_acc_empty[2];
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
 
@@ -349,7 +363,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
     if (!g.lower) return true;
     const OzItem it = item_of(g, t);
     const int lt = t - it.tile0;
-    return (lt % it.tiles_n) * OZ_BN <= (lt / it.tiles_n) * OZ_BM + OZ_BM - 1;
+    return (lt % it.tiles_n) * BN <= (lt / it.tiles_n) * OZ_BM + OZ_BM - 1;
   };
   auto next_tile = [&](int t) {
     for (t += gridDim.x; t < ntiles && !valid(t); t += gridDim.x) {
@@ -369,8 +383,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
         mbar_init(smem_u32(&bar_full[i]), 1);
         mbar_init(smem_u32(&bar_empty[i]), 1);
       }
-      mbar_init(smem_u32(&bar_acc_full), 1);
-      mbar_init(smem_u32(&bar_acc_empty), OZ_THREADS - 32);
+      for (int z = 0; z < 2; ++z) {
+        mbar_init(smem_u32(&bar_acc_full[z]), 1);
+        mbar_init(smem_u32(&bar_acc_empty[z]), OZ_THREADS - 32);
+      }
       abort_flag = 0;
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -393,7 +409,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
         const OzItem it = item_of(g, pt);
         const int lt = pt - it.tile0, rt = lt / it.tiles_n, ct = lt % it.tiles_n;
         pa = g.dig + (size_t)(it.arow0 + rt) * KS * OZ_A_BYTES;
-        pb = g.dig + (size_t)(it.brow0 + (ct >> 1)) * KS * OZ_A_BYTES + (size_t)(ct & 1) * (OZ_BLOCK / 2);
+        pb = g.dig + (size_t)(it.brow0 + ct / T::QB) * KS * OZ_A_BYTES + (size_t)(ct % T::QB) * T::B_DIGIT;
       };
       locate();
       auto produce = [&]() -> bool {
@@ -402,12 +418,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
         if (pgs >= OZ_NBUF && !mbar_wait(smem_u32(&bar_empty[buf]), ((pgs / OZ_NBUF) - 1) & 1, &abort_flag, g.err))
           return false;
         const uint32_t full = smem_u32(&bar_full[buf]);
-        const uint32_t dst = sbase + buf * OZ_STAGE;
-        mbar_expect_tx(full, OZ_STAGE);
+        const uint32_t dst = sbase + buf * T::STAGE;
+        mbar_expect_tx(full, T::STAGE);
         bulk_g2s(dst, pa + (size_t)pks * OZ_A_BYTES, OZ_A_BYTES, full);
         for (int t = 0; t < OZ_S; ++t)
-          bulk_g2s(dst + OZ_A_BYTES + t * (OZ_BLOCK / 2), pb + ((size_t)pks * OZ_S + t) * OZ_BLOCK, OZ_BLOCK / 2,
-                   full);
+          bulk_g2s(dst + OZ_A_BYTES + t * T::B_DIGIT, pb + ((size_t)pks * OZ_S + t) * OZ_BLOCK, T::B_DIGIT, full);
         ++pgs;
         if (++pks == KS) {
           pks = 0;
@@ -423,7 +438,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
         for (int ks = 0; ks < KS && ok; ++ks) {
           const int kin = ks % OZ_CHUNK;
           const int buf = gs % OZ_NBUF;
-          if (kin == 0 && gc > 0 && !mbar_wait(smem_u32(&bar_acc_empty), (gc - 1) & 1, &abort_flag, g.err)) {
+          const int z = gc % T::NSET;  // accumulator set of this chunk
+          if (kin == 0 && gc >= T::NSET &&
+              !mbar_wait(smem_u32(&bar_acc_empty[z]), ((gc / T::NSET) - 1) & 1, &abort_flag, g.err)) {
             ok = false;
             break;
           }
@@ -432,19 +449,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
             break;
           }
           tc_fence_after();
-          const uint32_t sa = sbase + buf * OZ_STAGE, sb = sa + OZ_A_BYTES;
+          const uint32_t sa = sbase + buf * T::STAGE, sb = sa + OZ_A_BYTES;
           const uint64_t da = smem_desc(sa), db = smem_desc(sb);
+          const uint32_t tacc = tmem + z * (OZ_NACC * BN);
 #pragma unroll
           for (int kk = 0; kk < OZ_NACC; ++kk)
 #pragma unroll
             for (int s = (kk > OZ_S - 1 ? kk - (OZ_S - 1) : 0); s <= (kk < OZ_S - 1 ? kk : OZ_S - 1); ++s)
               // start-address field in 16-byte units; the first pair of a class starts the chunk's sum
-              tc_mma(tmem + kk * OZ_BN, da + (uint64_t)(s * (OZ_BLOCK >> 4)),
-                     db + (uint64_t)((kk - s) * (OZ_BLOCK >> 5)), OZ_IDESC,
+              tc_mma(tacc + kk * BN, da + (uint64_t)(s * (OZ_BLOCK >> 4)),
+                     db + (uint64_t)((kk - s) * (T::B_DIGIT >> 4)), T::IDESC,
                      (kin > 0 || s > (kk > OZ_S - 1 ? kk - (OZ_S - 1) : 0)) ? 1u : 0u);
           tc_commit(smem_u32(&bar_empty[buf]));
           if (kin == OZ_CHUNK - 1 || ks == KS - 1) {
-            tc_commit(smem_u32(&bar_acc_full));
+            tc_commit(smem_u32(&bar_acc_full[z]));
             ++gc;
           }
           ++gs;
@@ -455,10 +473,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
     __syncwarp();
   } else {
     // epilogue: warps 1-8; warp w reads TMEM lanes 32 (w % 4) .. +31 (tile rows), columns
-    // 32 h .. 32 h + 31 with h = (w - 1) / 4
+    // EPI h .. EPI h + EPI - 1 with h = (w - 1) / 4
+    constexpr int OZ_EPI_COLS = T::EPI;
     const int quarter = warp & 3, half = (warp - 1) >> 2;
     const int row = quarter * 32 + lane;
-    const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + half * OZ_EPI_COLS;
+    const uint32_t trow0 = tmem + ((uint32_t)(quarter * 32) << 16) + half * OZ_EPI_COLS;
     // alpha, beta cases as integers, decided once (an FP64 compare per element would cost as
     // much as the element's arithmetic)
     const int amode = g.alpha == -1.0 ? 0 : (g.alpha == 1.0 ? 1 : 2);
@@ -471,11 +490,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
       for (int j = 0; j < OZ_EPI_COLS; ++j) acc[j] = 0.0;
       bool ok = true;
       for (int chunk = 0; chunk < nchunks; ++chunk, ++gc) {
-        if (!mbar_wait(smem_u32(&bar_acc_full), gc & 1, &abort_flag, g.err)) {
+        const int z = gc % T::NSET;
+        if (!mbar_wait(smem_u32(&bar_acc_full[z]), (gc / T::NSET) & 1, &abort_flag, g.err)) {
           ok = false;
           break;
         }
         tc_fence_after();
+        const uint32_t trow = trow0 + z * (OZ_NACC * BN);
 #pragma unroll
         for (int cb = 0; cb < OZ_EPI_COLS / 8; ++cb) {
           // sum_k v_k 2^(-8k) exactly: every v_k is an integer below 2^24 held in FP32; hi in
@@ -486,7 +507,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
           for (int part = 0; part < 2; ++part) {
             uint32_t v[OZ_NACC / 2][8];
 #pragma unroll
-            for (int q = 0; q < OZ_NACC / 2; ++q) tc_ld8(trow + (part * 4 + q) * OZ_BN + cb * 8, v[q]);
+            for (int q = 0; q < OZ_NACC / 2; ++q) tc_ld8(trow + (part * 4 + q) * BN + cb * 8, v[q]);
             tc_wait_ld();
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -513,7 +534,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
           }
         }
         tc_fence_before();
-        mbar_arrive(smem_u32(&bar_acc_empty));  // accumulators free: the next MMAs may start
+        mbar_arrive(smem_u32(&bar_acc_empty[z]));  // accumulators free: the next MMAs may start
       }
       if (!ok) break;
       const OzItem it = item_of(g, t);
@@ -521,9 +542,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
       const int i = rt * OZ_BM + row;
       const bool row_ok = i < it.m;
       const int ei = g.ex[(int64_t)(it.arow0 + rt) * OZ_BM + row];
-      const int c0 = ct * OZ_BN + half * OZ_EPI_COLS;
-      // lane j holds the exponent of column c0 + j (padding rows of the exponents are 0)
-      const int ecol = g.ex[(int64_t)(it.brow0 + (ct >> 1)) * OZ_BM + (ct & 1) * OZ_BN + half * OZ_EPI_COLS + lane];
+      const int c0 = ct * BN + half * OZ_EPI_COLS;
+      // lane j < EPI holds the exponent of column c0 + j (padding rows of the exponents are 0)
+      const int ecol = g.ex[(int64_t)(it.brow0 + ct / T::QB) * OZ_BM + (ct % T::QB) * BN + half * OZ_EPI_COLS +
+                            (lane < OZ_EPI_COLS ? lane : 0)];
       double* crow = it.c + (int64_t)i * it.c_rs;
 #pragma unroll
       for (int j0 = 0; j0 < OZ_EPI_COLS; j0 += 8) {
@@ -582,13 +604,30 @@ size_t ozaki_workspace_bytes(int64_t m, int64_t n, int64_t k, bool same) {
   return (size_t)rt * ks * OZ_A_BYTES + (size_t)rt * OZ_BM * sizeof(int32_t) + 256;
 }
 
+// output tile width: 64 (default) or 32 (FG_OZ_BN=32: two accumulator sets)
+static int oz_bn() {
+  static const int bn = [] {
+    const char* e = std::getenv("FG_OZ_BN");
+    return (e && std::atoi(e) == 32) ? 32 : 64;
+  }();
+  return bn;
+}
+
+template <int BN>
+static fg_status oz_gemm_launch(fg_ctx* ctx, cudaStream_t st, OzGemmArgs& g, int64_t ntiles) {
+  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_oz_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)OzT<BN>::SMEM));
+  // persistent: one CTA per SM (the shared memory allows no second), at most one per tile
+  k_oz_gemm<BN><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, ctx->sm_count)), OZ_THREADS,
+                  OzT<BN>::SMEM, st>>>(g);
+  return FG_OK;
+}
+
 static fg_status oz_launch(fg_ctx* ctx, cudaStream_t st, OzSplitArgs& sa, int64_t rtiles, OzGemmArgs& g,
                            int64_t ntiles) {
-  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM));
   k_oz_rowexp<<<dim3((unsigned)rtiles, 32), OZ_BM, 0, st>>>(sa);
   k_oz_split<<<dim3((unsigned)rtiles, (unsigned)sa.ksteps), OZ_BM, 0, st>>>(sa);
-  // persistent: one CTA per SM (the shared memory allows no second), at most one per tile
-  k_oz_gemm<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, ctx->sm_count)), OZ_THREADS, OZ_SMEM, st>>>(g);
+  FG_TRY(oz_bn() == 32 ? oz_gemm_launch<32>(ctx, st, g, ntiles) : oz_gemm_launch<64>(ctx, st, g, ntiles));
   ctx->launches += 3;
   FG_CUDA_TRY(cudaGetLastError());
   return FG_OK;
@@ -610,7 +649,7 @@ fg_status ozaki_gemm_nt(fg_ctx* ctx, cudaStream_t st, int64_t m, int64_t n, int6
   const bool same = B == nullptr;
   const int64_t ksteps = (k + OZ_BK - 1) / OZ_BK;
   const int64_t rta = rtiles_of(m), rtb = same ? 0 : rtiles_of(n);
-  const int64_t tiles_n = (n + OZ_BN - 1) / OZ_BN;
+  const int64_t tiles_n = (n + oz_bn() - 1) / oz_bn();
   if (rta * tiles_n > (1ll << 31) - 1 || rta + rtb > (1ll << 31) - 1 || ksteps > 65535) {
     set_error("ozaki_gemm_nt: %lld x %lld x %lld is too large", (long long)m, (long long)n, (long long)k);
     return FG_ERR_UNSUPPORTED;
@@ -658,7 +697,7 @@ fg_status ozaki_syrk_batch(fg_ctx* ctx, cudaStream_t st, const std::vector<OzSyr
       set_error("ozaki_syrk_batch: k = %d > 128", x.k);
       return FG_ERR_UNSUPPORTED;
     }
-    const int64_t tn = (x.m + OZ_BN - 1) / OZ_BN;
+    const int64_t tn = (x.m + oz_bn() - 1) / oz_bn();
     hs.push_back(OzSplit{x.p, 1, x.ld, x.m, x.k, (int)rt});
     hi.push_back(OzItem{x.c, 1, x.ld, x.m, x.m, (int)rt, (int)rt, (int)tn, (int)tiles});
     rt += rtiles_of(x.m);
