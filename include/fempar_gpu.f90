@@ -152,5 +152,14 @@ module fempar_gpu_names
       import; integer(c_int32_t) :: fg_system_spmv_device_noalloc
       type(c_ptr), value :: sys, x, y; integer(c_int), value :: precision
     end function
+    ! C = alpha A B^T + beta C on device arrays, FP64 emulated on the tensor cores; A(i,l) at
+    ! A[i*a_rs + l*a_cs] (column-major: a_rs = 1, a_cs = lda); b = c_null_ptr: B = A
+    function fg_dense_gemm_nt(ctx, m, n, k, alpha, a, a_rs, a_cs, b, b_rs, b_cs, beta, c, c_rs, c_cs, flags) &
+        bind(c, name="fg_dense_gemm_nt")
+      import; integer(c_int32_t) :: fg_dense_gemm_nt
+      type(c_ptr), value :: ctx, a, b, c
+      integer(c_int64_t), value :: m, n, k, a_rs, a_cs, b_rs, b_cs, c_rs, c_cs
+      real(c_double), value :: alpha, beta; integer(c_int32_t), value :: flags
+    end function
   end interface
 end module fempar_gpu_names

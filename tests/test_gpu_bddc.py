@@ -6,7 +6,9 @@ Bar:
   * apply with the FP32 factors: <= 1e-4;
   * BDDC-PCG: iteration count within 1 of the oracle's, solution within 1e-9 of the
     oracle's Jacobi-PCG solution at rtol 1e-12;
-  * mixed-precision BDDC-PCG to 1e-8: converged, error vs the FP64 solve <= 1e-7.
+  * mixed-precision BDDC-PCG (FP32 factors, FP64 Krylov vectors): to 1e-8 converged, error
+    <= 1e-7; to 1e-12 within 1e-9 of the oracle's solution, like the FP64 solve (the FP32
+    preconditioner costs iterations, not attainable accuracy).
 """
 import numpy as np
 import pytest
@@ -131,6 +133,10 @@ def test_bddc_pcg_matches_oracle(fg, ctx, case):
     assert sm.info()["converged"]
     assert sm.info()["iterations"] <= inf["iterations"] + 2
     assert np.linalg.norm(xm - ref["x"]) <= 1e-7 * np.linalg.norm(ref["x"])
+    sm.set_parameters_from_pl({"ILS_RTOL": 1e-12, "ILS_MAX_NUM_ITERATIONS": 2000})
+    xm12 = sm.solve()
+    assert sm.info()["converged"]
+    assert np.linalg.norm(xm12 - ref["x"]) <= 1e-9 * np.linalg.norm(ref["x"])
     M.close()
 
 
@@ -186,6 +192,11 @@ def test_bddc_elasticity_handler_matches_oracle(fg, ctx, case):
     xm = sm.solve()
     assert sm.info()["converged"]
     assert np.linalg.norm(xm - ref["x"]) <= 1e-6 * np.linalg.norm(ref["x"])
+    # to 1e-12 the FP32 preconditioner reaches the FP64 solution
+    sm.set_parameters_from_pl({"ILS_RTOL": 1e-12, "ILS_MAX_NUM_ITERATIONS": 2000})
+    xm12 = sm.solve()
+    assert sm.info()["converged"]
+    assert np.linalg.norm(xm12 - ref["x"]) <= 1e-9 * np.linalg.norm(ref["x"])
     M.close()
 
 
