@@ -27,6 +27,10 @@
 //   s = z - L_V^T u_V,  mu = S_e^-1 (L_e s - u_e + C_eV u_V),  w_r = L^-T (s - L_e^T mu),  w_V = u_V
 // (C_eV, the constraint weights on vertex dofs, is zero for the standard handler's averages
 // and nonzero for the elasticity handler's face functionals.)
+// Without primal vertices (use_vertices = 0, nV = 0) the constraints are added to the local
+// matrix as an augmented Lagrangian, K + C^T R C (k_bddc_augment): same constrained
+// solutions, an SPD leading block for floating subdomains; K_Pi = S~^-1 - R and the backward
+// solve gains L_e^T R u_e.
 // (u = the coarse solution restricted to the subdomain).  The coarse matrix is inverted
 // by the same partial Cholesky on [[K_c, I], [I, 0]] whose trailing block is -K_c^-1.
 #include <algorithm>
@@ -36,6 +40,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <numeric>
 #include <utility>
 #include <vector>
 
@@ -105,6 +110,7 @@ struct fg_bddc {
   bool stepped = false;        // factorise panel step by panel step over all subdomains
   bool coarse_emulated = false; // coarse trailing updates on the tensor cores (last setup)
   bool local_emulated = false;  // subdomain trailing updates on the tensor cores (last setup)
+  double* dRho = nullptr;       // use_vertices = 0: augmentation weights R_e at poff + nV + e
   int64_t* dIptr = nullptr;
   int64_t* dIsrc = nullptr;
   int32_t* dIvec = nullptr;
@@ -301,6 +307,53 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Without primal vertices (use_vertices = 0) a floating subdomain's K_rr is singular.  The
+// constrained Neumann problem [K C^T; C 0][w; mu] = [g; h] has the same solution as
+// [K + C^T R C, C^T; C 0][w; mu] = [g + C^T R h; h] for any diagonal R > 0, and K + C^T R C
+// is SPD once the constraints fix K's kernel.  R_e = mean(diag K_EE) / |c_e|^2 (the scale of
+// K on the constraint's direction).  The local coarse matrix becomes S~^-1 - R and the
+// backward apply adds L_e^T R u_e (k_bddc_coarse_local, k_bddc_neumann_bwd).  Entries are
+// grouped by row; rows are added one after another (each (i, j) once per row): deterministic.
+__global__ void __launch_bounds__(256)
+    k_bddc_augment(const BSub* __restrict__ subs, const int32_t* __restrict__ qrow, const int32_t* __restrict__ qcol,
+                   const double* __restrict__ qw, double* __restrict__ A, double* __restrict__ rho) {
+  const BSub S = subs[blockIdx.x];
+  double* As = A + S.aoff;
+  const int64_t N = S.N;
+  __shared__ double red[256];
+  __shared__ int rs[kMaxNe + 1];
+  double d = 0.0;
+  for (int k = threadIdx.x; k < S.nE; k += blockDim.x) d += As[(S.nI + k) + (int64_t)(S.nI + k) * N];
+  red[threadIdx.x] = d;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double dbar = S.nE > 0 ? red[0] / S.nE : 1.0;
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int e = 0; e <= S.ne; ++e) {
+      while (t < S.nq && qrow[S.qoff + t] < e) ++t;
+      rs[e] = t;
+    }
+  }
+  __syncthreads();
+  for (int e = 0; e < S.ne; ++e) {
+    const int t0 = rs[e], len = rs[e + 1] - rs[e];
+    double nrm = 0.0;
+    for (int t = 0; t < len; ++t) nrm += qw[S.qoff + t0 + t] * qw[S.qoff + t0 + t];
+    const double re = nrm > 0.0 ? dbar / nrm : 0.0;
+    if (threadIdx.x == 0) rho[S.poff + S.nV + e] = re;
+    for (int64_t pq = threadIdx.x; pq < (int64_t)len * len; pq += blockDim.x) {
+      const int a = (int)(pq / len), b = (int)(pq - (int64_t)a * len);
+      const int ca = qcol[S.qoff + t0 + a], cb = qcol[S.qoff + t0 + b];
+      if (ca >= cb) As[ca + (int64_t)cb * N] += re * qw[S.qoff + t0 + a] * qw[S.qoff + t0 + b];
+    }
+    __syncthreads();
+  }
+}
+
 // Interface weights: multiplicity (1 / subdomains around) or diag(A_i) / sum_j diag(A_j);
 // one thread per global interface dof, contributions in subdomain order.
 __global__ void k_bddc_weights(int64_t nG, const int64_t* __restrict__ iptr, const int64_t* __restrict__ isrc,
@@ -389,7 +442,7 @@ __global__ void __launch_bounds__(256) k_bstep_syrk_panel(const BSub* __restrict
 // Local coarse matrix K_Pi (order [V | e]), S_e^-1 and H = S_e^-1 T from the trailing block.
 __global__ void __launch_bounds__(128)
     k_bddc_coarse_local(const BSub* __restrict__ subs, const double* __restrict__ A, double* __restrict__ Kp,
-                        double* __restrict__ G, float* __restrict__ G32, int* err) {
+                        double* __restrict__ G, float* __restrict__ G32, const double* __restrict__ rho, int* err) {
   // dynamic shared memory: Se, Gi (kMaxNe x (kMaxNe+1)), T, H (kMaxNe x kMaxNv)
   extern __shared__ __align__(16) unsigned char smraw[];
   auto Se = reinterpret_cast<double(*)[kMaxNe + 1]>(smraw);
@@ -473,6 +526,7 @@ __global__ void __launch_bounds__(128)
       v = H[j - nV][i];
     } else {
       v = Gi[i - nV][j - nV];
+      if (rho && i == j) v -= rho[S.poff + i];  // augmented: Phi^T K Phi = S~^-1 - R
     }
     K[t] = v;
   }
@@ -750,7 +804,7 @@ __global__ void __launch_bounds__(256)
     k_bddc_neumann_bwd(const BSub* __restrict__ subs, const double* __restrict__ A, const float* __restrict__ F,
                        const T* __restrict__ R, const T* __restrict__ G, const T* __restrict__ Cv,
                        const int32_t* __restrict__ pc, const T* __restrict__ uc, const T* __restrict__ zE,
-                       const double* __restrict__ w, T* __restrict__ contrib) {
+                       const double* __restrict__ w, const double* __restrict__ rho, T* __restrict__ contrib) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* x = reinterpret_cast<T*>(smraw);
   __shared__ T uP[kMaxNv + kMaxNe], cm[kMaxNe], mu[kMaxNe];
@@ -764,6 +818,8 @@ __global__ void __launch_bounds__(256)
   for (int i = threadIdx.x; i < nr; i += blockDim.x) {
     T s = i < nI ? T(0) : zE[S.eoff + (i - nI)];
     for (int v = 0; v < nV; ++v) s -= Rs[(int64_t)v * nr + i] * uP[v];
+    if (rho)  // augmented: the right-hand side gains C^T R u_e, i.e. s gains L_e^T R u_e
+      for (int k = 0; k < ne; ++k) s += Rs[(int64_t)(nV + k) * nr + i] * (T)rho[S.poff + nV + k] * uP[nV + k];
     x[i] = s;
   }
   __syncthreads();
@@ -1152,7 +1208,9 @@ static fg_status bddc_symbolic(fg_bddc* B) {
               uint64_t key = 0;
               if (ncut > 0) {
                 if (npl == 3) {
-                  cls = 2;
+                  // a vertex: primal (V), or with use_vertices = 0 an interface dof without a
+                  // coarse dof of its own
+                  cls = B->prm.use_vertices ? 2 : 1;
                   key = enc(0, 0, X, Y, Z);
                 } else if (ncut == 2) {
                   cls = 1;
@@ -1250,6 +1308,21 @@ static fg_status bddc_symbolic(fg_bddc* B) {
           for (size_t f = 0; f < rfaces.size(); ++f)
             face_functionals(rfaces[f], (int)(6 * f), B->cuts, S.c0, S.c1, lo, bn, me->n, p, nc, xyz,
                              h_box.data() + b0, h_qrow, h_qcol, h_qw);
+        }
+        {  // entries grouped by constraint row (the augmentation takes them row by row)
+          std::vector<int64_t> ord((int64_t)h_qrow.size() - q0);
+          std::iota(ord.begin(), ord.end(), q0);
+          std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return h_qrow[a] < h_qrow[b]; });
+          std::vector<int32_t> r2(ord.size()), c2(ord.size());
+          std::vector<double> w2(ord.size());
+          for (size_t t = 0; t < ord.size(); ++t) {
+            r2[t] = h_qrow[ord[t]];
+            c2[t] = h_qcol[ord[t]];
+            w2[t] = h_qw[ord[t]];
+          }
+          std::copy(r2.begin(), r2.end(), h_qrow.begin() + q0);
+          std::copy(c2.begin(), c2.end(), h_qcol.begin() + q0);
+          std::copy(w2.begin(), w2.end(), h_qw.begin() + q0);
         }
         S.qoff = q0;
         S.nq = (int)((int64_t)h_qrow.size() - q0);
@@ -1437,6 +1510,7 @@ static fg_status bddc_symbolic(fg_bddc* B) {
   FG_TRY(balloc_n(B, &B->dFp, B->nP));
   FG_TRY(balloc_n(B, &B->dFp32, B->nP));
   FG_TRY(balloc_n(B, &B->dKp, B->nK));
+  if (!B->prm.use_vertices) FG_TRY(balloc_n(B, &B->dRho, std::max<int64_t>(B->nP, 1), true));
   FG_TRY(balloc_n(B, &B->dG, B->nG));
   FG_TRY(balloc_n(B, &B->dG32, B->nG));
   FG_TRY(balloc_n(B, &B->dKc, 4 * B->nC * B->nC));
@@ -1544,6 +1618,10 @@ static fg_status bddc_numeric(fg_bddc* B) {
   k_bddc_assemble<<<ns, 256, 0, st>>>(B->d_subs, sys->d_elmat, sp->mesh->n[0], sp->mesh->n[1], sp->order, sp->tab.nn,
                                       sp->tab.nd, sp->ncomp, B->dBox, B->dQrow, B->dQcol, B->dQw, B->dA,
                                       B->dDiag);
+  if (B->dRho) {
+    k_bddc_augment<<<ns, 256, 0, st>>>(B->d_subs, B->dQrow, B->dQcol, B->dQw, B->dA, B->dRho);
+    ctx->launches += 1;
+  }
   if (B->nIface > 0)
     k_bddc_weights<<<nblk(B->nIface, 256), 256, 0, st>>>(B->nIface, B->dIptr, B->dIsrc, B->dDiag,
                                                          B->prm.weighting == FG_BDDC_WEIGHT_STIFFNESS, B->dW);
@@ -1639,7 +1717,8 @@ static fg_status bddc_numeric(fg_bddc* B) {
   B->factor_ms = fms;
   FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_bddc_coarse_local, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kCoarseLocalSmem));
-  k_bddc_coarse_local<<<ns, 128, kCoarseLocalSmem, st>>>(B->d_subs, B->dA, B->dKp, B->dG, B->dG32, B->dErr);
+  k_bddc_coarse_local<<<ns, 128, kCoarseLocalSmem, st>>>(B->d_subs, B->dA, B->dKp, B->dG, B->dG32, B->dRho,
+                                                          B->dErr);
   k_bddc_panels<<<ns, 256, 0, st>>>(B->d_subs, B->dA, B->dF, B->dR, B->dR32);
   ctx->launches += 2;
   FG_CUDA_TRY(cudaGetLastError());
@@ -1734,7 +1813,8 @@ static fg_status bddc_apply_layout(fg_bddc* B, const double* r, double* z) {
     ctx->launches += 2;
   }
   const T* Cv = f32 ? (const T*)B->dCv32 : (const T*)B->dCv;
-  k_bddc_neumann_bwd<T><<<ns, 256, smR, st>>>(B->d_subs, B->dA, B->dF, R, G, Cv, B->dPc, uc, zE, B->dW, contrib);
+  k_bddc_neumann_bwd<T><<<ns, 256, smR, st>>>(B->d_subs, B->dA, B->dF, R, G, Cv, B->dPc, uc, zE, B->dW, B->dRho,
+                                              contrib);
   if (B->nIface > 0)
     k_iface_sum<T><<<nblk(B->nIface, 256), 256, 0, st>>>(B->nIface, B->dIptr, B->dIsrc, B->dIvec, contrib, v, z);
   // 5. harmonic extension
@@ -1946,8 +2026,8 @@ fg_status fg_bddc_create(fg_system* sys, const fg_bddc_params* prm, fg_bddc** ou
     set_error("BDDC: box subdomains are built for continuous spaces on structured meshes only");
     return FG_ERR_UNSUPPORTED;
   }
-  if (!prm->use_vertices) {
-    set_error("BDDC: vertex dofs are always primal here (use_vertices must be 1)");
+  if (!prm->use_vertices && !prm->use_edges && !prm->use_faces) {
+    set_error("BDDC: no coarse constraints (use_vertices, use_edges and use_faces all 0)");
     return FG_ERR_UNSUPPORTED;
   }
   if (prm->weighting != FG_BDDC_WEIGHT_MULTIPLICITY && prm->weighting != FG_BDDC_WEIGHT_STIFFNESS)

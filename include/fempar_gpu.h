@@ -369,9 +369,11 @@ fg_status fg_partition_solve(fg_partition* partition, fg_system* subassembled, c
  * component with per-component averages as constraints (:121-219), multiplicity weights
  * (:221-295).  The subdomain and coarse matrices are factorised by FP64 Cholesky on the
  * device (the reference calls a sparse direct solver).  Objects come from the box grid:
- * interface nodes on slab planes in all three directions are vertices (they are always
- * primal: use_vertices must be 1), nodes on two interior cut planes edge points, on one
- * a face point.  Subdomain matrices are dense: the library refuses (FG_ERR_OOM) a
+ * interface nodes on slab planes in all three directions are vertices (primal, or with
+ * use_vertices = 0 interface dofs without coarse dofs: the constrained Neumann problems are
+ * then solved with the constraints added to the local matrix as an augmented Lagrangian,
+ * which leaves the operator unchanged), nodes on two interior cut planes edge points, on
+ * one a face point.  Subdomain matrices are dense: the library refuses (FG_ERR_OOM) a
  * partition whose dense local matrices do not fit the context's HBM budget. */
 typedef struct fg_bddc fg_bddc;
 enum { FG_PREC_BDDC = 2 };
@@ -391,7 +393,7 @@ typedef struct {
   int32_t nsub[3];         /* subdomains per direction                                     */
   const int32_t* cuts;     /* NULL: even split; else nsub[0]+1, nsub[1]+1, nsub[2]+1 increasing
                               cell indices per direction, from 0 to n[d]                   */
-  int32_t use_vertices;    /* coarse_space_use_vertices (must be 1)                       */
+  int32_t use_vertices;    /* coarse_space_use_vertices                                     */
   int32_t use_edges;       /* coarse_space_use_edges                                       */
   int32_t use_faces;       /* coarse_space_use_faces                                       */
   int32_t weighting;       /* FG_BDDC_WEIGHT_MULTIPLICITY (reference standard handler) or

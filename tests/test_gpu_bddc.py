@@ -200,6 +200,59 @@ def test_bddc_elasticity_handler_matches_oracle(fg, ctx, case):
     M.close()
 
 
+NOVERTEX_CASES = [
+    # n, order, kind, dirichlet, nsub, jitter, edges, faces, weighting, handler: no primal
+    # vertices (the reference test's coarse_space_use_vertices = .false.); the centre
+    # subdomains of the first case touch no Dirichlet boundary (floating)
+    ((6, 6, 6), 1, O.POISSON, "all", (3, 3, 3), 0.0, True, True, WEIGHT_STIFFNESS, 0),
+    ((6, 5, 4), 2, O.POISSON, "all", (3, 2, 2), 0.3, False, True, WEIGHT_MULTIPLICITY, 0),
+    ((6, 4, 4), 1, O.ELASTICITY, "clamp", (3, 2, 2), 0.2, True, True, WEIGHT_STIFFNESS, 0),
+    ((6, 4, 4), 2, O.ELASTICITY, "clamp", (3, 2, 2), 0.0, False, True, WEIGHT_STIFFNESS, 1),
+]
+
+
+@pytest.mark.parametrize("case", NOVERTEX_CASES)
+def test_bddc_without_primal_vertices_matches_oracle(fg, ctx, case):
+    """use_vertices = 0: the device adds the constraints to the local matrices as an augmented
+    Lagrangian (the same constrained Neumann solutions); the oracle solves the saddle-point
+    systems directly.  Same coarse space, applies within 1e-10 (FP32 factors: 1e-4), PCG
+    iteration counts within 2 at 1e-10, solutions within 1e-9 of the oracle's Jacobi-PCG."""
+    import torch
+    n, order, kind, ids, nsub, jitter, edges, faces, wt, handler = case
+    P, keep, op, ncomp = pair(fg, ctx, n, order, kind, ids_of(ids))
+    cuts = fg.bddc_cuts(n, nsub, jitter=jitter, seed=7)
+    Bo = BDDCOracle(P, n, order, ncomp, cuts, use_vertices=False, use_edges=edges, use_faces=faces, weighting=wt,
+                    coarse_handler=HANDLER_ELASTICITY if handler else 0,
+                    vertex_xyz=perturbed(n, 0.15, 3) if handler else None)
+    M = fg.MLBDDC(op, nsub=nsub, cuts=cuts, use_vertices=False, use_edges=edges, use_faces=faces, weighting=wt,
+                  coarse_handler=fg.FG_BDDC_HANDLER_ELASTICITY if handler else fg.FG_BDDC_HANDLER_STANDARD)
+    assert M.info()["num_coarse_dofs"] == Bo.ncoarse
+    rng = np.random.default_rng(5)
+    dev = f"cuda:{ctx.device}"
+    for k in range(2):
+        r = rng.normal(size=P.nfree)
+        zo = Bo.apply(r)
+        rt = torch.tensor(r, device=dev)
+        z = torch.zeros_like(rt)
+        M.apply_device(rt, z)
+        err = np.linalg.norm(z.cpu().numpy() - zo) / np.linalg.norm(zo)
+        assert err <= 1e-10, err
+        z32 = torch.zeros_like(rt)
+        M.apply_device(rt, z32, precision=fg.FG_MIXED)
+        assert np.linalg.norm(z32.cpu().numpy() - zo) <= 1e-4 * np.linalg.norm(zo)
+    xo, ito, oko = Bo.pcg(P, P.rhs(), rtol=1e-10, maxit=1000)
+    ref = P.cg(precond=1, rtol=1e-13, maxit=100000)
+    s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, M)
+    s.set_parameters_from_pl({"ILS_RTOL": 1e-12, "ILS_MAX_NUM_ITERATIONS": 1000})
+    x = s.solve()
+    assert s.info()["converged"] and oko
+    s.set_parameters_from_pl({"ILS_RTOL": 1e-10, "ILS_MAX_NUM_ITERATIONS": 1000})
+    s.solve()
+    assert abs(s.info()["iterations"] - ito) <= 2, (s.info()["iterations"], ito)
+    assert np.linalg.norm(x - ref["x"]) <= 1e-9 * np.linalg.norm(ref["x"])
+    M.close()
+
+
 def test_bddc_elasticity_handler_rejects(fg, ctx):
     from fempar_gb300 import FGError
     P, keep, op, ncomp = pair(fg, ctx, (4, 4, 4), 1, O.ELASTICITY, CLAMP)
@@ -245,8 +298,8 @@ def test_bddc_reassembly_refreshes_numerical_setup(fg, ctx):
 def test_bddc_rejects_bad_parameters(fg, ctx):
     from fempar_gb300 import FGError
     P, keep, op, ncomp = pair(fg, ctx, (4, 4, 2), 1, O.POISSON, list(range(1, 27)))
-    with pytest.raises(FGError):
-        fg.MLBDDC(op, nsub=(2, 2, 2), use_vertices=False)
+    with pytest.raises(FGError):  # no coarse constraints at all
+        fg.MLBDDC(op, nsub=(2, 2, 2), use_vertices=False, use_edges=False, use_faces=False)
     with pytest.raises(FGError):
         fg.MLBDDC(op, nsub=(5, 1, 1))
     with pytest.raises(FGError):
