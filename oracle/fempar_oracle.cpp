@@ -698,9 +698,12 @@ void build_mesh_and_dofs(orc_problem& P) {
     }
     P.nfree = cur;
   }
-  // (3) nodal interpolation of the Dirichlet data (sbm_serial_fe_space.i90:997-1176)
+  // (3) nodal interpolation of the Dirichlet data (sbm_serial_fe_space.i90:997-1176); a vector
+  // field takes the function's value for every component (the reference's elasticity test
+  // functions give each component the same value: linear_elasticity_analytical_functions.f90
+  // :128-142)
   P.gvals.assign(P.ndir, 0.0);
-  if (P.ndir > 0 && p.kind == ORC_POISSON) {
+  if (P.ndir > 0) {
     std::vector<double> xv(P.ngeo * 3);
     for (int64_t c = 0; c < P.ncells; ++c) {
       bool any = false;

@@ -1,0 +1,83 @@
+"""The reference's physics-based BDDC test problem (tests/pb_elasticity_case.py: channels with
+an E jump of 1e8, u = x+y+z on the boundary, 20^3 Q1 elasticity) on the device:
+
+* rhs: 1e-6 ||b|| equals the reference's printed CG tolerance 3.708160389E+02 to its 10
+  digits, and b equals the oracle's to 1e-13 of its largest entry; the CSR pattern is the
+  oracle's bit for bit, the entries within 1e-13 of their row's largest;
+* BDDC as the test configures it -- 2 x 2 x 2 box parts, faces only (no primal vertices),
+  the elasticity handler's rigid-body face functionals -- with stiffness weights: converged
+  at rtol 1e-6 with a true residual <= 1e-6 ||b|| (checked on the host with the oracle's
+  matrix).  The reference reaches 1e-6 in 11 iterations with its physics-based partition
+  (objects split by material subparts, weights by subpart modulus), which is not built here;
+  the iteration counts are printed beside it.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import pb_elasticity_case as pb
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def fg():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import fempar_gb300 as fg
+    from fempar_gb300 import build
+    build.build()
+    return fg
+
+
+@pytest.fixture(scope="module")
+def case(fg):
+    ctx = fg.Context(0)
+    E = pb.cell_modulus()
+    P = O.Problem(pb.N, order=1, kind=O.ELASTICITY, limits=list(pb.LIMITS), cell_coef=E, nu=pb.NU,
+                  source_fn=O.FN_ZERO, boundary_fn=O.FN_LINEAR, dirichlet_ids=list(range(1, 27)))
+    tri = fg.SerialTriangulation(ctx, pb.N, limits=pb.LIMITS)
+    sp = fg.SerialFESpace(tri, order=1, ncomp=3, dirichlet_ids=fg.ALL_BOUNDARY_IDS)
+    op = fg.FEAffineOperator(sp, fg.ElasticityIntegration(cell_coef=E, nu=pb.NU, source_fn=fg.FG_FN_ZERO,
+                                                          boundary_fn=fg.FG_FN_LINEAR)).compute()
+    return ctx, P, tri, sp, op
+
+
+def test_rhs_and_matrix_match_the_reference_tolerance_and_the_oracle(fg, case):
+    ctx, P, tri, sp, op = case
+    b = op.get_translation()
+    assert abs(pb.RTOL * float(np.linalg.norm(b)) - pb.TOLERANCE) <= 0.5e-7
+    ob = P.rhs()
+    assert np.abs(b - ob).max() <= 1e-13 * np.abs(ob).max()
+    irp, ja, val = op.get_matrix()
+    oirp, oja, oval = P.csr_upper()
+    assert np.array_equal(irp, oirp) and np.array_equal(ja, oja)
+    rows = np.repeat(np.arange(P.nfree), np.diff(oirp))
+    scale = np.zeros(P.nfree)
+    np.maximum.at(scale, rows, np.abs(oval))
+    assert (np.abs(val - oval) / scale[rows]).max() <= 1e-13
+
+
+def _full(P):
+    import scipy.sparse as sps
+    irp, ja, val = P.csr_upper()
+    U = sps.csr_matrix((val, ja - 1, irp - 1), shape=(P.nfree, P.nfree))
+    return U + sps.triu(U, 1).T
+
+
+@pytest.mark.parametrize("use_vertices", [False, True])
+def test_bddc_faces_elasticity_handler_on_the_reference_problem(fg, case, use_vertices):
+    ctx, P, tri, sp, op = case
+    M = fg.MLBDDC(op, nsub=pb.NPARTS, cuts=[[0, 10, 20]] * 3, use_vertices=use_vertices, use_edges=False,
+                  use_faces=True, weighting=fg.FG_BDDC_WEIGHT_STIFFNESS, coarse_handler=fg.FG_BDDC_HANDLER_ELASTICITY)
+    s = fg.IterativeLinearSolver().set_type_from_string("CG").set_operators(op, M)
+    s.set_parameters_from_pl({"ILS_RTOL": pb.RTOL, "ILS_MAX_NUM_ITERATIONS": 5000})
+    x = s.solve()
+    info = s.info()
+    print(f"reference pb-BDDC problem, faces only{'' if not use_vertices else ' + vertices'}, stiffness weights: "
+          f"{info['iterations']} iterations to rtol 1e-6 (the reference, physics-based partition: {pb.ITERATIONS})")
+    assert info["converged"]
+    A, b = _full(P), P.rhs()
+    assert np.linalg.norm(b - A @ x) <= 1.01 * pb.RTOL * np.linalg.norm(b)
+    M.close()

@@ -91,3 +91,14 @@ def test_uniform_strain_is_in_equilibrium_inside(dim, n, order):
     scale = np.abs(P.csr_full()[2]).max() * np.abs(u).max()
     assert np.abs(Ku[interior]).max() <= 1e-11 * scale
     assert np.abs(Ku[~interior]).max() > 1e-6 * scale   # the boundary carries the tractions
+
+
+def test_reference_pb_bddc_problem_rhs_norm():
+    """The rhs of the reference's physics-based BDDC test problem (channels with E jump 1e8,
+    u = x+y+z on the boundary): 1e-6 ||b|| equals the tolerance the reference printed,
+    3.708160389E+02, to its 10 significant digits."""
+    import pb_elasticity_case as pb
+    P = O.Problem(pb.N, order=1, kind=O.ELASTICITY, limits=list(pb.LIMITS), cell_coef=pb.cell_modulus(), nu=pb.NU,
+                  source_fn=O.FN_ZERO, boundary_fn=O.FN_LINEAR, dirichlet_ids=list(range(1, 27)))
+    tol = pb.RTOL * float(np.linalg.norm(P.rhs()))
+    assert abs(tol - pb.TOLERANCE) <= 0.5e-7, tol
