@@ -18,6 +18,7 @@ FG_FP64 = _lib.FG_FP64
 FG_MIXED = _lib.FG_MIXED
 FG_BDDC_WEIGHT_MULTIPLICITY = _lib.FG_BDDC_WEIGHT_MULTIPLICITY
 FG_BDDC_WEIGHT_STIFFNESS = _lib.FG_BDDC_WEIGHT_STIFFNESS
+FG_BDDC_WEIGHT_SUBPART = _lib.FG_BDDC_WEIGHT_SUBPART
 FG_BDDC_HANDLER_STANDARD = _lib.FG_BDDC_HANDLER_STANDARD
 FG_BDDC_HANDLER_ELASTICITY = _lib.FG_BDDC_HANDLER_ELASTICITY
 

@@ -20,7 +20,7 @@ FG_POISSON, FG_ELASTICITY = 0, 1
 FG_FN_ZERO, FG_FN_CONST, FG_FN_SHARP_WAVE, FG_FN_LINEAR, FG_FN_QP_VALUES = 0, 1, 2, 3, 4
 FG_INPUTS_ON_DEVICE, FG_LEAN_SYSTEM, FG_FAST_INTEGRATION = 1, 2, 4
 FG_PREC_NONE, FG_PREC_JACOBI, FG_PREC_BDDC = 0, 1, 2
-FG_BDDC_WEIGHT_MULTIPLICITY, FG_BDDC_WEIGHT_STIFFNESS = 0, 1
+FG_BDDC_WEIGHT_MULTIPLICITY, FG_BDDC_WEIGHT_STIFFNESS, FG_BDDC_WEIGHT_SUBPART = 0, 1, 2
 FG_BDDC_HANDLER_STANDARD, FG_BDDC_HANDLER_ELASTICITY = 0, 1
 FG_FP64, FG_MIXED = 0, 1
 FG_DENSE_LOWER = 1
@@ -134,6 +134,7 @@ class BddcParams(C.Structure):
         ("use_faces", C.c_int32),
         ("weighting", C.c_int32),
         ("coarse_handler", C.c_int32),
+        ("use_subparts", C.c_int32),
     ]
 
 

@@ -1018,15 +1018,13 @@ struct AxisInfo {
 // depends on the constraints' span only) is the same; in the reference's coordinates the
 // rotation rows are nearly combinations of the translation rows far from the origin, and
 // S_e = C K^-1 C^T is too ill-conditioned for the FP32 factors.
-static void face_functionals(uint64_t key, int row0, const std::vector<int32_t>* cuts, const int* c0, const int* c1,
-                             const int* lo, const int* bn, const int* ncell, int p, int nc, const std::vector<double>& xyz,
-                             const int32_t* box, std::vector<int32_t>& qrow, std::vector<int32_t>& qcol,
-                             std::vector<double>& qw) {
-  const int a = (int)((key >> 60) & 3);
-  const int ia[3] = {(int)((key >> 40) & 0xFFFFF), (int)((key >> 20) & 0xFFFFF), (int)(key & 0xFFFFF)};
-  const int plane = cuts[a][ia[a]];                  // cell index of the plane along a
-  const int ca = plane == c0[a] ? c0[a] : c1[a] - 1;  // this subdomain's cells along a
-  const int side = plane == c0[a] ? 0 : 1;
+// The facets: the subdomain's cell faces on the plane normal to axis a at side `side` of its
+// cells ca (0: the low face, 1: the high face) for which facet(cb, cc) holds.
+template <typename Facet>
+static void face_functionals_on(int a, int ca, int side, Facet facet, int row0, const int* c0, const int* c1,
+                                const int* lo, const int* bn, const int* ncell, int p, int nc,
+                                const std::vector<double>& xyz, const int32_t* box, std::vector<int32_t>& qrow,
+                                std::vector<int32_t>& qcol, std::vector<double>& qw) {
   const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;  // the face's axes, b < c
   const int nq = p + 1;
   std::vector<double> gx(nq), gw(nq);
@@ -1038,6 +1036,7 @@ static void face_functionals(uint64_t key, int row0, const std::vector<int32_t>*
   auto sweep = [&](int pass) {
     for (int cc = c0[c]; cc < c1[c]; ++cc)
       for (int cb = c0[b]; cb < c1[b]; ++cb) {
+        if (!facet(cb, cc)) continue;
         double V[2][2][3];
         for (int v = 0; v < 2; ++v)
           for (int u = 0; u < 2; ++u) {
@@ -1096,6 +1095,7 @@ static void face_functionals(uint64_t key, int row0, const std::vector<int32_t>*
       }
   };
   sweep(0);
+  if (!(meas > 0.0)) return;
   for (int d = 0; d < 3; ++d) xF[d] /= meas;
   scale = 1.0 / std::sqrt(meas);
   sweep(1);
@@ -1106,6 +1106,20 @@ static void face_functionals(uint64_t key, int row0, const std::vector<int32_t>*
         qcol.push_back(kv.first);
         qw.push_back(kv.second[m] / meas);
       }
+}
+
+// The face object `key` of the box grid: all of the subdomain's cell faces on that plane.
+static void face_functionals(uint64_t key, int row0, const std::vector<int32_t>* cuts, const int* c0, const int* c1,
+                             const int* lo, const int* bn, const int* ncell, int p, int nc, const std::vector<double>& xyz,
+                             const int32_t* box, std::vector<int32_t>& qrow, std::vector<int32_t>& qcol,
+                             std::vector<double>& qw) {
+  const int a = (int)((key >> 60) & 3);
+  const int ia[3] = {(int)((key >> 40) & 0xFFFFF), (int)((key >> 20) & 0xFFFFF), (int)(key & 0xFFFFF)};
+  const int plane = cuts[a][ia[a]];                  // cell index of the plane along a
+  const int ca = plane == c0[a] ? c0[a] : c1[a] - 1;  // this subdomain's cells along a
+  const int side = plane == c0[a] ? 0 : 1;
+  face_functionals_on(a, ca, side, [](int, int) { return true; }, row0, c0, c1, lo, bn, ncell, p, nc, xyz, box, qrow,
+                      qcol, qw);
 }
 
 static fg_status bddc_symbolic(fg_bddc* B) {
@@ -1150,6 +1164,82 @@ static fg_status bddc_symbolic(fg_bddc* B) {
   }
   B->nsub = ns[0] * ns[1] * ns[2];
   B->subs.assign(B->nsub, BSub());
+  // physics-based partition: the subparts are the face-connected components of equal cell
+  // coefficient within each subdomain, numbered in order of their first cell
+  const bool pb = B->prm.use_subparts != 0;
+  const int ncx = me->n[0], ncy = me->n[1], ncz = me->n[2];
+  std::vector<int32_t> csub, sub_part;
+  std::vector<double> subE;
+  auto cell_part = [&](int i, int j, int k) {
+    int q[3] = {i, j, k}, s3[3];
+    for (int d = 0; d < 3; ++d) {
+      s3[d] = 0;
+      while (s3[d] + 1 < ns[d] && q[d] >= B->cuts[d][s3[d] + 1]) ++s3[d];
+    }
+    return s3[0] + ns[0] * (s3[1] + ns[1] * s3[2]);
+  };
+  if (pb) {
+    const int64_t ncell = (int64_t)ncx * ncy * ncz;
+    std::vector<double> coef(ncell, B->sys->integ.coef_const);
+    if (B->sys->d_coef) {
+      FG_CUDA_TRY(cudaMemcpyAsync(coef.data(), B->sys->d_coef, sizeof(double) * ncell, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+      FG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    }
+    std::vector<int32_t> cpart(ncell);
+    for (int k = 0; k < ncz; ++k)
+      for (int j = 0; j < ncy; ++j)
+        for (int i = 0; i < ncx; ++i) cpart[i + (int64_t)ncx * (j + (int64_t)ncy * k)] = cell_part(i, j, k);
+    csub.assign(ncell, -1);
+    std::vector<int64_t> stack;
+    for (int64_t c0 = 0; c0 < ncell; ++c0) {
+      if (csub[c0] >= 0) continue;
+      const int32_t id = (int32_t)subE.size();
+      subE.push_back(coef[c0]);
+      sub_part.push_back(cpart[c0]);
+      csub[c0] = id;
+      stack.assign(1, c0);
+      while (!stack.empty()) {
+        const int64_t c = stack.back();
+        stack.pop_back();
+        const int i = (int)(c % ncx), j = (int)((c / ncx) % ncy), k = (int)(c / ((int64_t)ncx * ncy));
+        const int nbr[6][3] = {{i - 1, j, k}, {i + 1, j, k}, {i, j - 1, k}, {i, j + 1, k}, {i, j, k - 1}, {i, j, k + 1}};
+        for (auto& q : nbr) {
+          if (q[0] < 0 || q[0] >= ncx || q[1] < 0 || q[1] >= ncy || q[2] < 0 || q[2] >= ncz) continue;
+          const int64_t cq = q[0] + (int64_t)ncx * (q[1] + (int64_t)ncy * q[2]);
+          if (csub[cq] < 0 && cpart[cq] == cpart[c0] && coef[cq] == coef[c0]) {
+            csub[cq] = id;
+            stack.push_back(cq);
+          }
+        }
+      }
+    }
+  }
+  // subparts of the cells around lattice node (X, Y, Z), sorted and unique
+  auto node_subparts = [&](int X, int Y, int Z, int* out) {
+    int lo3[3], hi3[3];
+    const int P3[3] = {X, Y, Z}, nn3[3] = {ncx, ncy, ncz};
+    for (int d = 0; d < 3; ++d) {
+      if (P3[d] % p == 0) {
+        lo3[d] = std::max(0, P3[d] / p - 1);
+        hi3[d] = std::min(nn3[d] - 1, P3[d] / p);
+      } else {
+        lo3[d] = hi3[d] = P3[d] / p;
+      }
+    }
+    int cnt = 0;
+    for (int k = lo3[2]; k <= hi3[2]; ++k)
+      for (int j = lo3[1]; j <= hi3[1]; ++j)
+        for (int i = lo3[0]; i <= hi3[0]; ++i) {
+          const int32_t sid = csub[i + (int64_t)ncx * (j + (int64_t)ncy * k)];
+          bool seen = false;
+          for (int t = 0; t < cnt; ++t) seen |= out[t] == sid;
+          if (!seen) out[cnt++] = sid;
+        }
+    std::sort(out, out + cnt);
+    return cnt;
+  };
+  std::vector<double> h_w;  // FG_BDDC_WEIGHT_SUBPART: interface weights, computed here
   std::map<std::pair<uint64_t, int>, int32_t> coarse_id;
   std::vector<int64_t> iface_of(nfree > 0 ? nfree : 1, -1);
   std::vector<int32_t> ivec;
@@ -1177,6 +1267,7 @@ static fg_status bddc_symbolic(fg_bddc* B) {
     int32_t gid;
     int cls;  // 0 I, 1 E, 2 V
     uint64_t key;
+    double w;  // subpart weight (FG_BDDC_WEIGHT_SUBPART)
   };
   std::vector<LD> dofs;
   for (int sk = 0; sk < ns[2]; ++sk)
@@ -1206,7 +1297,33 @@ static fg_status bddc_symbolic(fg_bddc* B) {
               }
               int cls = 0;
               uint64_t key = 0;
-              if (ncut > 0) {
+              double wsub = 0.0;
+              if (ncut > 0 && pb) {
+                // objects by the subparts around: a face object holds the dofs whose cells
+                // belong to exactly two subparts (one per side of one cut plane); the rest
+                // are edge or vertex objects, primal vertices only as asked
+                int sg[8];
+                const int nsg = node_subparts(X, Y, Z, sg);
+                double tot = 0.0, own = 0.0;
+                for (int t = 0; t < nsg; ++t) {
+                  tot += subE[sg[t]];
+                  if (sub_part[sg[t]] == s) own += subE[sg[t]];
+                }
+                wsub = tot > 0.0 ? own / tot : 0.0;
+                if (npl == 3 && B->prm.use_vertices) {
+                  cls = 2;
+                  key = enc(0, 0, X, Y, Z);
+                } else if (ncut == 1 && nsg == 2) {
+                  cls = 1;
+                  int a = 0;
+                  for (int d = 0; d < 3; ++d)
+                    if (ax[d].on_cut[P3[d]]) a = d;
+                  key = enc(2, a, sg[0], sg[1], 0);
+                } else {
+                  cls = 1;
+                  key = enc(1, 0, 0, 0, 0);  // no constraint (edges are off with subparts)
+                }
+              } else if (ncut > 0) {
                 if (npl == 3) {
                   // a vertex: primal (V), or with use_vertices = 0 an interface dof without a
                   // coarse dof of its own
@@ -1233,7 +1350,7 @@ static fg_status bddc_symbolic(fg_bddc* B) {
               for (int c = 0; c < nc; ++c) {
                 int32_t ld = latdof[L * nc + c];
                 if (ld <= 0) continue;
-                dofs.push_back({L, c, ld - 1, cls, key});
+                dofs.push_back({L, c, ld - 1, cls, key, wsub});
               }
             }
         // local order I | E | V (stable)
@@ -1305,9 +1422,37 @@ static fg_status bddc_symbolic(fg_bddc* B) {
               h_qw.push_back(1.0 / (double)lcnt[econ[k]]);
             }
         } else {
-          for (size_t f = 0; f < rfaces.size(); ++f)
-            face_functionals(rfaces[f], (int)(6 * f), B->cuts, S.c0, S.c1, lo, bn, me->n, p, nc, xyz,
-                             h_box.data() + b0, h_qrow, h_qcol, h_qw);
+          for (size_t f = 0; f < rfaces.size(); ++f) {
+            if (!pb) {
+              face_functionals(rfaces[f], (int)(6 * f), B->cuts, S.c0, S.c1, lo, bn, me->n, p, nc, xyz,
+                               h_box.data() + b0, h_qrow, h_qcol, h_qw);
+              continue;
+            }
+            // a subpart face object: the facets between its two subparts
+            const uint64_t key = rfaces[f];
+            const int a = (int)((key >> 60) & 3);
+            const int s1 = (int)((key >> 40) & 0xFFFFF), s2 = (int)((key >> 20) & 0xFFFFF);
+            const int other = sub_part[s1] == s ? sub_part[s2] : sub_part[s1];
+            const int o3[3] = {other % ns[0], (other / ns[0]) % ns[1], other / (ns[0] * ns[1])};
+            const int side = o3[a] < sc[a] ? 0 : 1;
+            const int ca = side == 0 ? S.c0[a] : S.c1[a] - 1;
+            const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+            auto facet = [&](int cb, int cc) {
+              int q[3], r3[3];
+              q[a] = ca;
+              q[b] = cb;
+              q[c] = cc;
+              r3[0] = q[0];
+              r3[1] = q[1];
+              r3[2] = q[2];
+              r3[a] = side == 0 ? ca - 1 : ca + 1;
+              const int32_t u = csub[q[0] + (int64_t)ncx * (q[1] + (int64_t)ncy * q[2])];
+              const int32_t v = csub[r3[0] + (int64_t)ncx * (r3[1] + (int64_t)ncy * r3[2])];
+              return (u == s1 && v == s2) || (u == s2 && v == s1);
+            };
+            face_functionals_on(a, ca, side, facet, (int)(6 * f), S.c0, S.c1, lo, bn, me->n, p, nc, xyz,
+                                h_box.data() + b0, h_qrow, h_qcol, h_qw);
+          }
         }
         {  // entries grouped by constraint row (the augmentation takes them row by row)
           std::vector<int64_t> ord((int64_t)h_qrow.size() - q0);
@@ -1360,6 +1505,7 @@ static fg_status bddc_symbolic(fg_bddc* B) {
         const int nP = nV + ne;
         // interface contributions in subdomain order
         for (int k = 0; k < nE + nV; ++k) {
+          h_w.push_back(dofs[nI + k].w);
           int32_t gid = dofs[nI + k].gid;
           if (iface_of[gid] < 0) {
             iface_of[gid] = (int64_t)ivec.size();
@@ -1501,7 +1647,8 @@ static fg_status bddc_symbolic(fg_bddc* B) {
   FG_TRY(balloc_n(B, &B->dF, B->nF));
   FG_TRY(balloc_n(B, &B->dR, B->nR));
   FG_TRY(balloc_n(B, &B->dR32, B->nR));
-  FG_TRY(balloc_n(B, &B->dW, B->nW));
+  if (B->prm.weighting == FG_BDDC_WEIGHT_SUBPART) FG_TRY(upload(B, &B->dW, h_w));
+  else FG_TRY(balloc_n(B, &B->dW, B->nW));
   FG_TRY(balloc_n(B, &B->dDiag, B->nW));
   FG_TRY(balloc_n(B, &B->dC, B->nW));
   FG_TRY(balloc_n(B, &B->dC32, B->nW));
@@ -1622,7 +1769,7 @@ static fg_status bddc_numeric(fg_bddc* B) {
     k_bddc_augment<<<ns, 256, 0, st>>>(B->d_subs, B->dQrow, B->dQcol, B->dQw, B->dA, B->dRho);
     ctx->launches += 1;
   }
-  if (B->nIface > 0)
+  if (B->nIface > 0 && B->prm.weighting != FG_BDDC_WEIGHT_SUBPART)
     k_bddc_weights<<<nblk(B->nIface, 256), 256, 0, st>>>(B->nIface, B->dIptr, B->dIsrc, B->dDiag,
                                                          B->prm.weighting == FG_BDDC_WEIGHT_STIFFNESS, B->dW);
   cudaEvent_t ev[4];
@@ -2030,8 +2177,13 @@ fg_status fg_bddc_create(fg_system* sys, const fg_bddc_params* prm, fg_bddc** ou
     set_error("BDDC: no coarse constraints (use_vertices, use_edges and use_faces all 0)");
     return FG_ERR_UNSUPPORTED;
   }
-  if (prm->weighting != FG_BDDC_WEIGHT_MULTIPLICITY && prm->weighting != FG_BDDC_WEIGHT_STIFFNESS)
+  if (prm->weighting != FG_BDDC_WEIGHT_MULTIPLICITY && prm->weighting != FG_BDDC_WEIGHT_STIFFNESS &&
+      prm->weighting != FG_BDDC_WEIGHT_SUBPART)
     return bddc_bad("weighting");
+  if ((prm->weighting == FG_BDDC_WEIGHT_SUBPART || prm->use_subparts) && (!prm->use_subparts || prm->use_edges)) {
+    set_error("BDDC: subpart weights need use_subparts = 1, and subparts need use_edges = 0");
+    return FG_ERR_UNSUPPORTED;
+  }
   if (prm->coarse_handler != FG_BDDC_HANDLER_STANDARD && prm->coarse_handler != FG_BDDC_HANDLER_ELASTICITY)
     return bddc_bad("coarse_handler");
   if (prm->coarse_handler == FG_BDDC_HANDLER_ELASTICITY && (sp->ncomp != 3 || prm->use_edges)) {

@@ -426,7 +426,7 @@ class MLBDDC:
 
     def __init__(self, A: FEAffineOperator, nsub=(2, 2, 2), cuts=None, use_vertices=True, use_edges=True,
                  use_faces=False, weighting=L.FG_BDDC_WEIGHT_MULTIPLICITY,
-                 coarse_handler=L.FG_BDDC_HANDLER_STANDARD):
+                 coarse_handler=L.FG_BDDC_HANDLER_STANDARD, use_subparts=False):
         p = L.BddcParams()
         L.lib().fg_bddc_params_default(C.byref(p))
         for d in range(3):
@@ -438,6 +438,7 @@ class MLBDDC:
         p.use_vertices, p.use_edges, p.use_faces = int(use_vertices), int(use_edges), int(use_faces)
         p.weighting = int(weighting)
         p.coarse_handler = int(coarse_handler)
+        p.use_subparts = int(use_subparts)
         self.A = A
         h = C.c_void_p()
         L.check(L.lib().fg_bddc_create(A.h, C.byref(p), C.byref(h)), "fg_bddc_create")

@@ -45,6 +45,7 @@ module fempar_gpu_names
     type(c_ptr)        :: cuts            ! nsub(1)+1 + nsub(2)+1 + nsub(3)+1 cell indices, or c_null_ptr
     integer(c_int32_t) :: use_vertices, use_edges, use_faces, weighting
     integer(c_int32_t) :: coarse_handler  ! 0 standard, 1 elasticity (rigid-body face functionals)
+    integer(c_int32_t) :: use_subparts    ! 1: physics-based partition (subparts of equal coefficient)
   end type
 
   type, bind(c) :: fg_error_norms

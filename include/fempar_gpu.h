@@ -377,7 +377,7 @@ fg_status fg_partition_solve(fg_partition* partition, fg_system* subassembled, c
  * partition whose dense local matrices do not fit the context's HBM budget. */
 typedef struct fg_bddc fg_bddc;
 enum { FG_PREC_BDDC = 2 };
-enum { FG_BDDC_WEIGHT_MULTIPLICITY = 0, FG_BDDC_WEIGHT_STIFFNESS = 1 };
+enum { FG_BDDC_WEIGHT_MULTIPLICITY = 0, FG_BDDC_WEIGHT_STIFFNESS = 1, FG_BDDC_WEIGHT_SUBPART = 2 };
 /* Coarse FE handler.  STANDARD: sbm_standard_coarse_fe_handler.i90 (one coarse dof per
  * object and component, algebraic averages).  ELASTICITY: elasticity_pb_bddc_l1_coarse_fe_handler_t
  * (sbm_elasticity_coarse_fe_handler.i90:75-381): 3 coarse dofs per vertex, no edge
@@ -399,6 +399,15 @@ typedef struct {
   int32_t weighting;       /* FG_BDDC_WEIGHT_MULTIPLICITY (reference standard handler) or
                               FG_BDDC_WEIGHT_STIFFNESS (diag(A_i) / sum_j diag(A_j))        */
   int32_t coarse_handler;  /* FG_BDDC_HANDLER_STANDARD (default) or FG_BDDC_HANDLER_ELASTICITY */
+  int32_t use_subparts;    /* physics-based partition (the reference's pb_bddc): a subdomain's
+                              cells split into subparts (face-connected cells of equal cell
+                              coefficient); interface dofs are grouped by the subparts around
+                              them, a face object being the dofs whose cells belong to exactly
+                              two subparts, one on each side; with FG_BDDC_WEIGHT_SUBPART the
+                              weight of subdomain i is the sum of the coefficients of its
+                              subparts around the dof over that of all of them
+                              (sbm_elasticity_coarse_fe_handler.i90:422-516).  Elasticity
+                              handler, faces only (use_edges = 0)                          */
 } fg_bddc_params;
 typedef struct {
   int32_t num_subdomains;

@@ -28,6 +28,7 @@ NU = 0.2
 RTOL = 1.0e-6
 TOLERANCE = 3.708160389e02   # printed with 10 significant digits
 ITERATIONS = 11
+FIRST_RESIDUAL = 8.967533941e06  # the CG log's first error estimate (test1_convergence:2)
 
 
 def _positions(d):
