@@ -38,7 +38,8 @@
 // warps per TMEM lane quarter, 32 columns each) and write C.  CTAs are persistent (one per SM, tiles round robin):
 // the epilogue releases the accumulators before its FP64 writes, which then overlap the next
 // tile's MMAs, and the stages of the next tile are loaded meanwhile.  Every wait is bounded: after ~1 s the CTA records
-// FG_ERR_TIMEOUT, stops, frees its tensor memory and returns.
+// FG_ERR_TIMEOUT, stops, waits (bounded) for its copies and MMAs in flight, frees its tensor
+// memory and returns.
 
 #include <cuda_runtime.h>
 
@@ -140,6 +141,16 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
 }
 
 // bounded wait; false (and the CTA's abort flag and the error status set) when it runs out
+// after an abort: wait (bounded, ignoring the abort flag) for the copies or MMAs still in
+// flight, so that nothing writes this CTA's shared or tensor memory once it is released
+__device__ __forceinline__ void mbar_drain(uint32_t a, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try(a, parity)) {
+    __nanosleep(64);
+    if (clock64() - t0 > OZ_WAIT_CYCLES) return;
+  }
+}
+
 __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err) {
   const long long t0 = clock64();
   int spins = 0;
@@ -468,6 +479,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
           ++gs;
           ok = produce();
         }
+      }
+      if (!ok) {
+        // drain: the stages whose copies were issued but not consumed, then every MMA issued
+        for (int q = gs; q < pgs; ++q) mbar_drain(smem_u32(&bar_full[q % OZ_NBUF]), (q / OZ_NBUF) & 1);
+        if (gs > 0) mbar_drain(smem_u32(&bar_empty[(gs - 1) % OZ_NBUF]), ((gs - 1) / OZ_NBUF) & 1);
       }
     }
     __syncwarp();
