@@ -307,6 +307,7 @@ struct OzGemmArgs {
   int ksteps;
   double alpha, beta;
   int lower;             // write only i >= j
+  int drop_stage;        // test switch (FG_OZ_TEST_DROP_STAGE): CTA 0 never issues this stage's copies
   int* err;
 };
 
@@ -431,9 +432,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
         const uint32_t full = smem_u32(&bar_full[buf]);
         const uint32_t dst = sbase + buf * T::STAGE;
         mbar_expect_tx(full, T::STAGE);
-        bulk_g2s(dst, pa + (size_t)pks * OZ_A_BYTES, OZ_A_BYTES, full);
-        for (int t = 0; t < OZ_S; ++t)
-          bulk_g2s(dst + OZ_A_BYTES + t * T::B_DIGIT, pb + ((size_t)pks * OZ_S + t) * OZ_BLOCK, T::B_DIGIT, full);
+        if (!(blockIdx.x == 0 && pgs == g.drop_stage)) {
+          bulk_g2s(dst, pa + (size_t)pks * OZ_A_BYTES, OZ_A_BYTES, full);
+          for (int t = 0; t < OZ_S; ++t)
+            bulk_g2s(dst + OZ_A_BYTES + t * T::B_DIGIT, pb + ((size_t)pks * OZ_S + t) * OZ_BLOCK, T::B_DIGIT, full);
+        }
         ++pgs;
         if (++pks == KS) {
           pks = 0;
@@ -641,6 +644,10 @@ static fg_status oz_gemm_launch(fg_ctx* ctx, cudaStream_t st, OzGemmArgs& g, int
 
 static fg_status oz_launch(fg_ctx* ctx, cudaStream_t st, OzSplitArgs& sa, int64_t rtiles, OzGemmArgs& g,
                            int64_t ntiles) {
+  // test switch for the failure-detection test: a stage whose copies never arrive makes the
+  // bounded wait run out (FG_ERR_TIMEOUT) without a fault
+  const char* drop = std::getenv("FG_OZ_TEST_DROP_STAGE");
+  g.drop_stage = drop ? std::atoi(drop) : -1;
   k_oz_rowexp<<<dim3((unsigned)rtiles, 32), OZ_BM, 0, st>>>(sa);
   k_oz_split<<<dim3((unsigned)rtiles, (unsigned)sa.ksteps), OZ_BM, 0, st>>>(sa);
   FG_TRY(oz_bn() == 32 ? oz_gemm_launch<32>(ctx, st, g, ntiles) : oz_gemm_launch<64>(ctx, st, g, ntiles));

@@ -8,7 +8,9 @@ against cuBLAS DGEMM (torch.matmul on float64).
 * rows scaled by powers of two from 2^-60 to 2^60 (per-row exponents);
 * the lower-triangle flag writes nothing above the diagonal; B = NULL is A A^T, e.g. the
   trailing update of a column-major Cholesky panel;
-* k = 0 gives beta C.
+* k = 0 gives beta C;
+* a bounded wait that runs out (test switch) returns FG_ERR_TIMEOUT and leaves the context
+  usable.
 """
 import numpy as np
 import pytest
@@ -114,3 +116,22 @@ def test_k_zero_scales_c(env):
     Cm = C0.clone()
     gemm_nt(ctx, A, B, Cm, alpha=1.0, beta=2.0)
     assert torch.equal(Cm, 2.0 * C0)
+
+
+def test_bounded_wait_runs_out_and_context_survives(env, monkeypatch):
+    """Failure detection without a GPU fault: CTA 0 never issues the copies of its third stage
+    (test switch), its bounded wait runs out after ~1 s, the call returns FG_ERR_TIMEOUT after
+    draining what is in flight, and the same context then computes the product correctly."""
+    fg, ctx, torch = env
+    from fempar_gb300 import FGError
+    from fempar_gb300.dense import gemm_nt
+    A = torch.randn((256, 256), dtype=torch.float64, device="cuda")
+    B = torch.randn((192, 256), dtype=torch.float64, device="cuda")
+    monkeypatch.setenv("FG_OZ_TEST_DROP_STAGE", "2")
+    with pytest.raises(FGError) as ei:
+        gemm_nt(ctx, A, B)
+    assert "FG_ERR_TIMEOUT" in str(ei.value)
+    monkeypatch.delenv("FG_OZ_TEST_DROP_STAGE")
+    X = gemm_nt(ctx, A, B).cpu().numpy()
+    ref = (A @ B.T).cpu().numpy()
+    assert scaled_err(X, ref, A.cpu().numpy(), B.cpu().numpy(), 256) <= TOL
