@@ -304,3 +304,29 @@ def test_bddc_rejects_bad_parameters(fg, ctx):
         fg.MLBDDC(op, nsub=(5, 1, 1))
     with pytest.raises(FGError):
         fg.MLBDDC(op, nsub=(2, 1, 1), cuts=[[0, 3, 3], [0, 4], [0, 2]])
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_subparts_with_one_material_reduce_to_the_box_objects(fg, ctx, order):
+    """With one material the subparts are the subdomains: the physics-based partition's face
+    objects are the box faces and its weights the multiplicities, so the preconditioner equals
+    the faces-only one with multiplicity weights (same coarse space, applies equal to 1e-12)."""
+    import torch
+    n = (6, 4, 4)
+    tri = fg.SerialTriangulation(ctx, n, vertex_xyz=perturbed(n, 0.15, 3))
+    sp = fg.SerialFESpace(tri, order=order, ncomp=3, dirichlet_ids=CLAMP)
+    op = fg.FEAffineOperator(sp, fg.ElasticityIntegration(coef_const=2.5, nu=0.3, source_fn=fg.FG_FN_CONST,
+                                                          fn_param=[0.0, 0.0, -1.0])).compute()
+    cuts = fg.bddc_cuts(n, (3, 2, 2), jitter=0.2, seed=7)
+    common = dict(nsub=(3, 2, 2), cuts=cuts, use_vertices=False, use_edges=False, use_faces=True,
+                  coarse_handler=fg.FG_BDDC_HANDLER_ELASTICITY)
+    Mp = fg.MLBDDC(op, weighting=fg.FG_BDDC_WEIGHT_SUBPART, use_subparts=True, **common)
+    Mb = fg.MLBDDC(op, weighting=fg.FG_BDDC_WEIGHT_MULTIPLICITY, **common)
+    assert Mp.info()["num_coarse_dofs"] == Mb.info()["num_coarse_dofs"]
+    r = torch.randn(sp.num_free_dofs, dtype=torch.float64, device=f"cuda:{ctx.device}")
+    zp, zb = torch.zeros_like(r), torch.zeros_like(r)
+    Mp.apply_device(r, zp)
+    Mb.apply_device(r, zb)
+    assert float((zp - zb).norm() / zb.norm()) <= 1e-12
+    Mp.close()
+    Mb.close()
