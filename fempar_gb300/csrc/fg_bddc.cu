@@ -41,6 +41,7 @@
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -876,7 +877,20 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(int64_t nC, const T* __rest
   if (row >= nC) return;
   const T* k = K + row * nC;
   double acc = 0.0;
-  for (int64_t j = lane; j < nC; j += 32) acc += (double)k[j] * (double)f[j];
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 factors: compensated FP32 sums per lane (a conversion and an FP64 FMA per element
+    // would make this FP64-pipe bound), the 32 lane sums in FP64
+    float s = 0.f, c = 0.f;
+    for (int64_t j = lane; j < nC; j += 32) {
+      const float y = fmaf(k[j], f[j], -c);
+      const float t = s + y;
+      c = (t - s) - y;
+      s = t;
+    }
+    acc = (double)s - (double)c;
+  } else {
+    for (int64_t j = lane; j < nC; j += 32) acc += (double)k[j] * (double)f[j];
+  }
   acc = warp_sum(acc);
   if (lane == 0) u[row] = (T)acc;
 }
