@@ -349,10 +349,12 @@ __global__ void __launch_bounds__(RB)
     for (int j = 0; j < (Bp >> 2); ++j) {
       const int4 o = __ldg(reinterpret_cast<const int4*>(soff + offbase) + j);
       const int64_t e = v0 + (int64_t)j * 128;
-      out[e + 0] = (float)(tval[e + 0] * srow * sd[base + o.x]);
-      out[e + 1] = (float)(tval[e + 1] * srow * sd[base + o.y]);
-      out[e + 2] = (float)(tval[e + 2] * srow * sd[base + o.z]);
-      out[e + 3] = (float)(tval[e + 3] * srow * sd[base + o.w]);
+      // s_i s_j is one product for (i, j) and (j, i): the FP32 copy of an exactly symmetric
+      // matrix stays exactly symmetric
+      out[e + 0] = (float)(tval[e + 0] * (srow * sd[base + o.x]));
+      out[e + 1] = (float)(tval[e + 1] * (srow * sd[base + o.y]));
+      out[e + 2] = (float)(tval[e + 2] * (srow * sd[base + o.z]));
+      out[e + 3] = (float)(tval[e + 3] * (srow * sd[base + o.w]));
     }
   }
 }
@@ -372,7 +374,7 @@ __global__ void __launch_bounds__(RB)
     for (int j = 0; j < w4; ++j) {
       const int64_t e = base + 4 * lane + (int64_t)j * 128;
 #pragma unroll
-      for (int t = 0; t < 4; ++t) out[e + t] = (float)(sval[e + t] * srow * sd[scol[e + t]]);
+      for (int t = 0; t < 4; ++t) out[e + t] = (float)(sval[e + t] * (srow * sd[scol[e + t]]));
     }
   }
 }
