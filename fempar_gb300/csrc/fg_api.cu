@@ -372,6 +372,7 @@ static void space_free(fg_space* sp) {
   dev_free(ctx, sp->d_st_row);
   dev_free(ctx, sp->d_row2st);
   dev_free(ctx, sp->d_st_slot2row);
+  dev_free(ctx, sp->d_tcT);
   delete sp;
 }
 
@@ -574,7 +575,7 @@ static void system_free(fg_system* sys) {
   fg_ctx* ctx = sys->space->mesh->ctx;
   void* ptrs[] = {sys->d_val, sys->d_val32, sys->d_rhs, sys->d_gvals, sys->d_elmat, sys->d_elvec, sys->d_coef,
                   sys->d_qpsrc, sys->d_sval, sys->d_sval32, sys->d_tval, sys->d_tval32, sys->d_idiag, sys->d_idiag32, sys->d_work, sys->d_work32, sys->d_red, sys->d_ticket,
-                  sys->d_val32s, sys->d_sdiag};
+                  sys->d_val32s, sys->d_sdiag, sys->d_tcbuf};
   for (void* p : ptrs) dev_free(ctx, p);
   delete sys;
 }
@@ -615,7 +616,10 @@ static fg_status numeric_phase(fg_system* sys, const fg_integrand* g) {
     // element matrices are scratch of the scatter: release them before the solver layout
     dev_free(ctx, sys->d_elmat);
     dev_free(ctx, sys->d_elvec);
+    dev_free(ctx, sys->d_tcbuf);
     sys->d_elmat = sys->d_elvec = nullptr;
+    sys->d_tcbuf = nullptr;
+    sys->tcbuf_bytes = 0;
     if (sp->layout == FG_LAYOUT_SELL) {
       FG_TRY(dev_alloc(ctx, (void**)&sys->d_sval, sizeof(double) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1)));
       FG_TRY(dev_alloc(ctx, (void**)&sys->d_sval32, sizeof(float) * (sp->sell_nnz > 0 ? sp->sell_nnz : 1)));

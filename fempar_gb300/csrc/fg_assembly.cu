@@ -176,35 +176,17 @@ __device__ __forceinline__ void ff_split(double v, float& h, float& l) {
   l = (float)(v - (double)h);
 }
 
-template <int P, bool FF>
-__global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
-    k_integrate_poisson(AsmGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
-                        const int32_t* __restrict__ latdof, const double* __restrict__ gvals,
-                        const double* __restrict__ coef, double coef_const, SourceSpec src,
-                        double* __restrict__ E, double* __restrict__ EV) {
-  using S = typename PoissonShapeSel<P, FF>::type;
-  constexpr bool STREAM = FF && P <= 2;
-  constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND;
-  extern __shared__ double smem[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  double* base = smem + (size_t)wib * (S::SM_BYTES_WARP / 8);
-  double* xv = base;
-  double* invj = xv + S::SM_XV;
-  double* fac = invj + S::SM_INVJ;
-  double* xq = fac + S::SM_FAC;
-  double* fsrc = xq + S::SM_XQ;
-  double* sq = fsrc + S::SM_F;
-  double* sg = sq + S::SM_SQ;
-  double* el = sg + S::SM_G;
-  int32_t* gid = (int32_t*)(el + S::SM_EL);
-
-  const int64_t c = (int64_t)blockIdx.x * S::WARPS + wib;
-  if (c >= ncells) return;
-  const int ci = (int)(c % g.n[0]);
-  const int cj = (int)((c / g.n[0]) % g.n[1]);
-  const int ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
-  const double kc = coef ? coef[c] : coef_const;
-
+// Per cell: vertex coordinates, the dofs' global ids (negative: Dirichlet), and per Gauss
+// point J^-1 (invmtx order), |det J| w_q and the source value.  Reference: sbm_cell_map.i90:
+// 245-369, invmtx in sbm_cell_integrator.i90:448-500; |det| everywhere if the first det is
+// negative.
+template <int P>
+__device__ __forceinline__ void poisson_cell_geometry(const AsmGeom& g, int64_t c, int ci, int cj, int ck,
+                                                      const double* __restrict__ coords, const DevTables& tb,
+                                                      const int32_t* __restrict__ latdof, const SourceSpec& src,
+                                                      int lane, double* xv, double* invj, double* fac, double* xq,
+                                                      double* fsrc, int32_t* gid) {
+  constexpr int NQ = PoissonShape<P>::NQ, ND = PoissonShape<P>::ND;
   if (lane < 24) {
     int k = lane / 3, l = lane % 3;
     xv[lane] = coords[asm_vertex(g, c, ci, cj, ck, k) * 3 + l];
@@ -243,15 +225,17 @@ __global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
     b[6] = (J[3] * J[7] - J[4] * J[6]) * denom;
     b[7] = (-J[0] * J[7] + J[1] * J[6]) * denom;
     fac[q] = det;
-    double x0 = 0.0, x1 = 0.0, x2 = 0.0;
+    if (src.fn == FG_FN_SHARP_WAVE) {  // the only source that reads the physical coordinates
+      double x0 = 0.0, x1 = 0.0, x2 = 0.0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      double a = tb.gshp[k * NQ + q];
-      x0 = x0 + a * xv[k * 3 + 0];
-      x1 = x1 + a * xv[k * 3 + 1];
-      x2 = x2 + a * xv[k * 3 + 2];
+      for (int k = 0; k < 8; ++k) {
+        double a = tb.gshp[k * NQ + q];
+        x0 = x0 + a * xv[k * 3 + 0];
+        x1 = x1 + a * xv[k * 3 + 1];
+        x2 = x2 + a * xv[k * 3 + 2];
+      }
+      xq[q * 3 + 0] = x0; xq[q * 3 + 1] = x1; xq[q * 3 + 2] = x2;
     }
-    xq[q * 3 + 0] = x0; xq[q * 3 + 1] = x1; xq[q * 3 + 2] = x2;
   }
   __syncwarp();
   const bool neg = fac[0] < 0.0;  // reference: |det| everywhere if the first one is negative
@@ -265,8 +249,41 @@ __global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
     else if (src.fn == FG_FN_CONST) f = src.prm[0];
     else f = 0.0;
     fsrc[q] = f;
-    sq[q] = sqrt(fac[q] * kc);  // |det J| w k > 0
   }
+  __syncwarp();
+}
+
+template <int P, bool FF>
+__global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
+    k_integrate_poisson(AsmGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
+                        const int32_t* __restrict__ latdof, const double* __restrict__ gvals,
+                        const double* __restrict__ coef, double coef_const, SourceSpec src,
+                        double* __restrict__ E, double* __restrict__ EV) {
+  using S = typename PoissonShapeSel<P, FF>::type;
+  constexpr bool STREAM = FF && P <= 2;
+  constexpr int NN = S::NN, NQ = S::NQ, ND = S::ND;
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double* base = smem + (size_t)wib * (S::SM_BYTES_WARP / 8);
+  double* xv = base;
+  double* invj = xv + S::SM_XV;
+  double* fac = invj + S::SM_INVJ;
+  double* xq = fac + S::SM_FAC;
+  double* fsrc = xq + S::SM_XQ;
+  double* sq = fsrc + S::SM_F;
+  double* sg = sq + S::SM_SQ;
+  double* el = sg + S::SM_G;
+  int32_t* gid = (int32_t*)(el + S::SM_EL);
+
+  const int64_t c = (int64_t)blockIdx.x * S::WARPS + wib;
+  if (c >= ncells) return;
+  const int ci = (int)(c % g.n[0]);
+  const int cj = (int)((c / g.n[0]) % g.n[1]);
+  const int ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
+  const double kc = coef ? coef[c] : coef_const;
+
+  poisson_cell_geometry<P>(g, c, ci, cj, ck, coords, tb, latdof, src, lane, xv, invj, fac, xq, fsrc, gid);
+  for (int q = lane; q < NQ; q += 32) sq[q] = sqrt(fac[q] * kc);  // |det J| w k > 0
   __syncwarp();
   if constexpr (FF) {
     // float-float variant: J^-1 and sqrt(fk) as FP32 pairs (converted in place: the pairs
@@ -461,6 +478,112 @@ __global__ void __launch_bounds__(PoissonShapeSel<P, FF>::type::WARPS * 32)
   for (int idx = lane; idx < ND * ND; idx += 32) Ec[idx] = gid[idx % ND] < 0 ? 0.0 : el[idx];
 }
 
+// ---------------------------------------------------------------------------
+// Poisson element matrices on the tensor cores.  With r_a(q) the reference gradient of shape
+// a at Gauss point q and M_q = |det J_q| w_q k J_q^-1 J_q^-T (symmetric 3 x 3), an element
+// entry is E_ab = sum_q r_a(q)^T M_q r_b(q) = sum_{q,m} T[ab][6q + m] G[c][6q + m], m running
+// over the six entries of M_q (T holds r_ai r_bj + r_aj r_bi off the diagonal).  T (upper
+// pairs x 6 NQ) is the same for every cell, so the element matrices of all cells are one
+// product G T^T (cells x pairs, K = 6 NQ) -- the tensor form of the element matrix (Kirby and
+// Logg, ACM TOMS 32 (2006)) -- computed in FP64 emulated on the bf16 tensor cores
+// (ozaki_gemm_nt, fg_ozaki.cu).  Three kernels around it: the geometric factors G and the
+// source part of the element vector (warp per cell, the geometry of k_integrate_poisson), the
+// product, and the unpacking of each cell's upper triangle into the staged element matrix
+// with the Dirichlet lifting.
+template <int P>
+struct PoissonTC {
+  using S = PoissonShape<P>;
+  static constexpr int NQ = S::NQ, ND = S::ND, NPAIR = S::NPAIR, K = 6 * NQ;
+  static constexpr int WARPS = 8;
+  static constexpr int SM_DOUBLES = S::SM_XV + S::SM_INVJ + S::SM_FAC + S::SM_XQ + S::SM_F;
+  static constexpr size_t SM_BYTES_WARP = ((size_t)SM_DOUBLES * 8 + ND * 4 + 15) / 16 * 16;
+};
+
+template <int P>
+__global__ void __launch_bounds__(PoissonTC<P>::WARPS * 32)
+    k_poisson_geom(AsmGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
+                   const int32_t* __restrict__ latdof, const double* __restrict__ coef, double coef_const,
+                   SourceSpec src, double* __restrict__ G, double* __restrict__ EV) {
+  using T = PoissonTC<P>;
+  constexpr int NQ = T::NQ, ND = T::ND, K = T::K;
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double* xv = smem + (size_t)wib * (T::SM_BYTES_WARP / 8);
+  double* invj = xv + T::S::SM_XV;
+  double* fac = invj + T::S::SM_INVJ;
+  double* xq = fac + T::S::SM_FAC;
+  double* fsrc = xq + T::S::SM_XQ;
+  int32_t* gid = (int32_t*)(fsrc + T::S::SM_F);
+  const int64_t c = (int64_t)blockIdx.x * T::WARPS + wib;
+  if (c >= ncells) return;
+  const int ci = (int)(c % g.n[0]);
+  const int cj = (int)((c / g.n[0]) % g.n[1]);
+  const int ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
+  const double kc = coef ? coef[c] : coef_const;
+  poisson_cell_geometry<P>(g, c, ci, cj, ck, coords, tb, latdof, src, lane, xv, invj, fac, xq, fsrc, gid);
+  // per Gauss point: |det J| w k (into xq, free unless the source read it) and |det J| w f
+  double* fk = xq;
+  for (int q = lane; q < NQ; q += 32) {
+    const double fq = fac[q];
+    fk[q] = fq * kc;
+    fsrc[q] = fq * fsrc[q];
+  }
+  __syncwarp();
+  // M_jk = |det J| w k sum_l B[j + 3l] B[k + 3l], B = J^-1 as stored by invmtx; order 00 11 22 01 02 12
+  for (int e = lane; e < K; e += 32) {
+    const int q = e / 6, m = e - 6 * q;
+    const int j = m < 3 ? m : (m == 5 ? 1 : 0), k = m < 3 ? m : (m == 3 ? 1 : 2);
+    const double* b = invj + q * 9;
+    G[c * K + e] = fk[q] * (b[j] * b[k] + b[j + 3] * b[k + 3] + b[j + 6] * b[k + 6]);
+  }
+  // element vector, source part (the lifting follows the product); the same products and
+  // order as k_integrate_poisson's (fac f) phi
+  for (int a = lane; a < ND; a += 32) {
+    double ev = 0.0;
+    for (int q = 0; q < NQ; ++q) ev = ev + fsrc[q] * tb.shp[(size_t)a * NQ + q];
+    EV[c * ND + a] = ev;
+  }
+}
+
+// upper triangle (row-packed pairs) -> the staged element matrix, Dirichlet columns zero, and
+// the strong-Dirichlet lifting elvec -= elmat(:, j) g_j in column order, as k_integrate_poisson
+template <int P>
+__global__ void __launch_bounds__(256)
+    k_poisson_unpack(AsmGeom g, int64_t ncells, const int32_t* __restrict__ latdof, const double* __restrict__ gvals,
+                     const double* __restrict__ Cp, double* __restrict__ E, double* __restrict__ EV) {
+  using T = PoissonTC<P>;
+  constexpr int ND = T::ND, NPAIR = T::NPAIR;
+  __shared__ int32_t sgid[8][ND];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * 8 + wib;
+  if (c >= ncells) return;
+  const int ci = (int)(c % g.n[0]);
+  const int cj = (int)((c / g.n[0]) % g.n[1]);
+  const int ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
+  int32_t* gid = sgid[wib];
+  for (int s = lane; s < ND; s += 32) gid[s] = latdof[asm_node<P>(g, c, ci, cj, ck, s)];
+  __syncwarp();
+  const double* cp = Cp + c * NPAIR;
+  double* Ec = E + (size_t)c * ND * ND;
+  for (int idx = lane; idx < ND * ND; idx += 32) {
+    const int a = idx / ND, b = idx - a * ND;
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    Ec[idx] = gid[b] < 0 ? 0.0 : cp[lo * ND - lo * (lo - 1) / 2 + (hi - lo)];
+  }
+  bool any_dir = false;
+  for (int s = lane; s < ND; s += 32) any_dir |= gid[s] < 0;
+  if (!__any_sync(0xffffffffu, any_dir)) return;
+  for (int a = lane; a < ND; a += 32) {
+    double ev = EV[c * ND + a];
+    for (int b = 0; b < ND; ++b) {
+      const int32_t gb = gid[b];
+      const int lo = a < b ? a : b, hi = a < b ? b : a;
+      if (gb < 0) ev = ev - cp[lo * ND - lo * (lo - 1) / 2 + (hi - lo)] * gvals[-gb - 1];
+    }
+    EV[c * ND + a] = ev;
+  }
+}
+
 // warp per free row; CAP = power-of-two box capacity
 template <int P, int CAP, int W = 8>
 __global__ void __launch_bounds__(W * 32)
@@ -546,8 +669,8 @@ __global__ void __launch_bounds__(W * 32)
 // so they add exact zeros to positions that stay zero.  The slice's 32 x Bp
 // block is then written out with consecutive threads on consecutive addresses, FP64 and
 // FP32, padding included: no clearing pass and no CSR in between.
-template <int P, int NC, int W>
-__global__ void __launch_bounds__(W * 32)
+template <int P, int NC, int W, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB)
     k_scatter_stencil(AsmGeom g, const uint8_t* __restrict__ scls, const int64_t* __restrict__ voff,
                       const StencilClass* __restrict__ cls,
                       const int32_t* __restrict__ slot2row, const int32_t* __restrict__ free2lat,
@@ -587,11 +710,10 @@ __global__ void __launch_bounds__(W * 32)
     const int ncell = nci * ncj * nck;
     double v[8][BCH];
     int pos[8][BCH];
-    double ev[8];
+    double evl = 0.0;  // lane q: the element-vector entry of cell q
     // loads first (up to 8 cells x BCH columns per lane in flight), in increasing cell order
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      ev[q] = 0.0;
 #pragma unroll
       for (int h = 0; h < BCH; ++h) pos[q][h] = -1;
       if (q < ncell) {
@@ -611,7 +733,7 @@ __global__ void __launch_bounds__(W * 32)
             v[q][h] = __ldcs(Erow + b);
           }
         }
-        if (lane == 0) ev[q] = EV[c * ND + a];
+        if (lane == q) evl = EV[c * ND + a];
       }
     }
     double rsum = 0.0;
@@ -622,7 +744,7 @@ __global__ void __launch_bounds__(W * 32)
 #pragma unroll
         for (int h = 0; h < BCH; ++h)
           if (pos[q][h] >= 0) acc[pos[q][h]] = acc[pos[q][h]] + v[q][h];
-        rsum = rsum + ev[q];
+        rsum = rsum + __shfl_sync(0xffffffffu, evl, q);
         __syncwarp();
       }
     }
@@ -652,11 +774,14 @@ static fg_status launch_scatter_stencil(fg_system* sys, const AsmGeom& g) {
   fg_ctx* ctx = sp->mesh->ctx;
   constexpr int W = 8;
   const size_t smem = scatter_stencil_smem(sp);
-  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_scatter_stencil<P, NC, W>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // scalar Q1/Q2 rows fit three blocks per SM in 80 registers without spills (128^3 Q2: the
+  // whole assembly 73.2 -> 66.1 ms, identical results); Q3 and vector rows would spill
+  constexpr int MINB = (NC == 1 && P <= 2) ? 3 : 1;
+  auto kern = k_scatter_stencil<P, NC, W, MINB>;
+  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (sp->st_nslices > 0) {
     ctx->launches += 1;
-    k_scatter_stencil<P, NC, W><<<(unsigned)sp->st_nslices, W * 32, smem, ctx->stream>>>(
+    kern<<<(unsigned)sp->st_nslices, W * 32, smem, ctx->stream>>>(
         g, sp->d_st_scls, sp->d_st_voff, sp->d_st_cls, sp->d_st_slot2row, sp->d_free2lat, sp->d_latdof, sys->d_elmat, sys->d_elvec,
         sys->d_tval, sys->d_tval32, sys->d_rhs);
     FG_CUDA_TRY(cudaGetLastError());
@@ -740,28 +865,9 @@ fg_status system_interpolate_dirichlet(fg_system* sys, int boundary_fn, const do
 }
 
 template <int P>
-static fg_status launch_poisson(fg_system* sys) {
-  using S = PoissonShape<P>;
+static fg_status poisson_scatter(fg_system* sys, const AsmGeom& g) {
   fg_space* sp = sys->space;
   fg_ctx* ctx = sp->mesh->ctx;
-  AsmGeom g = make_geom(sp);
-  const int64_t ncells = sp->mesh->ncells;
-  SourceSpec src;
-  src.fn = sys->integ.source_fn;
-  for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
-  src.qp = sys->d_qpsrc;
-  const bool ff = (sys->integ.flags & FG_FAST_INTEGRATION) != 0;
-  using SF = typename PoissonShapeSel<P, true>::type;
-  const int warps = ff ? SF::WARPS : S::WARPS;
-  const size_t smem = ff ? SF::SM_BYTES_WARP * SF::WARPS : S::SM_BYTES_WARP * S::WARPS;
-  auto kern = ff ? k_integrate_poisson<P, true> : k_integrate_poisson<P, false>;
-  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const unsigned grid = nblk(ncells, warps);
-  ctx->launches += sp->nfree > 0 ? 2 : 1;
-  kern<<<grid, warps * 32, smem, ctx->stream>>>(g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof,
-                                                sys->d_gvals, sys->d_coef, sys->integ.coef_const, src,
-                                                sys->d_elmat, sys->d_elvec);
-  FG_CUDA_TRY(cudaGetLastError());
   const int64_t n = sp->nfree;
   if (sp->dg) return dg_assemble_rows(sys);
   if (sp->explicit_nodes) return usystem_scatter(sys);
@@ -769,12 +875,126 @@ static fg_status launch_poisson(fg_system* sys) {
   if (!sys->lean && stencil_direct_ok(sp) && sys->d_tval && sys->d_tval32) return launch_scatter_stencil<P, 1>(sys, g);
   if (n > 0) {
     constexpr int CAP = P == 1 ? 32 : (P == 2 ? 128 : 512);
+    ctx->launches += 1;
     k_scatter_rows<P, CAP><<<nblk(n, 8), 256, 0, ctx->stream>>>(g, n, sp->d_free2lat, sp->d_latdof, sp->d_rowptr,
                                                                  sp->d_col, sys->d_elmat, sys->d_elvec, sys->d_val,
                                                                  sys->d_val32, sys->d_rhs);
     FG_CUDA_TRY(cudaGetLastError());
   }
   return FG_OK;
+}
+
+// FG_TC_INTEGRATION: 0 the FP64-pipe and float-float kernels only; 1 Poisson element
+// matrices on the tensor cores where FP64 integration is asked for; 2 (default) also where
+// float-float is (FG_FAST_INTEGRATION): the tensor-core matrices are FP64-accurate and, on
+// GB300, faster than both (128^3 Q2: 77 ms per assembly against 192 ms FP64, 90 ms float-float)
+static int tc_integration_mode() {
+  const char* e = getenv("FG_TC_INTEGRATION");
+  const int v = e ? atoi(e) : 2;
+  return v < 0 ? 0 : (v > 2 ? 2 : v);
+}
+
+// scratch of the tensor-core path: G (cells x K), the packed upper triangles (cells x pairs),
+// the product's workspace and its error flag, 256-byte aligned pieces
+static size_t tc_align(size_t b) { return (b + 255) / 256 * 256; }
+
+template <int P>
+static fg_status launch_poisson_tc(fg_system* sys) {
+  using T = PoissonTC<P>;
+  constexpr int NQ = T::NQ, ND = T::ND, NPAIR = T::NPAIR, K = T::K;
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  cudaStream_t st = ctx->stream;
+  const int64_t ncells = sp->mesh->ncells;
+  if (!sp->d_tcT) {
+    // T[p][6q + m] for the row-packed upper pairs p = (a, b), b >= a
+    std::vector<double> hT((size_t)NPAIR * K);
+    const std::vector<double>& r = sp->tab.shg;  // (a NQ + q) 3 + j
+    size_t p = 0;
+    for (int a = 0; a < ND; ++a)
+      for (int b = a; b < ND; ++b, ++p)
+        for (int q = 0; q < NQ; ++q) {
+          const double* ra = &r[((size_t)a * NQ + q) * 3];
+          const double* rb = &r[((size_t)b * NQ + q) * 3];
+          double* t = &hT[p * K + 6 * q];
+          t[0] = ra[0] * rb[0];
+          t[1] = ra[1] * rb[1];
+          t[2] = ra[2] * rb[2];
+          t[3] = ra[0] * rb[1] + ra[1] * rb[0];
+          t[4] = ra[0] * rb[2] + ra[2] * rb[0];
+          t[5] = ra[1] * rb[2] + ra[2] * rb[1];
+        }
+    FG_TRY(dev_alloc(ctx, (void**)&sp->d_tcT, sizeof(double) * hT.size()));
+    FG_CUDA_TRY(cudaMemcpyAsync(sp->d_tcT, hT.data(), sizeof(double) * hT.size(), cudaMemcpyHostToDevice, st));
+    FG_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  const size_t gbytes = tc_align(sizeof(double) * ncells * K), cbytes = tc_align(sizeof(double) * ncells * NPAIR);
+  const size_t wbytes = tc_align(ozaki_workspace_bytes(ncells, NPAIR, K, false));
+  const size_t need = gbytes + cbytes + wbytes + 256;
+  if (!sys->d_tcbuf || sys->tcbuf_bytes < need) {
+    dev_free(ctx, sys->d_tcbuf);
+    sys->d_tcbuf = nullptr;
+    sys->tcbuf_bytes = 0;
+    FG_TRY(dev_alloc(ctx, &sys->d_tcbuf, need));
+    sys->tcbuf_bytes = need;
+  }
+  double* G = (double*)sys->d_tcbuf;
+  double* Cp = (double*)((uint8_t*)sys->d_tcbuf + gbytes);
+  void* work = (uint8_t*)sys->d_tcbuf + gbytes + cbytes;
+  int* d_err = (int*)((uint8_t*)work + wbytes);
+  AsmGeom g = make_geom(sp);
+  SourceSpec src;
+  src.fn = sys->integ.source_fn;
+  for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
+  src.qp = sys->d_qpsrc;
+  const size_t smem = T::SM_BYTES_WARP * T::WARPS;
+  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_poisson_geom<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_poisson_geom<P><<<nblk(ncells, T::WARPS), T::WARPS * 32, smem, st>>>(g, ncells, sp->mesh->d_coords, sp->dtab,
+                                                                       sp->d_latdof, sys->d_coef, sys->integ.coef_const,
+                                                                       src, G, sys->d_elvec);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+  FG_TRY(ozaki_gemm_nt(ctx, st, ncells, NPAIR, K, 1.0, G, K, 1, sp->d_tcT, K, 1, 0.0, Cp, NPAIR, 1, false, work, d_err));
+  k_poisson_unpack<P><<<nblk(ncells, 8), 256, 0, st>>>(g, ncells, sp->d_latdof, sys->d_gvals, Cp, sys->d_elmat,
+                                                       sys->d_elvec);
+  FG_CUDA_TRY(cudaGetLastError());
+  ctx->launches += 2;
+  int h_err = 0;
+  FG_CUDA_TRY(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  FG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h_err) {
+    set_error("element matrices on the tensor cores: a bounded device wait ran out");
+    return (fg_status)h_err;
+  }
+  return poisson_scatter<P>(sys, g);
+}
+
+template <int P>
+static fg_status launch_poisson(fg_system* sys) {
+  using S = PoissonShape<P>;
+  fg_space* sp = sys->space;
+  fg_ctx* ctx = sp->mesh->ctx;
+  const bool ff = (sys->integ.flags & FG_FAST_INTEGRATION) != 0;
+  const int tcm = tc_integration_mode();
+  if (!sp->dg && sp->mesh->ncells > 0 && (ff ? tcm == 2 : tcm >= 1)) return launch_poisson_tc<P>(sys);
+  AsmGeom g = make_geom(sp);
+  const int64_t ncells = sp->mesh->ncells;
+  SourceSpec src;
+  src.fn = sys->integ.source_fn;
+  for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
+  src.qp = sys->d_qpsrc;
+  using SF = typename PoissonShapeSel<P, true>::type;
+  const int warps = ff ? SF::WARPS : S::WARPS;
+  const size_t smem = ff ? SF::SM_BYTES_WARP * SF::WARPS : S::SM_BYTES_WARP * S::WARPS;
+  auto kern = ff ? k_integrate_poisson<P, true> : k_integrate_poisson<P, false>;
+  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned grid = nblk(ncells, warps);
+  ctx->launches += 1;
+  kern<<<grid, warps * 32, smem, ctx->stream>>>(g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_latdof,
+                                                sys->d_gvals, sys->d_coef, sys->integ.coef_const, src,
+                                                sys->d_elmat, sys->d_elvec);
+  FG_CUDA_TRY(cudaGetLastError());
+  return poisson_scatter<P>(sys, g);
 }
 
 // ---------------------------------------------------------------------------

@@ -156,6 +156,7 @@ struct fg_space {
   int32_t* d_st_slot2row = nullptr;  // 32*st_nslices: free row of each row slot (-1: padding)
   int st_max_bp = 0;              // largest Bp of the classes
   std::vector<fg::StencilClass> h_st_cls;
+  double* d_tcT = nullptr;        // Poisson element tensor T (upper pairs x 6 NQ), tensor-core path
   // unstructured mesh: nodes (nlat of them) are vertices, edge, face and cell interior nodes
   int32_t* d_cellnode = nullptr;  // nn*ncells node ids
   int64_t* d_nptr = nullptr;      // nlat+1 offsets of the cells around each node
@@ -191,6 +192,8 @@ struct fg_system {
   float* d_val32s = nullptr;      // st_nvals (lattice-implicit) or sell_nnz (SELL) values
   double* d_sdiag = nullptr;      // nvec
   bool scaled_valid = false;      // d_val32s matches the current values
+  void* d_tcbuf = nullptr;        // scratch of the tensor-core element matrices (fg_assembly.cu)
+  size_t tcbuf_bytes = 0;
   // solver work vectors (allocated on first solve)
   double* d_work = nullptr;       // FP64 work area
   float* d_work32 = nullptr;      // FP32 work area

@@ -322,11 +322,13 @@ def test_order_4_reported_unsupported(fg, ctx):
         fg.FEAffineOperator(sp, fg.ElasticityIntegration(cell_coef=np.ones(8), nu=0.3)).compute()
 
 
+@pytest.mark.parametrize("tc", ["0", "2"], ids=["float_float", "tensor_cores"])
 @pytest.mark.parametrize("order", [1, 2, 3])
-def test_fast_integration_matrix_and_mixed_solution(fg, ctx, order):
-    """FG_FAST_INTEGRATION (float-float element matrices): entries within 1e-12 of the
-    row scale of the FP64 integration (the reference-parity one), pattern identical, and the
-    mixed solve on it within 1e-9 of the FP64 drop-in's solution."""
+def test_fast_integration_matrix_and_mixed_solution(fg, ctx, order, tc, monkeypatch):
+    """FG_FAST_INTEGRATION element matrices -- float-float (FG_TC_INTEGRATION=0) or, by default,
+    the tensor-core product: entries within 1e-12 of the row scale of the FP64-pipe
+    integration (the reference-parity one), pattern identical, and the mixed solve on them
+    within 1e-9 of the FP64 drop-in's solution."""
     n = (5, 4, 6)
     xyz = perturbed_vertices(n, 0.15, seed=21)
     k = np.exp(np.random.default_rng(2).normal(size=n[0] * n[1] * n[2]))
@@ -334,6 +336,7 @@ def test_fast_integration_matrix_and_mixed_solution(fg, ctx, order):
     sp = fg.SerialFESpace(tri, order=order, dirichlet_ids=list(range(1, 27)))
     sols, mats = [], []
     for fast in (False, True):
+        monkeypatch.setenv("FG_TC_INTEGRATION", tc if fast else "0")
         op = fg.FEAffineOperator(sp, fg.PoissonIntegration(cell_coef=k, source_fn=O.FN_CONST, fn_param=[1.0],
                                                            fast_integration=fast)).compute()
         mats.append(op.get_matrix())
