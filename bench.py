@@ -362,7 +362,8 @@ def main():
     t_symbolic = time.perf_counter() - t0
     coef_dev = torch.from_numpy(coef).to(f"cuda:{local}")
     integ_dev = fg.PoissonIntegration(cell_coef=coef_dev, source_fn=fg.FG_FN_CONST, fn_param=[1.0])
-    # the mixed arm integrates in float-float (FG_FAST_INTEGRATION); the FP64 drop-in in FP64
+    # the mixed arm asks for fast integration (FG_FAST_INTEGRATION), the FP64 drop-in for FP64;
+    # by default both get the tensor-core element matrices (FG_TC_INTEGRATION=2)
     integ_fast = fg.PoissonIntegration(cell_coef=coef_dev, source_fn=fg.FG_FN_CONST, fn_param=[1.0],
                                        fast_integration=True)
     op = fg.FEAffineOperator(space, integ_dev).compute()
@@ -524,7 +525,8 @@ def main():
         "p50_ms": srt[len(srt) // 2], "p99_ms": srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))],
         "iterations": imx[-1]["iterations"], "outer_iterations": imx[-1]["outer_iterations"],
         "assembly_ms": ms_asm, "assembly_fp64_ms": ms_asm64,
-        "mixed_integration": "float-float element matrices (FG_FAST_INTEGRATION); the fp64 arm integrates in FP64",
+        "mixed_integration": "element matrices of both arms: one emulated-FP64 tensor-core product of the cells' "
+                             "geometric factors with the shared reference-gradient table (FG_TC_INTEGRATION=2)",
         "solve_ms": imx[-1]["solve_ms"],
         "error_vs_fp64": err_vs_fp64,
         "error_vs_oracle": oracle_err,
