@@ -2,10 +2,13 @@
 matrices (``python -m fempar_gb300.bench_assembly --n 128``).
 
 Modes (FG_TC_INTEGRATION with the integrand's precision request):
-  fp64_pipe   FP64 integration kernel (k_integrate_poisson<P, false>)
-  float_float float-float integration kernel (k_integrate_poisson<P, true>)
-  tensor_core one emulated-FP64 tcgen05 product of the cells' geometric factors with the shared
-              reference-gradient table (k_poisson_geom, k_oz_gemm, k_poisson_unpack)
+  fp64_pipe        FP64 integration kernel (k_integrate_poisson<P, false>)
+  float_float      float-float integration kernel (k_integrate_poisson<P, true>)
+  tensor_core_fp64 one emulated-FP64 tcgen05 product of the cells' geometric factors with the
+                   shared reference-gradient table (k_poisson_geom, k_oz_gemm, k_poisson_unpack):
+                   the FP64 request's default
+  tensor_core      the same with the geometric factors in float-float (k_poisson_geom_ff): the
+                   fast request's default (the mixed solver's)
 Each assembly includes the row gather into the solver layout.  The mesh is the unit cube with
 interior vertices moved by U(+-0.15 h) and k = exp(N(0,1)) per cell, f = 1, u = 0 on the
 boundary (seeded).  Times are CUDA events on the library's stream, the minimum of --reps
@@ -36,14 +39,15 @@ def workload(n: int, seed: int = SEED):
     return np.ascontiguousarray(xyz.ravel()), np.exp(rng.normal(0.0, 1.0, size=n ** 3))
 
 
-MODES = {"fp64_pipe": ("0", False), "float_float": ("0", True), "tensor_core": ("2", True)}
+MODES = {"fp64_pipe": ("0", False), "float_float": ("0", True), "tensor_core_fp64": ("2", False),
+         "tensor_core": ("2", True)}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--reps", type=int, default=3)
-    ap.add_argument("--modes", default="fp64_pipe,float_float,tensor_core")
+    ap.add_argument("--modes", default="fp64_pipe,float_float,tensor_core_fp64,tensor_core")
     args = ap.parse_args()
     import torch
     import fempar_gb300 as fg

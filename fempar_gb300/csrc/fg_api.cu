@@ -373,6 +373,7 @@ static void space_free(fg_space* sp) {
   dev_free(ctx, sp->d_row2st);
   dev_free(ctx, sp->d_st_slot2row);
   dev_free(ctx, sp->d_tcT);
+  dev_free(ctx, sp->d_tcff);
   delete sp;
 }
 

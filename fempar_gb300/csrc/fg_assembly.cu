@@ -175,6 +175,31 @@ __device__ __forceinline__ void ff_split(double v, float& h, float& l) {
   h = (float)v;
   l = (float)(v - (double)h);
 }
+// (h, l) = a * b
+__device__ __forceinline__ void ff_mul(float ah, float al, float bh, float bl, float& h, float& l) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, fmaf(al, bh, e));
+  h = p + e;
+  l = e - (h - p);
+}
+// (h, l) = a + b
+__device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, float& h, float& l) {
+  float sh, e;
+  ff_two_sum(ah, bh, sh, e);
+  e += al + bl;
+  h = sh + e;
+  l = e - (h - sh);
+}
+// (h, l) = 1 / a: FP32 reciprocal and one Newton step in float-float
+__device__ __forceinline__ void ff_recip(float ah, float al, float& h, float& l) {
+  const float r = 1.0f / ah;
+  float ph, pl, eh, el, ch, cl;
+  ff_mul(ah, al, r, 0.f, ph, pl);
+  ff_add(1.0f, 0.f, -ph, -pl, eh, el);  // 1 - a r
+  ff_mul(r, 0.f, eh, el, ch, cl);
+  ff_add(r, 0.f, ch, cl, h, l);
+}
 
 // Per cell: vertex coordinates, the dofs' global ids (negative: Dirichlet), and per Gauss
 // point J^-1 (invmtx order), |det J| w_q and the source value.  Reference: sbm_cell_map.i90:
@@ -542,6 +567,154 @@ __global__ void __launch_bounds__(PoissonTC<P>::WARPS * 32)
     double ev = 0.0;
     for (int q = 0; q < NQ; ++q) ev = ev + fsrc[q] * tb.shp[(size_t)a * NQ + q];
     EV[c * ND + a] = ev;
+  }
+}
+
+// The same in float-float (FP32 pairs, ~2^-44 relative), for fast-integration requests: the
+// Jacobian, invmtx, |det J| w k J^-1 J^-T and the source part of the element vector run on the
+// FP32 pipe (GB300's FP64 rate is ~1/70 of FP32's).  ff tables: the Q1 geometry gradients
+// (8 x NQ x 3), the shape values (ND x NQ) and the weights (NQ), hi then lo.
+template <int P>
+struct PoissonTCFF {
+  static constexpr int NQ = PoissonTC<P>::NQ, ND = PoissonTC<P>::ND;
+  static constexpr int WARPS = 8;
+  static constexpr int G3 = 8 * NQ * 3, SH = ND * NQ;
+  static constexpr int TAB = 2 * (G3 + SH + NQ);  // floats of the table
+  // per warp: vertices (24 pairs), J^-1 (9 pairs per point), det, |det| w k, |det| w f (pairs)
+  static constexpr int SM_FLOATS = 48 + NQ * 18 + NQ * 2 * 3;
+  static constexpr size_t SM_BYTES_WARP = ((size_t)SM_FLOATS * 4 + 15) / 16 * 16;
+};
+
+template <int P>
+__global__ void __launch_bounds__(PoissonTCFF<P>::WARPS * 32)
+    k_poisson_geom_ff(AsmGeom g, int64_t ncells, const double* __restrict__ coords, DevTables tb,
+                      const float* __restrict__ tab, const double* __restrict__ coef, double coef_const, SourceSpec src,
+                      double* __restrict__ G, double* __restrict__ EV) {
+  using T = PoissonTCFF<P>;
+  constexpr int NQ = T::NQ, ND = T::ND, K = PoissonTC<P>::K;
+  extern __shared__ float fsm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float* xvh = fsm + (size_t)wib * (T::SM_BYTES_WARP / 4);
+  float* xvl = xvh + 24;
+  float* bh = xvl + 24;      // NQ x 9
+  float* bl = bh + NQ * 9;
+  float* dh = bl + NQ * 9;   // det
+  float* dl = dh + NQ;
+  float* kh = dl + NQ;       // |det| w k
+  float* kl = kh + NQ;
+  float* wh = kl + NQ;       // |det| w f
+  float* wl = wh + NQ;
+  const float* gh = tab;
+  const float* gl = gh + T::G3;
+  const float* shh = gl + T::G3;
+  const float* shl = shh + T::SH;
+  const float* qwh = shl + T::SH;
+  const float* qwl = qwh + NQ;
+  const int64_t c = (int64_t)blockIdx.x * T::WARPS + wib;
+  if (c >= ncells) return;
+  const int ci = (int)(c % g.n[0]);
+  const int cj = (int)((c / g.n[0]) % g.n[1]);
+  const int ck = (int)(c / ((int64_t)g.n[0] * g.n[1]));
+  float kch, kcl;
+  ff_split(coef ? coef[c] : coef_const, kch, kcl);
+  // vertex coordinates relative to vertex 0, taken in FP64: J = sum_k grad N_k x_k = sum_k
+  // grad N_k (x_k - x_0) (the gradients sum to zero), so the O(h) Jacobian is not a
+  // cancellation of O(1) coordinates in float-float
+  const int64_t v0 = asm_vertex(g, c, ci, cj, ck, 0);
+  if (lane < 24)
+    ff_split(coords[asm_vertex(g, c, ci, cj, ck, lane / 3) * 3 + lane % 3] - coords[v0 * 3 + lane % 3], xvh[lane],
+             xvl[lane]);
+  __syncwarp();
+  for (int q = lane; q < NQ; q += 32) {
+    float Jh[9], Jl[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const float th = gh[(k * NQ + q) * 3 + j], tl = gl[(k * NQ + q) * 3 + j];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) ff_fma(th, tl, xvh[k * 3 + i], xvl[k * 3 + i], ah[i], al[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        ff_renorm(ah[i], al[i]);
+        Jh[i + 3 * j] = ah[i];
+        Jl[i + 3 * j] = al[i];
+      }
+    }
+    // invmtx cofactors: x = a b - c d as two products and a sum
+    auto cof = [&](int a, int b, int cc, int d, float& h, float& l) {
+      float ph, pl, mh, ml;
+      ff_mul(Jh[a], Jl[a], Jh[b], Jl[b], ph, pl);
+      ff_mul(Jh[cc], Jl[cc], Jh[d], Jl[d], mh, ml);
+      ff_add(ph, pl, -mh, -ml, h, l);
+    };
+    float c0h, c0l, c1h, c1l, c2h, c2l, c3h, c3l, c4h, c4l, c5h, c5l, c6h, c6l, c7h, c7l, c8h, c8l;
+    cof(4, 8, 5, 7, c0h, c0l);  // t1
+    cof(2, 7, 1, 8, c1h, c1l);  // t2
+    cof(1, 5, 2, 4, c2h, c2l);  // t3
+    cof(5, 6, 3, 8, c3h, c3l);
+    cof(0, 8, 2, 6, c4h, c4l);
+    cof(3, 2, 0, 5, c5h, c5l);
+    cof(3, 7, 4, 6, c6h, c6l);
+    cof(1, 6, 0, 7, c7h, c7l);
+    cof(0, 4, 1, 3, c8h, c8l);
+    float deth, detl, th, tl;
+    ff_mul(Jh[0], Jl[0], c0h, c0l, deth, detl);
+    ff_mul(Jh[3], Jl[3], c1h, c1l, th, tl);
+    ff_add(deth, detl, th, tl, deth, detl);
+    ff_mul(Jh[6], Jl[6], c2h, c2l, th, tl);
+    ff_add(deth, detl, th, tl, deth, detl);
+    float rh, rl;
+    ff_recip(deth, detl, rh, rl);
+    const float ch[9] = {c0h, c1h, c2h, c3h, c4h, c5h, c6h, c7h, c8h};
+    const float cl[9] = {c0l, c1l, c2l, c3l, c4l, c5l, c6l, c7l, c8l};
+#pragma unroll
+    for (int m = 0; m < 9; ++m) ff_mul(ch[m], cl[m], rh, rl, bh[q * 9 + m], bl[q * 9 + m]);
+    dh[q] = deth;
+    dl[q] = detl;
+  }
+  __syncwarp();
+  const bool neg = dh[0] < 0.f;  // reference: |det| everywhere if the first one is negative
+  for (int q = lane; q < NQ; q += 32) {
+    float ah = dh[q], al = dl[q];
+    if (neg && ah < 0.f) { ah = -ah; al = -al; }
+    float fh, fl;
+    ff_mul(ah, al, qwh[q], qwl[q], fh, fl);  // |det J| w
+    ff_mul(fh, fl, kch, kcl, kh[q], kl[q]);
+    double f;
+    if (src.fn == FG_FN_SHARP_WAVE) {  // x = x_0 + sum_k N_k (x_k - x_0)
+      double x[3] = {coords[v0 * 3], coords[v0 * 3 + 1], coords[v0 * 3 + 2]};
+      for (int k = 0; k < 8; ++k)
+        for (int i = 0; i < 3; ++i)
+          x[i] = x[i] + tb.gshp[k * NQ + q] * ((double)xvh[k * 3 + i] + (double)xvl[k * 3 + i]);
+      f = sharp_wave_source(src.prm, x);
+    } else if (src.fn == FG_FN_QP_VALUES) f = src.qp[c * NQ + q];
+    else if (src.fn == FG_FN_CONST) f = src.prm[0];
+    else f = 0.0;
+    float sh, sl;
+    ff_split(f, sh, sl);
+    ff_mul(fh, fl, sh, sl, wh[q], wl[q]);
+  }
+  __syncwarp();
+  for (int e = lane; e < K; e += 32) {
+    const int q = e / 6, m = e - 6 * q;
+    const int j = m < 3 ? m : (m == 5 ? 1 : 0), k = m < 3 ? m : (m == 3 ? 1 : 2);
+    const float* b0 = bh + q * 9;
+    const float* b1 = bl + q * 9;
+    float sh = 0.f, sl = 0.f;
+#pragma unroll
+    for (int l = 0; l < 3; ++l) ff_fma(b0[j + 3 * l], b1[j + 3 * l], b0[k + 3 * l], b1[k + 3 * l], sh, sl);
+    ff_renorm(sh, sl);
+    float vh, vl;
+    ff_mul(kh[q], kl[q], sh, sl, vh, vl);
+    G[c * K + e] = (double)vh + (double)vl;
+  }
+  for (int a = lane; a < ND; a += 32) {
+    float sh = 0.f, sl = 0.f;
+    for (int q = 0; q < NQ; ++q) ff_fma(wh[q], wl[q], shh[a * NQ + q], shl[a * NQ + q], sh, sl);
+    EV[c * ND + a] = (double)sh + (double)sl;
   }
 }
 
@@ -938,6 +1111,25 @@ static fg_status launch_poisson_tc(fg_system* sys) {
     FG_TRY(dev_alloc(ctx, &sys->d_tcbuf, need));
     sys->tcbuf_bytes = need;
   }
+  const bool ff = (sys->integ.flags & FG_FAST_INTEGRATION) != 0;
+  if (ff && !sp->d_tcff) {
+    // float-float tables of the geometry kernel: Q1 geometry gradients, shape values, weights
+    using F = PoissonTCFF<P>;
+    std::vector<float> h(F::TAB);
+    auto split = [&](const std::vector<double>& src, size_t n, float* hi, float* lo) {
+      for (size_t i = 0; i < n; ++i) {
+        hi[i] = (float)src[i];
+        lo[i] = (float)(src[i] - (double)hi[i]);
+      }
+    };
+    float* t = h.data();
+    split(sp->tab.gshg, F::G3, t, t + F::G3);
+    split(sp->tab.shp, F::SH, t + 2 * F::G3, t + 2 * F::G3 + F::SH);
+    split(sp->tab.qw, NQ, t + 2 * (F::G3 + F::SH), t + 2 * (F::G3 + F::SH) + NQ);
+    FG_TRY(dev_alloc(ctx, (void**)&sp->d_tcff, sizeof(float) * h.size()));
+    FG_CUDA_TRY(cudaMemcpyAsync(sp->d_tcff, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice, st));
+    FG_CUDA_TRY(cudaStreamSynchronize(st));
+  }
   double* G = (double*)sys->d_tcbuf;
   double* Cp = (double*)((uint8_t*)sys->d_tcbuf + gbytes);
   void* work = (uint8_t*)sys->d_tcbuf + gbytes + cbytes;
@@ -947,11 +1139,21 @@ static fg_status launch_poisson_tc(fg_system* sys) {
   src.fn = sys->integ.source_fn;
   for (int i = 0; i < 8; ++i) src.prm[i] = sys->integ.fn_param[i];
   src.qp = sys->d_qpsrc;
-  const size_t smem = T::SM_BYTES_WARP * T::WARPS;
-  FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_poisson_geom<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_poisson_geom<P><<<nblk(ncells, T::WARPS), T::WARPS * 32, smem, st>>>(g, ncells, sp->mesh->d_coords, sp->dtab,
-                                                                       sp->d_latdof, sys->d_coef, sys->integ.coef_const,
-                                                                       src, G, sys->d_elvec);
+  if (ff) {
+    using F = PoissonTCFF<P>;
+    const size_t smem = F::SM_BYTES_WARP * F::WARPS;
+    FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_poisson_geom_ff<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    k_poisson_geom_ff<P><<<nblk(ncells, F::WARPS), F::WARPS * 32, smem, st>>>(
+        g, ncells, sp->mesh->d_coords, sp->dtab, sp->d_tcff, sys->d_coef, sys->integ.coef_const, src, G, sys->d_elvec);
+  } else {
+    const size_t smem = T::SM_BYTES_WARP * T::WARPS;
+    FG_CUDA_TRY(cudaFuncSetAttribute((const void*)k_poisson_geom<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    k_poisson_geom<P><<<nblk(ncells, T::WARPS), T::WARPS * 32, smem, st>>>(g, ncells, sp->mesh->d_coords, sp->dtab,
+                                                                         sp->d_latdof, sys->d_coef,
+                                                                         sys->integ.coef_const, src, G, sys->d_elvec);
+  }
   FG_CUDA_TRY(cudaGetLastError());
   FG_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
   FG_TRY(ozaki_gemm_nt(ctx, st, ncells, NPAIR, K, 1.0, G, K, 1, sp->d_tcT, K, 1, 0.0, Cp, NPAIR, 1, false, work, d_err));

@@ -157,6 +157,7 @@ struct fg_space {
   int st_max_bp = 0;              // largest Bp of the classes
   std::vector<fg::StencilClass> h_st_cls;
   double* d_tcT = nullptr;        // Poisson element tensor T (upper pairs x 6 NQ), tensor-core path
+  float* d_tcff = nullptr;        // float-float tables of its fast-integration geometry kernel
   // unstructured mesh: nodes (nlat of them) are vertices, edge, face and cell interior nodes
   int32_t* d_cellnode = nullptr;  // nn*ncells node ids
   int64_t* d_nptr = nullptr;      // nlat+1 offsets of the cells around each node

@@ -12,8 +12,10 @@ Checks here:
   (FG_TC_INTEGRATION=0).  Right-hand side (source part and the strong-Dirichlet lifting
   through the unpacked element matrices): within 1e-14 of its largest entry.  Q1-Q3,
   perturbed vertices, lognormal coefficients, sharp-wave Dirichlet data.
-* With mode 2, the mixed-precision solve on these element matrices reaches the FP64
-  drop-in's solution to 1e-9.
+* Fast-integration requests compute the geometric factors G in float-float on the FP32
+  pipe.  Their matrices must be within 1e-12 of the FP64-pipe kernel's, the float-float
+  kernel's bar.  The mixed-precision solve on them reaches the FP64 drop-in's solution
+  to 1e-9.
 * A bounded wait of the product that runs out (test switch) makes the assembly return
   FG_ERR_TIMEOUT; the next assembly on the same context is correct.
 """
@@ -87,6 +89,20 @@ def test_tensor_core_element_matrices_match_fp64_pipe(fg, ctx, monkeypatch, n, o
     monkeypatch.setenv("FG_TC_INTEGRATION", "1")
     tc = matrix_rhs(op.compute())
     assert_close(tc, ref, 1e-14)
+
+
+@pytest.mark.parametrize("n,order", [((14, 11, 9), 1), ((10, 9, 8), 2), ((6, 5, 7), 3)])
+def test_fast_requests_float_float_geometry(fg, ctx, monkeypatch, n, order):
+    """Fast-integration requests run the geometric factors in float-float (FP32 pipe): matrix
+    and right-hand side within 1e-12 of the FP64-pipe kernel's (the float-float integration
+    kernel's bar; measured ~1e-14)."""
+    tri, sp, op = operator(fg, ctx, n, order)
+    monkeypatch.setenv("FG_TC_INTEGRATION", "0")
+    ref = matrix_rhs(op.compute())
+    _, _, op2 = operator(fg, ctx, n, order, fast=True)
+    monkeypatch.setenv("FG_TC_INTEGRATION", "2")
+    ff = matrix_rhs(op2.compute())
+    assert_close(ff, ref, 1e-12)
 
 
 def test_mixed_solve_on_tensor_core_element_matrices(fg, ctx, monkeypatch):
