@@ -1178,7 +1178,12 @@ static fg_status launch_poisson(fg_system* sys) {
   fg_ctx* ctx = sp->mesh->ctx;
   const bool ff = (sys->integ.flags & FG_FAST_INTEGRATION) != 0;
   const int tcm = tc_integration_mode();
-  if (!sp->dg && sp->mesh->ncells > 0 && (ff ? tcm == 2 : tcm >= 1)) return launch_poisson_tc<P>(sys);
+  if (!sp->dg && sp->mesh->ncells > 0 && (ff ? tcm == 2 : tcm >= 1)) {
+    // the tensor-core path needs scratch (G, packed triangles, digits: ~7 KB per Q2 cell);
+    // where the context's HBM budget has no room for it, the direct kernels run instead
+    const fg_status s = launch_poisson_tc<P>(sys);
+    if (s != FG_ERR_OOM) return s;
+  }
   AsmGeom g = make_geom(sp);
   const int64_t ncells = sp->mesh->ncells;
   SourceSpec src;

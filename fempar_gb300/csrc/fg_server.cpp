@@ -121,7 +121,13 @@ static fg_status footprint(const fg_request* q, uint64_t* bytes, int64_t* nfree_
   // requests are assembled lean (FG_LEAN_SYSTEM): the element matrices are released before
   // the solver layout is allocated, the CSR after it is filled, so the peak is the larger of
   // (element matrices + CSR) and (CSR + solver layout), plus what lives throughout
-  const double elm = ncells * nd * nd * 8 + ncells * nd * 8;  // element matrices and vectors
+  double elm = ncells * nd * nd * 8 + ncells * nd * 8;  // element matrices and vectors
+  if (ncomp == 1) {
+    // Poisson element matrices on the tensor cores: geometric factors (K = 6 NQ per cell),
+    // packed upper triangles and the digit workspace (7 bf16 digits, K padded to 16)
+    const double K = 6.0 * t.nq, npair = nd * (nd + 1) / 2;
+    elm += ncells * (K * 8 + npair * 8 + std::ceil(K / 16.0) * 16 * 7 * 2) + npair * K * 8;
+  }
   const double csr = nnz * (4 + 8) + nfree * 8.0;             // CSR pattern + FP64 values + row pointers
   const double lay = nnz * 1.15 * (8 + 4);                    // solver layout FP64 + FP32 (padding)
   double b = std::max(elm, lay) + csr;

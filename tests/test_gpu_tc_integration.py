@@ -18,6 +18,8 @@ Checks here:
   to 1e-9.
 * A bounded wait of the product that runs out (test switch) makes the assembly return
   FG_ERR_TIMEOUT; the next assembly on the same context is correct.
+* Where the context's HBM budget has no room for the product's scratch, the assembly runs
+  the FP64-pipe kernel instead: same matrix bit for bit.
 """
 import numpy as np
 import pytest
@@ -134,3 +136,20 @@ def test_bounded_wait_runs_out_in_the_assembly(fg, ctx, monkeypatch):
     assert "FG_ERR_TIMEOUT" in str(ei.value)
     monkeypatch.delenv("FG_OZ_TEST_DROP_STAGE")
     assert_close(matrix_rhs(op.compute()), ref, 1e-14)
+
+
+def test_budget_without_room_for_the_product_falls_back(fg, ctx, monkeypatch):
+    n = (12, 10, 8)
+    monkeypatch.setenv("FG_TC_INTEGRATION", "0")
+    ca = fg.Context(0)
+    _, _, opa = operator(fg, ca, n, 2, seed=5)
+    ref = matrix_rhs(opa.compute())
+    used_direct = ca.memory()[0]
+    monkeypatch.setenv("FG_TC_INTEGRATION", "2")
+    opa.compute()
+    assert ca.memory()[0] - used_direct > 4 << 20   # the product's scratch is held by the system
+    cb = fg.Context(0, hbm_budget_bytes=used_direct + (2 << 20))
+    _, _, opb = operator(fg, cb, n, 2, seed=5)
+    got = matrix_rhs(opb.compute())
+    assert np.array_equal(got[2], ref[2]) and np.array_equal(got[3], ref[3])
+    assert cb.memory()[0] <= used_direct + (2 << 20)
