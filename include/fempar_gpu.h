@@ -63,11 +63,17 @@ enum {
  * BDDC on such a system return FG_ERR_UNSUPPORTED.  Peak device memory of an assembly drops
  * from elmat + CSR + layout to max(elmat + CSR, CSR + layout). */
 enum { FG_INPUTS_ON_DEVICE = 1, FG_LEAN_SYSTEM = 2, FG_FAST_INTEGRATION = 4 };
-/* FG_FAST_INTEGRATION (Poisson): element matrices accumulated in float-float (pairs of FP32
- * with error-free products, ~2^-48 relative) instead of FP64 — several times faster on
- * GB300, whose FP64 rate is ~1/70 of FP32; entries agree with the FP64 integration to
- * ~1e-13 of the row scale.  Meant for FG_MIXED solves (the FP64 copy of the matrix then feeds
- * the residual refinement); the default FP64 integration is the one with reference parity. */
+/* Poisson element matrices.  By default those of all cells are one FP64 product, emulated on
+ * the tensor cores: the cells' geometric factors times a table shared by all cells.  They
+ * match the FP64-pipe integration to ~1e-15 of the row scale, with reference parity.
+ * FG_FAST_INTEGRATION asks for float-float accuracy (~2^-44, meant for FG_MIXED solves, whose
+ * FP64 copy of the matrix feeds the residual refinement).  Its geometric factors are then
+ * computed in float-float on the FP32 pipe (GB300's FP64 rate is ~1/70 of FP32's): ~2e-14 of
+ * the row scale.  The environment variable FG_TC_INTEGRATION selects the path: 2 (default)
+ * the tensor cores for both requests; 1 for FP64 requests only, with the float-float
+ * integration kernel (~2e-13) for fast ones; 0 neither.  Where the context's HBM budget has
+ * no room for the product's scratch (~7 KB per Q2 cell), the assembly uses the direct
+ * kernels. */
 
 typedef struct {
   int kind;                        /* FG_POISSON / FG_ELASTICITY                     */
