@@ -8,21 +8,25 @@
 // K. Ozaki, R. Yokota, "DGEMM on integer matrix multiplication unit", IJHPCA 2024), with
 // bf16 digits instead of int8 ones because this part's int8 MMA rate is low:
 //
-//   * every row i of an operand gets a power of two 2^e_i with |x_il| 2^-e_i < 1/2 and is cut
+//   * every row i of an operand gets a power of two 2^e_i with |x_il| 2^-e_i < 1/4 and is cut
 //     into S = 7 signed digits, x_il = 2^e_i sum_s d_s 2^(-8(s+1)) (+ a tail below
-//     2^(e_i-57)), |d_s| <= 128, so every digit is an exact bf16.  The cut is integer
-//     arithmetic on the FP64 bit pattern (56 fraction bits, digits rounded to nearest);
+//     2^(e_i-56)), |d_0| <= 64, |d_s| <= 128, so every digit is an exact bf16.  The cut is
+//     integer arithmetic on the FP64 bit pattern (56 fraction bits, 54 of them below the row
+//     maximum, digits rounded to nearest);
 //   * the digit matrices are multiplied by tcgen05.mma kind::f16 (bf16 x bf16 -> FP32).  A
-//     digit product is at most 2^14, and an accumulator sums at most 7 pairs over K <= 128:
-//     every FP32 partial sum is an integer below 2^24, i.e. exact;
+//     digit product is at most 2^14 (2^13 with a leading digit), and an accumulator sums at
+//     most the equivalent of 6 full pairs (class 6: two leading-digit pairs and five others;
+//     class 7: six others) over at most 170 K values: every FP32 partial sum is an integer
+//     below 6 2^14 170 < 2^24, i.e. exact.  K up to 170 is one exact chunk (the Poisson
+//     element matrices' K = 162 among them), longer K is cut into chunks of 160;
 //   * the products of weight 2^(-8k), k = s + t = 0..7 (34 digit pairs), go to 8 FP32
 //     accumulators in tensor memory (8 x 64 columns: all 512); pairs with s + t >= 8 are
-//     dropped (|error| <~ K 2^-59 max_l |x_il| max_l |y_jl|).  The cut keeps 56 bits below
-//     2^e_i, so a value far below its row's maximum loses its low bits: overall the product
-//     is within ~K 2^-53 max|x_i.| max|y_j.| of the exact one (the FP64 dot-product bound);
+//     dropped (|error| <~ K 2^-57 max_l |x_il| max_l |y_jl|).  The cut keeps 54 bits below
+//     the row maximum, so a value far below it loses its low bits: overall the product is
+//     within ~K 2^-52 max|x_i.| max|y_j.| of the exact one (about the FP64 dot-product bound);
 //   * the epilogue converts the 8 class sums to integers, combines them exactly in int64,
 //     turns the chunk's sum into FP64 with one rounding (two exact conversions by bit
-//     arithmetic, one addition), adds the K chunks of 128 in FP64, applies the power of two
+//     arithmetic, one addition), adds the K chunks in FP64, applies the power of two
 //     2^(e_i + f_j - 16) through the exponent field and updates C: about two FP64
 //     operations per output element and chunk instead of 128.  (A rounding by integer
 //     arithmetic alone measured slower: 421 vs 330 us at 4096 x 4096 x 128.)
@@ -56,7 +60,8 @@ namespace {
 constexpr int OZ_S = 7;                       // digits per value
 constexpr int OZ_NACC = 8;                    // accumulators: digit weights k = s + t = 0..7
 constexpr int OZ_BM = 128, OZ_BK = 16;
-constexpr int OZ_CHUNK = 8;                   // K steps per exact accumulation (K <= 128)
+constexpr int OZ_KEXACT = 170;                // K values one exact accumulation may sum
+constexpr int OZ_CHUNK_STEPS = 10;            // K steps of a chunk when K > OZ_KEXACT (160 values)
 constexpr uint32_t OZ_BLOCK = OZ_BM * OZ_BK * 2;           // one digit block: 4096 B
 constexpr uint32_t OZ_A_BYTES = OZ_S * OZ_BLOCK;           // 28672 B per K step
 constexpr uint32_t OZ_TMEM_COLS = 512;                     // all of it
@@ -198,7 +203,7 @@ __device__ __forceinline__ OzSplit split_of(const OzSplitArgs& a, int rtile) {
   return a.items[lo];
 }
 
-// Row exponents: e_r with max_l |x_rl| < 2^(e_r - 1), from the largest biased exponent of
+// Row exponents: e_r with max_l |x_rl| < 2^(e_r - 2), from the largest biased exponent of
 // the row (an all-zero or padding row gets 0).  Blocks (digit row tile, part of 32).  Rows
 // with consecutive elements (cs == 1): a warp per row, lanes along it, part p taking rows
 // 4p .. 4p + 3; otherwise part 0 takes the tile, a thread per row (consecutive rows are
@@ -210,7 +215,7 @@ __global__ void __launch_bounds__(OZ_BM) k_oz_rowexp(OzSplitArgs a) {
   const int64_t r0 = (int64_t)(rtile - it.rtile0) * OZ_BM;
   auto finish = [&](int local, unsigned long long mx) {
     const int E = (int)(mx >> 52);  // biased exponent of the largest |x| (0: zero/subnormal)
-    a.ex[(int64_t)rtile * OZ_BM + local] = mx == 0 ? 0 : (E == 0 ? 1 : E) - 1021;
+    a.ex[(int64_t)rtile * OZ_BM + local] = mx == 0 ? 0 : (E == 0 ? 1 : E) - 1020;
   };
   if (it.cs == 1) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -255,13 +260,13 @@ __global__ void __launch_bounds__(OZ_BM) k_oz_split(OzSplitArgs a) {
       const int E = (int)((b >> 52) & 0x7FF);
       const long long mant = (long long)(b & 0xFFFFFFFFFFFFFull) | (E ? (1ll << 52) : 0ll);
       // F = |v| 2^(56 - e_r) as an integer: v = mant 2^(max(E,1) - 1075)
-      const int sh = (E ? E : 1) - 1019 - er;  // <= 2 by the choice of e_r
+      const int sh = (E ? E : 1) - 1019 - er;  // <= 1 by the choice of e_r: F < 2^54
       long long F = sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> -sh) : 0ll);
       if (b >> 63) F = -F;
 #pragma unroll
       for (int s = 0; s < OZ_S - 1; ++s) {
         const int q = 48 - 8 * s;
-        const long long dg = (F + (1ll << (q - 1))) >> q;  // nearest digit, in [-128, 128]
+        const long long dg = (F + (1ll << (q - 1))) >> q;  // nearest digit, in [-128, 128] ([-64, 64] for s = 0)
         F -= dg << q;
         d[h][s] = (int32_t)dg;
       }
@@ -305,6 +310,7 @@ struct OzGemmArgs {
   OzItem one;
   int ntiles;            // output tiles of all items
   int ksteps;
+  int chunk;             // K steps per exact accumulation
   double alpha, beta;
   int lower;             // write only i >= j
   int drop_stage;        // test switch (FG_OZ_TEST_DROP_STAGE): CTA 0 never issues this stage's copies
@@ -408,7 +414,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
   const int KS = g.ksteps;
-  const int nchunks = (KS + OZ_CHUNK - 1) / OZ_CHUNK;
+  const int nchunks = (KS + g.chunk - 1) / g.chunk;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -450,7 +456,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
       int gs = 0, gc = 0;
       for (int t = first; t < ntiles && ok; t = next_tile(t)) {
         for (int ks = 0; ks < KS && ok; ++ks) {
-          const int kin = ks % OZ_CHUNK;
+          const int kin = ks % g.chunk;
           const int buf = gs % OZ_NBUF;
           const int z = gc % T::NSET;  // accumulator set of this chunk
           if (kin == 0 && gc >= T::NSET &&
@@ -475,7 +481,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzGemmArgs g) {
                      db + (uint64_t)((kk - s) * (T::B_DIGIT >> 4)), T::IDESC,
                      (kin > 0 || s > (kk > OZ_S - 1 ? kk - (OZ_S - 1) : 0)) ? 1u : 0u);
           tc_commit(smem_u32(&bar_empty[buf]));
-          if (kin == OZ_CHUNK - 1 || ks == KS - 1) {
+          if (kin == g.chunk - 1 || ks == KS - 1) {
             tc_commit(smem_u32(&bar_acc_full[z]));
             ++gc;
           }
@@ -694,6 +700,7 @@ fg_status ozaki_gemm_nt(fg_ctx* ctx, cudaStream_t st, int64_t m, int64_t n, int6
   g.one = OzItem{C, c_rs, c_cs, (int)m, (int)n, 0, same ? 0 : (int)rta, (int)tiles_n, 0};
   g.ntiles = (int)(rta * tiles_n);
   g.ksteps = (int)ksteps;
+  g.chunk = k <= OZ_KEXACT ? (int)ksteps : OZ_CHUNK_STEPS;
   g.alpha = alpha;
   g.beta = beta;
   g.lower = lower ? 1 : 0;
@@ -755,6 +762,7 @@ fg_status ozaki_syrk_batch(fg_ctx* ctx, cudaStream_t st, const std::vector<OzSyr
   g.nitems = (int)hi.size();
   g.ntiles = (int)tiles;
   g.ksteps = ksteps;
+  g.chunk = ksteps;  // k <= 128 <= OZ_KEXACT
   g.alpha = -1.0;
   g.beta = 1.0;
   g.lower = 1;

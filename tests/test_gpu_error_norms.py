@@ -63,9 +63,13 @@ def test_error_norms_match_oracle(fg, ctx, order, fn):
                   boundary_fn=O.FN_SHARP_WAVE if fn == "sharp" else O.FN_LINEAR, fn_param=prm)
     o = P.error_norms(x, O.FN_SHARP_WAVE if fn == "sharp" else O.FN_LINEAR, prm)
     scale = max(o["h1_norm"], 1e-300)
+    # absolute floor: for u = x + y + z the error is the solver's (~1e-11), and a pointwise
+    # gradient error is a difference of O(1) values that two summation orders reproduce to
+    # ~nd u max|grad u| (nd <= 64 dofs, |grad u| = sqrt(3)): ~1e-14-1e-13
+    floor = 1e-13 if fn == "linear" else 1e-14
     for k, v in o.items():
         ref = scale if k in ("mean_norm",) else max(abs(v), 1e-14 * scale)
-        assert abs(d[k] - v) <= 1e-12 * max(abs(ref), 1e-30) + 1e-14, (k, d[k], v)
+        assert abs(d[k] - v) <= 1e-12 * max(abs(ref), 1e-30) + floor, (k, d[k], v)
     assert abs(np.sqrt(cells.sum()) - d["energy_norm"]) <= 1e-12 * max(d["energy_norm"], 1e-30)
     assert abs(d["energy_norm"] - d["h1_seminorm"]) <= 1e-12 * max(d["h1_seminorm"], 1e-30)
     if fn == "linear":  # u = x + y + z lies in the space: the error is the solver's
