@@ -1060,7 +1060,8 @@ static fg_status poisson_scatter(fg_system* sys, const AsmGeom& g) {
 // FG_TC_INTEGRATION: 0 the FP64-pipe and float-float kernels only; 1 Poisson element
 // matrices on the tensor cores where FP64 integration is asked for; 2 (default) also where
 // float-float is (FG_FAST_INTEGRATION): the tensor-core matrices are FP64-accurate and, on
-// GB300, faster than both (128^3 Q2: 66 ms per assembly against 186 ms FP64, 84 ms float-float)
+// GB300, faster than both (128^3 Q2: 61 / 48 ms per assembly against 186 ms FP64, 84 ms
+// float-float)
 static int tc_integration_mode() {
   const char* e = getenv("FG_TC_INTEGRATION");
   const int v = e ? atoi(e) : 2;
