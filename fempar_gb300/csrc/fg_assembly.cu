@@ -947,9 +947,11 @@ static fg_status launch_scatter_stencil(fg_system* sys, const AsmGeom& g) {
   fg_ctx* ctx = sp->mesh->ctx;
   constexpr int W = 8;
   const size_t smem = scatter_stencil_smem(sp);
-  // scalar Q1/Q2 rows fit three blocks per SM in 80 registers without spills (128^3 Q2: the
-  // whole assembly 73.2 -> 66.1 ms, identical results); Q3 and vector rows would spill
-  constexpr int MINB = (NC == 1 && P <= 2) ? 3 : 1;
+  // scalar Q1/Q2 rows: four blocks per SM (64 registers, a 4-byte spill; the shared slices
+  // take 4 x 34 KB).  The gather is latency-bound: at 128^3 Q2 the row gather takes ~22.5 ms
+  // at two blocks, 17.9 ms at three, ~14.5 ms at four (identical results: only the register
+  // allocation changes).  Q3 and vector rows would spill heavily.
+  constexpr int MINB = (NC == 1 && P <= 2) ? 4 : 1;
   auto kern = k_scatter_stencil<P, NC, W, MINB>;
   FG_CUDA_TRY(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (sp->st_nslices > 0) {
