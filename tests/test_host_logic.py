@@ -28,6 +28,25 @@ def test_footprint_grows_with_problem_size():
     assert 4 * small < big < 10 * small  # ~8x the data plus a fixed per-request reserve
 
 
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_footprint_covers_the_tensor_core_assembly_scratch(order):
+    """A Poisson request is assembled with its element matrices on the tensor cores: the
+    admission footprint must cover, besides the element matrices and vectors, the product's
+    scratch per cell -- the 6 NQ geometric factors, the packed upper triangle and the 7 bf16
+    digits of the factors (K padded to 16) -- and the shared table T."""
+    import math
+    from fempar_gb300 import build, serving as S
+    build.build()
+    n = (24, 20, 16)
+    b, nf = S.footprint(kind=S.POISSON, n=n, order=order)
+    ncells = n[0] * n[1] * n[2]
+    nd = nq = (order + 1) ** 3
+    K, npair = 6 * nq, nd * (nd + 1) // 2
+    elm = ncells * (nd * nd + nd) * 8
+    tc = ncells * (K * 8 + npair * 8 + math.ceil(K / 16) * 16 * 7 * 2) + npair * K * 8
+    assert b >= elm + tc
+
+
 def test_server_and_context_without_device_report_status():
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():
