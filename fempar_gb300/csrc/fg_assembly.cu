@@ -10,8 +10,13 @@
 // reference's element matrix is exactly symmetric), the element vector, and the
 // strong-Dirichlet lifting elvec -= elmat(:,j) g_j in column order
 // (sbm_fe_cell_iterator.i90:1610-1637).  Element matrices go to an HBM buffer.
-// GB300's FP64 rate (about 1.25 TFLOP/s) makes this stage FP64-bound; the buffer's
-// extra HBM traffic costs a few milliseconds at cfg2 size.
+// GB300's FP64 rate (about 1 TFLOP/s) makes this stage FP64-bound; the buffer's
+// extra HBM traffic costs a few milliseconds at the 128^3 Q2 size.
+//
+// Stage 1 by default for Poisson (structured and unstructured, not dG): the element
+// matrices of all cells as one emulated-FP64 tensor-core product of the cells' geometric
+// factors with a table shared by all cells (k_poisson_geom or k_poisson_geom_ff, then
+// ozaki_gemm_nt, then k_poisson_unpack with the lifting; see the comment at PoissonTC).
 //
 // Stage 2, k_scatter_rows<P>: one warp per free row.  The row's node sits in at most
 // 8 cells; they are visited in increasing cell index, so every entry is summed in the
